@@ -1,0 +1,247 @@
+/*
+ * wavegpu.h — C ABI of libwavegpu.so, the sm_103a (GB300) implementation of the
+ * explicit leapfrog wave-equation stepper of nilsberglund-orleans/YouTube-simulations
+ * (`wave_billiard`) and the energy diagnostics of `wave_energy`.
+ *
+ * Plain C types only: pointers, sizes, int32 status codes.  No CUDA or torch type
+ * appears in a signature; a CUDA stream is passed as `void *` (cudaStream_t).
+ *
+ * Two surfaces:
+ *   1. Drop-in: the reference's own functions with the reference's argument meaning,
+ *      row-pointer field layout (`double *phi[NX]`, each row NY values, j contiguous)
+ *      and compile-time configuration turned into a runtime wg_params.  The header
+ *      wavegpu_dropin.h builds that wg_params from the reference's macros.
+ *   2. Native handle API: scenes resident in HBM, FP64 or FP32, runtime sizes,
+ *      batches of uneven scenes, and a serving loop.
+ *
+ * Every function returns WG_OK (0) or a negative wg_status; wg_last_error() gives a
+ * thread-local message for the last failure of the calling thread.
+ */
+#ifndef WAVEGPU_H
+#define WAVEGPU_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ------------------------------------------------------------------------- */
+/* Status codes                                                               */
+/* ------------------------------------------------------------------------- */
+typedef int32_t wg_status;
+enum {
+    WG_OK = 0,
+    WG_ERR_INVALID = -1,   /* bad argument or size */
+    WG_ERR_CUDA = -2,      /* a CUDA runtime call failed */
+    WG_ERR_NOMEM = -3,     /* device or pinned allocation failed */
+    WG_ERR_BUDGET = -4,    /* admission refused: HBM budget exceeded */
+    WG_ERR_STATE = -5,     /* call not valid in the object's current state */
+    WG_ERR_TIMEOUT = -6,   /* a bounded device/host wait gave up */
+    WG_ERR_NONFINITE = -7, /* a field holds NaN/Inf (blow-up detector) */
+    WG_ERR_NOTFOUND = -8   /* unknown scene/request id */
+};
+
+/* ------------------------------------------------------------------------- */
+/* Configuration: the reference's compile-time macros as a runtime struct.    */
+/* Names follow the macros of wave_billiard.c:46-285 and global_pdes.c.       */
+/* ------------------------------------------------------------------------- */
+enum { WG_BC_DIRICHLET = 0, WG_BC_PERIODIC = 1, WG_BC_ABSORBING = 2, WG_BC_VPER_HABS = 3 };
+
+/* OSCILLATION_SCHEDULE values (global_pdes.c:282-296) */
+enum {
+    WG_OSC_PERIODIC = 0, WG_OSC_SLOWING = 1, WG_OSC_WAVE_PACKET = 2, WG_OSC_WAVE_PACKETS = 21,
+    WG_OSC_CHIRP = 3, WG_OSC_BEAM = 4, WG_OSC_BEAM_GAUSSIAN = 41, WG_OSC_BEAM_SINE = 42,
+    WG_OSC_BEAM_SINE_DECREASING = 43, WG_OSC_BEAM_SINE_CHIRP = 44, WG_OSC_BEAM_TWOPERIODS = 5,
+    WG_OSC_BEAM_SINE_TWOPERIODS = 51, WG_OSC_TWO_WAVES = 6, WG_OSC_TWO_WAVES_ADDED = 61,
+    WG_OSC_TWOFREQ_TOPBOT = 7
+};
+
+enum { WG_FP64 = 0, WG_FP32 = 1 };
+
+/* Coefficient storage of a native scene.
+ *  WG_COEF_MASK : tcc/tgamma/tc follow the mask bit exactly as init_ior_2d's constant
+ *                 branch builds them (sub_wave.c:12983-13002): inside COURANT^2/GAMMA/
+ *                 COURANT, outside (TWOSPEEDS) COURANTB^2/GAMMAB/COURANTB.  0 bytes/cell.
+ *  WG_COEF_TABLE: a spatially varying tcc table is kept on the device (S bytes/cell);
+ *                 tgamma is a table too unless it is uniform; tc is kept for the four
+ *                 boundary lines only (it is read nowhere else). */
+enum { WG_COEF_MASK = 0, WG_COEF_TABLE = 1 };
+
+typedef struct wg_params {
+    int32_t nx, ny;                 /* NX, NY: grid size, field[i][j], j contiguous */
+    int32_t b_cond;                 /* B_COND (WG_BC_*) */
+    int32_t twospeeds;              /* TWOSPEEDS */
+    int32_t bc_neumann;             /* BC_NEUMANN */
+    int32_t oscillate_left;         /* OSCILLATE_LEFT */
+    int32_t oscillate_topbot;       /* OSCILLATE_TOPBOT */
+    int32_t oscillation_schedule;   /* OSCILLATION_SCHEDULE (WG_OSC_*) */
+    int32_t floor_clamp;            /* FLOOR */
+    int32_t src_on;                 /* project point source on/off (see src_*) */
+    int32_t src_i, src_j;           /* point-source cell */
+    double xmin, xmax, ymin, ymax;  /* XMIN, XMAX, YMIN, YMAX */
+    double courant, courantb;       /* COURANT, COURANTB */
+    double gamma, gammab;           /* GAMMA, GAMMAB (used by WG_COEF_MASK) */
+    double kappa, kappa_sides, kappa_topbot;  /* KAPPA, KAPPA_SIDES, KAPPA_TOPBOT */
+    double gamma_sides, gamma_topbot;         /* GAMMA_SIDES, GAMMA_TOPBOT */
+    double omega, omega_b, amplitude, damping, achirp;       /* OMEGA, OMEGA_B, AMPLITUDE, DAMPING, ACHIRP */
+    double oscil_ymax, oscil_ymid, oscil_left_yshift;        /* OSCIL_YMAX, OSCIL_YMID, OSCIL_LEFT_YSHIFT */
+    double initial_variance, initial_shift, wave_packet_shift; /* INITIAL_VARIANCE, INITIAL_SHIFT, WAVE_PACKET_SHIFT */
+    double vmax;                    /* VMAX (FLOOR clamp) */
+    double e_scale;                 /* E_SCALE (energy) */
+    /* Point source of the project (not in the reference): after update number t
+     * (t counts from 1), phi_out[src_i][src_j] += src_amp * sin(2*pi*t/src_period). */
+    double src_amp, src_period;
+} wg_params;
+
+/* Neumann boundary record, binary-identical to t_neumann_bc (global_pdes.c:518-528). */
+typedef struct wg_neumann_bc {
+    double nx, ny;
+    int16_t signx1, signy1;
+    int16_t signx2, signy2;
+    int32_t nbi1, nbj1, nbk1;
+    int32_t nbi2, nbj2, nbk2;
+    int32_t i, j, k;
+    int16_t top;
+    int16_t active;
+} wg_neumann_bc;
+
+/* Fills *p with the macro values of wave_billiard.c:46-285 for the fields it shares
+ * with wg_params, sized nx x ny, box [-2,2]x[-1.125,1.125]. */
+void wg_params_default(wg_params *p, int32_t nx, int32_t ny);
+
+const char *wg_last_error(void);
+const char *wg_status_string(wg_status s);
+int32_t wg_abi_version(void);
+
+/* ------------------------------------------------------------------------- */
+/* 1. Drop-in surface (row-pointer layout, FP64, reference semantics)          */
+/* ------------------------------------------------------------------------- */
+
+/* Sets NX, NY and the macros used by the drop-in calls below.  Replaces the
+ * compile-time #defines of wave_billiard.c:46-285; wavegpu_dropin.h calls it. */
+wg_status wg_dropin_configure(const wg_params *p);
+
+/* Drop-in transfer modes.
+ *  WG_DROPIN_STRICT  : every call copies the fields in, steps on the GPU and copies
+ *                      them back, so host arrays are current after each call.
+ *  WG_DROPIN_RESIDENT: fields stay in HBM between calls (matched by the row-pointer
+ *                      arrays' identity); wg_dropin_sync() copies them back and
+ *                      wg_dropin_invalidate() forces a fresh upload after host edits. */
+enum { WG_DROPIN_STRICT = 0, WG_DROPIN_RESIDENT = 1 };
+wg_status wg_dropin_set_mode(int32_t mode);
+wg_status wg_dropin_sync(void);
+wg_status wg_dropin_invalidate(void);
+/* Step counter of the drop-in (the reference's `static long time`, wave_billiard.c:310). */
+wg_status wg_dropin_get_time(int64_t *t);
+wg_status wg_dropin_set_time(int64_t t);
+
+/* Replaces evolve_wave_half (wave_billiard.c:302-610): one leapfrog update,
+ * phi_out <- F(phi_in, psi_in).  Arrays are NX row pointers of NY values each. */
+wg_status wg_evolve_wave_half(double **phi_in, double **psi_in, double **phi_out,
+                              int16_t **xy_in, double **tcc, double **tc, double **tgamma,
+                              const wg_neumann_bc *neumann_bc, int32_t n_neumann);
+
+/* Replaces evolve_wave (wave_billiard.c:613-631): three updates with the
+ * phi -> tmp -> psi -> phi buffer rotation. */
+wg_status wg_evolve_wave(double **phi, double **psi, double **tmp,
+                         int16_t **xy_in, double **tcc, double **tc, double **tgamma,
+                         const wg_neumann_bc *neumann_bc, int32_t n_neumann);
+
+/* Replaces the wave_energy variant (wave_energy.c:662-925): the stepper on the half
+ * domain j < NY/2 with coefficient tables built from the mask and the macros. */
+wg_status wg_evolve_wave_half_energy(double **phi_in, double **psi_in, double **phi_out,
+                                     int16_t **xy_in);
+wg_status wg_evolve_wave_energy(double **phi, double **psi, double **tmp, int16_t **xy_in);
+
+/* compute_energy (wave_common.c:453-472) for one cell. */
+wg_status wg_compute_energy(double **phi, double **psi, int16_t **xy_in,
+                            int32_t i, int32_t j, double *out);
+/* compute_energy_x for every column i (wave_energy.c:292-302): out[i] = sum_{j<NY/2} E(i,j). */
+wg_status wg_compute_energy_x_all(double **phi, double **psi, int16_t **xy_in, double *out);
+/* compute_energy_tblr (sub_wave_comp.c:1752-1858) with the box limits given. */
+wg_status wg_compute_energy_tblr(double **phi, double **psi, int16_t **xy_in,
+                                 int32_t ileft, int32_t iright, double energies[6]);
+
+/* ------------------------------------------------------------------------- */
+/* 2. Native handle API: resident scenes                                       */
+/* ------------------------------------------------------------------------- */
+typedef struct wg_scene wg_scene;
+
+/* Creates a scene with device buffers for phi/psi, the packed mask and coefficients.
+ * precision: WG_FP64 or WG_FP32.  coef_mode: WG_COEF_MASK or WG_COEF_TABLE.
+ * stream: cudaStream_t to run on (NULL = a stream owned by the scene). */
+wg_status wg_scene_create(const wg_params *p, int32_t precision, int32_t coef_mode,
+                          void *stream, wg_scene **out);
+wg_status wg_scene_destroy(wg_scene *s);
+/* Device bytes the scene holds (fields, mask, tables, scratch). */
+wg_status wg_scene_bytes(const wg_params *p, int32_t precision, int32_t coef_mode, size_t *bytes);
+
+/* Uploads flat [nx][ny] FP64 host arrays (j contiguous).  xy_in is the reference's
+ * short mask.  tcc/tc/tgamma may be NULL in WG_COEF_MASK mode.  Values are rounded
+ * to the scene precision on the device. */
+wg_status wg_scene_upload(wg_scene *s, const double *phi, const double *psi, const int16_t *xy_in,
+                          const double *tcc, const double *tc, const double *tgamma);
+/* Uploads only phi/psi (the state), from FP64 or from the scene's own precision. */
+wg_status wg_scene_upload_state(wg_scene *s, const void *phi, const void *psi, int32_t host_precision);
+wg_status wg_scene_set_neumann(wg_scene *s, const wg_neumann_bc *recs, int32_t n);
+/* Advances nsteps leapfrog updates (one kernel pass per temporal block). */
+wg_status wg_scene_step(wg_scene *s, int32_t nsteps);
+/* Copies phi (time t) and psi (time t-1) to flat host arrays in FP64 or the scene's
+ * precision.  Either pointer may be NULL. */
+wg_status wg_scene_download(wg_scene *s, void *phi, void *psi, int32_t host_precision);
+/* Energy diagnostics with FP64 compensated (Neumaier) sums.
+ *  total   : sum of compute_energy over all cells (may be NULL)
+ *  columns : nx values, sum over j < ny/2 (compute_energy_x), may be NULL
+ *  boxes   : 6 values (compute_energy_tblr) for ileft/iright, may be NULL */
+wg_status wg_scene_energy(wg_scene *s, double *total, double *columns,
+                          int32_t ileft, int32_t iright, double *boxes);
+wg_status wg_scene_get_time(wg_scene *s, int64_t *t);
+wg_status wg_scene_set_time(wg_scene *s, int64_t t);
+wg_status wg_scene_sync(wg_scene *s);
+/* Temporal-block depth (updates per kernel pass) and tile shape; 0 = autotuned. */
+wg_status wg_scene_set_blocking(wg_scene *s, int32_t k, int32_t tile_i, int32_t tile_j);
+wg_status wg_scene_get_blocking(wg_scene *s, int32_t *k, int32_t *tile_i, int32_t *tile_j);
+/* Number of kernel launches this library issued for the scene so far. */
+wg_status wg_scene_launch_count(wg_scene *s, int64_t *n);
+/* Blow-up detector: *bad = number of non-finite phi values (0 = healthy). */
+wg_status wg_scene_check_finite(wg_scene *s, int64_t *bad);
+
+/* Turbo-style frame: P_AMPLITUDE colour map of phi (wave_common.c:1053-1065,
+ * colors_waves.c:3-16,161-218, colormaps.c:2449-2482) downsampled by `size`,
+ * written as rows of RGB8 (nx/size x ny/size x 3, row = j/size, bottom row first).
+ * lut: the caller's 256x3 byte palette (the reference's turbo_srgb_bytes). */
+typedef struct wg_frame_params {
+    int32_t size;            /* downsampling (draw_wave_highres_palette's size=2) */
+    int32_t fade;            /* apply fade_value */
+    double vshift, vscale;   /* VSHIFT_AMPLITUDE, VSCALE_AMPLITUDE */
+    double slope, color_range, scale; /* SLOPE, COLOR_RANGE, scale */
+    double fade_value;
+} wg_frame_params;
+wg_status wg_scene_frame_rgb8(wg_scene *s, const wg_frame_params *fp, const uint8_t *lut,
+                              uint8_t *rgb_host, void *rgb_device);
+
+/* ------------------------------------------------------------------------- */
+/* 3. Batches of uneven scenes: one persistent launch over a tile work queue   */
+/* ------------------------------------------------------------------------- */
+typedef struct wg_batch wg_batch;
+wg_status wg_batch_create(int32_t precision, void *stream, wg_batch **out);
+wg_status wg_batch_destroy(wg_batch *b);
+/* Adds a scene (WG_COEF_MASK only) to the batch; *slot gets its index. */
+wg_status wg_batch_add(wg_batch *b, const wg_params *p, const double *phi, const double *psi,
+                       const int16_t *xy_in, int32_t *slot);
+/* Removes a scene; its device memory is returned to the batch's pool. */
+wg_status wg_batch_remove(wg_batch *b, int32_t slot);
+/* Advances every active scene by nsteps updates: one persistent kernel per
+ * temporal block, the launches of a frame recorded once as a CUDA graph. */
+wg_status wg_batch_step(wg_batch *b, int32_t nsteps);
+wg_status wg_batch_download(wg_batch *b, int32_t slot, double *phi, double *psi);
+wg_status wg_batch_energy(wg_batch *b, int32_t slot, double *total);
+wg_status wg_batch_count(wg_batch *b, int32_t *n_active, int64_t *cells);
+wg_status wg_batch_launch_count(wg_batch *b, int64_t *n);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* WAVEGPU_H */

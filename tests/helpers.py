@@ -1,0 +1,56 @@
+"""Shared test inputs: deterministic seeded scenes for every compiled-reference variant."""
+import numpy as np
+
+import ref_variants
+from youtube_simulations_gb300 import params as P
+from youtube_simulations_gb300 import scenes
+
+
+def params_of(variant, **over):
+    d = ref_variants.params_dict(variant)
+    d.update(over)
+    nx, ny = d.pop("nx"), d.pop("ny")
+    return P.make_params(nx, ny, **d)
+
+
+def variant_inputs(variant, seed=1, noisy_tmp=True, smooth=False):
+    """(params, fields dict, xy, nbc) for a variant: its mask, spatially varying
+    tables, a pulse plus noise in phi/psi, and (optionally) noise in tmp so that
+    cells the stepper must not write are visible."""
+    m = ref_variants.VARIANTS[variant]["macros"]
+    p = params_of(variant)
+    rng = np.random.default_rng(seed)
+    dom = m["B_DOMAIN"]
+    if dom == 20:
+        circ = scenes.seeded_discs(rng, 6, 0.1, 0.3)
+        xy = scenes.mask(p, dom, circles=circ)
+    else:
+        xy = scenes.mask(p, dom, lam=m["LAMBDA"], npoly=m["NPOLY"], apoly=m["APOLY"])
+    nbc = None
+    if m["BC_NEUMANN"]:
+        import oracle
+        xy, nbc = oracle.init_neumann(p, dom, m["LAMBDA"], xy, npoly=m["NPOLY"], apoly=m["APOLY"])
+    n = p.nx * p.ny
+    tcc, tc, tg = scenes.tables(p, xy)
+    tcc = tcc * (1.0 + 0.2 * rng.random(n))
+    tc = tc * (1.0 + 0.2 * rng.random(n))
+    tg = tg + 1e-3 * rng.random(n)
+    if p.nx > 4 and p.ny > 4:
+        inside = np.argwhere(xy.reshape(p.nx, p.ny) > 0)
+        ci, cj = inside[len(inside) // 2] if len(inside) else (p.nx // 2, p.ny // 2)
+    else:
+        ci, cj = p.nx // 2, p.ny // 2
+    x, y = scenes.grid_xy(p)
+    phi = scenes.pulse(p, np.ones(n, np.int16), x[ci], y[cj], variance=0.15 ** 2)
+    if not smooth:
+        phi = phi + 0.05 * rng.standard_normal(n)
+    psi = phi * 0.98 + (0.0 if smooth else 0.01 * rng.standard_normal(n))
+    tmp = 0.3 * rng.standard_normal(n) if noisy_tmp else np.zeros(n)
+    fields = dict(phi=phi, psi=psi, tmp=tmp, tcc=tcc, tc=tc, tgamma=tg)
+    return p, fields, xy, nbc
+
+
+def rel_err(a, b):
+    a, b = np.asarray(a, np.float64), np.asarray(b, np.float64)
+    scale = max(np.max(np.abs(b)), 1e-300)
+    return float(np.max(np.abs(a - b)) / scale)
