@@ -1,0 +1,339 @@
+#!/usr/bin/env python3
+"""Benchmark of the GB300 wave stepper on the single-grid workload.
+
+Workload (one GPU): 3840x2160 grid, 64 seeded discs of refractive index 1.5
+(TWOSPEEDS, COURANTB = COURANT/1.5) through the tcc table, absorbing boundary,
+GAMMA = 1e-4, an oscillating point source of amplitude 0.05 and seeded period in
+[20, 60] updates, energy reported every 100 updates with FP64 compensated sums.
+One bench step = 100 leapfrog updates + one energy report; 100 steps = the full 10^4
+updates.  `value` is the FP32 form in Gcell-updates/s (all cells count), with inputs
+resident in HBM; `e2e` is the same metric through the C ABI with host buffers (the
+state is copied in and out every step); the plain FP64 form is reported beside it.
+
+--impl reference times the reference's own OpenMP CPU stepper (compiled headlessly
+from its sources into oracle/_ref) on this machine's host cores.
+"""
+import argparse
+import json
+import math
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+from pathlib import Path
+
+ROOT = Path(__file__).resolve().parent
+NX, NY, UPDATES_PER_STEP = 3840, 2160, 100
+METRIC = "Gcell-updates/s"
+CELLS = NX * NY
+
+
+def _package():
+    import importlib.util
+    name = "youtube_simulations_gb300"
+    if name not in sys.modules:
+        d = ROOT / "youtube-simulations_gb300"
+        spec = importlib.util.spec_from_file_location(name, d / "__init__.py", submodule_search_locations=[str(d)])
+        mod = importlib.util.module_from_spec(spec)
+        sys.modules[name] = mod
+        spec.loader.exec_module(mod)
+    return sys.modules[name]
+
+
+def bytes_per_cell_update(precision, coef):
+    """Algorithmic bytes of one cell update (single-step compulsory traffic):
+    read phi(t), psi(t-1), write phi(t+1), the 1-bit mask, and each spatially varying
+    coefficient table (tcc here; tgamma is uniform, tc is read on the boundary only)."""
+    s = 4 if precision == "fp32" else 8
+    return 3 * s + (s if coef == "table" else 0) + 1.0 / 8.0
+
+
+class Clocks:
+    """nvidia-smi clock/throttle samples during the timed region."""
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index):
+        self.f = tempfile.NamedTemporaryFile("w+", suffix=".csv", delete=False)
+        self.gpu = gpu_index
+        self.p = None
+
+    def start(self):
+        try:
+            self.p = subprocess.Popen(["nvidia-smi", f"--id={self.gpu}", f"--query-gpu={self.Q}",
+                                       "--format=csv,noheader,nounits", "-lms", "200"],
+                                      stdout=self.f, stderr=subprocess.DEVNULL)
+        except (FileNotFoundError, OSError):
+            self.p = None
+
+    def stop(self):
+        if self.p is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.p.terminate()
+        self.p.wait(timeout=10)
+        self.f.flush()
+        rows = []
+        for line in Path(self.f.name).read_text().splitlines():
+            parts = [x.strip() for x in line.split(",")]
+            if len(parts) >= 9:
+                rows.append(parts)
+        os.unlink(self.f.name)
+        if not rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["no samples"]}
+        sm = [float(r[1]) for r in rows if r[1].replace(".", "").isdigit()]
+        mx = [float(r[2]) for r in rows if r[2].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[k] for r in rows for k in range(4) if r[5 + k].lower().startswith("active")})
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": reasons, "samples": len(rows)}
+
+
+def dist_env():
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return rank, world, local
+
+
+# ---------------------------------------------------------------------------
+# Reference arm: the reference's own CPU stepper
+# ---------------------------------------------------------------------------
+def reference_sample(updates, threads=None):
+    sys.path.insert(0, str(ROOT / "oracle"))
+    import refio
+    from youtube_simulations_gb300 import scenes
+    sc = scenes.config2(seed=0, nx=NX, ny=NY)
+    m = sc.meta
+    src = (m["source"][0], m["source"][1], 0.05, m["period"])
+    el, _, th = refio.time_reference("c2", NX, NY, updates, m["discs"], m["centre"], src=src, threads=threads)
+    return el, th
+
+
+def run_reference(args):
+    rank, world, _ = dist_env()
+    if rank != 0:
+        return 0
+    sys.path.insert(0, str(ROOT / "oracle"))
+    import refio
+    if not refio.available("c2"):
+        print(json.dumps({"impl": "reference", "unavailable": "compiled reference (oracle/_ref) absent: "
+                          "run oracle/build_ref.py where the reference sources are present"}))
+        return 0
+    threads = os.cpu_count()
+    upd = args.ref_updates
+    for _ in range(args.warmup):
+        reference_sample(3, threads)
+    times = []
+    for _ in range(args.steps):
+        el, th = reference_sample(upd, threads)
+        times.append(el)
+    total = sum(times)
+    value = CELLS * upd * len(times) / total / 1e9
+    line = {"metric": METRIC, "value": value, "unit": METRIC, "n_gpus": args.gpus, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": 1e3 * total / len(times), "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "impl": "reference",
+            "config": {"workload": f"single grid {NX}x{NY}, 64 discs n=1.5, absorbing, point source",
+                       "updates_per_step": upd, "parallelism": f"openmp x{th}"},
+            "cpu_baseline": {"value": value, "unit": METRIC, "cores": th, "kind": "reference",
+                             "sample": f"{upd} updates of the {NX}x{NY} grid per step (stepping loop only)"},
+            "e2e": {"value": value, "unit": METRIC, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line))
+    return 0
+
+
+# ---------------------------------------------------------------------------
+# Our arm
+# ---------------------------------------------------------------------------
+def run_ours(args):
+    import torch
+    _package()
+    from youtube_simulations_gb300 import params as P
+    from youtube_simulations_gb300 import scenes
+    from youtube_simulations_gb300 import wavegpu as W
+
+    rank, world, local = dist_env()
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    # a stream of our own (torch's default stream has handle 0, which the library
+    # would read as "no stream"); torch work and the scenes are ordered on it
+    stream = torch.cuda.Stream(dev)
+    torch.cuda.set_stream(stream)
+
+    def barrier():
+        if world > 1:
+            torch.distributed.barrier()
+        torch.cuda.synchronize(dev)
+
+    # replicas: every rank advances its own instance of the workload (seed = rank)
+    sc = scenes.config2(seed=rank, nx=NX, ny=NY)
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)  # > L2 (126 MB)
+
+    def make_scene(prec):
+        s = W.Scene(sc.params, P.FP32 if prec == "fp32" else P.FP64, P.COEF_TABLE, stream=stream.cuda_stream)
+        s.upload(sc.phi, sc.psi, sc.xy, sc.tcc, sc.tc, sc.tgamma)
+        if args.k:
+            s.set_blocking(args.k)
+        return s
+
+    def timed(s, steps, warmup):
+        for _ in range(warmup):
+            s.step(UPDATES_PER_STEP)
+            s.total_energy()
+        barrier()
+        l0 = s.launches()
+        step_ms, energy_ms = 0.0, 0.0
+        clocks = Clocks(local)
+        clocks.start()
+        wall0 = time.perf_counter()
+        for _ in range(steps):
+            flush.zero_()
+            e0, e1, e2 = (torch.cuda.Event(enable_timing=True) for _ in range(3))
+            e0.record(stream)
+            s.step(UPDATES_PER_STEP)
+            e1.record(stream)
+            s.total_energy()
+            e2.record(stream)
+            e2.synchronize()
+            step_ms += e0.elapsed_time(e1)
+            energy_ms += e1.elapsed_time(e2)
+        barrier()
+        wall = time.perf_counter() - wall0
+        ck = clocks.stop()
+        return step_ms, energy_ms, wall, s.launches() - l0, ck
+
+    results = {}
+    for prec in (["fp32", "fp64"] if not args.fp32_only else ["fp32"]):
+        s = make_scene(prec)
+        step_ms, energy_ms, wall, launches, ck = timed(s, args.steps, args.warmup)
+        k, ti, tj = s.blocking()
+        e_final = s.total_energy()
+        s.close()
+        t_ms = step_ms + energy_ms
+        if world > 1:
+            tt = torch.tensor([t_ms], device=dev)
+            torch.distributed.all_reduce(tt, op=torch.distributed.ReduceOp.MAX)
+            t_ms = float(tt.item())
+        updates = args.steps * UPDATES_PER_STEP
+        kernel_launches_per_step = UPDATES_PER_STEP / max(k, 1)
+        per_launch_s = step_ms / 1e3 / (args.steps * kernel_launches_per_step)
+        algo = bytes_per_cell_update(prec, "table") * CELLS * max(k, 1)
+        results[prec] = dict(value=world * CELLS * updates / (t_ms / 1e3) / 1e9, ms=t_ms / args.steps,
+                             step_ms=step_ms, energy_ms=energy_ms, wall=wall, launches=launches, clocks=ck,
+                             blocking=(k, ti, tj), achieved_gbs=algo / per_launch_s / 1e9,
+                             bytes_per_update=bytes_per_cell_update(prec, "table"), energy=e_final)
+
+    # end to end through the C ABI with pinned host buffers (FP32)
+    s = make_scene("fp32")
+    h_phi = torch.empty(CELLS, dtype=torch.float32).pin_memory()
+    h_psi = torch.empty(CELLS, dtype=torch.float32).pin_memory()
+    h_phi.copy_(torch.from_numpy(sc.phi.astype("float32")))
+    h_psi.copy_(torch.from_numpy(sc.psi.astype("float32")))
+    lib = W.lib()
+    for _ in range(max(1, args.warmup)):
+        W.check(lib.wg_scene_upload_state(s.h, h_phi.data_ptr(), h_psi.data_ptr(), P.FP32))
+        s.step(UPDATES_PER_STEP)
+        s.total_energy()
+        W.check(lib.wg_scene_download(s.h, h_phi.data_ptr(), h_psi.data_ptr(), P.FP32))
+    barrier()
+    e2e_ms = 0.0
+    for _ in range(args.steps):
+        flush.zero_()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        W.check(lib.wg_scene_upload_state(s.h, h_phi.data_ptr(), h_psi.data_ptr(), P.FP32))
+        s.step(UPDATES_PER_STEP)
+        s.total_energy()
+        W.check(lib.wg_scene_download(s.h, h_phi.data_ptr(), h_psi.data_ptr(), P.FP32))
+        e1.record(stream)
+        e1.synchronize()
+        e2e_ms += e0.elapsed_time(e1)
+    s.close()
+    barrier()
+    if world > 1:
+        tt = torch.tensor([e2e_ms], device=dev)
+        torch.distributed.all_reduce(tt, op=torch.distributed.ReduceOp.MAX)
+        e2e_ms = float(tt.item())
+    e2e_value = world * CELLS * args.steps * UPDATES_PER_STEP / (e2e_ms / 1e3) / 1e9
+
+    if rank != 0:
+        return 0
+    peaks = {}
+    pk = ROOT / "MEASURED_PEAKS.json"
+    if pk.exists():
+        peaks = json.loads(pk.read_text())
+    hbm = peaks.get("hbm_gbs", 6800.0)
+    peak_src = "measured" if "hbm_gbs" in peaks else "fallback"
+    r32, r64 = results["fp32"], results.get("fp64")
+    traffic = None
+    tf = ROOT / "profiles" / "traffic.json"
+    if tf.exists():
+        traffic = json.loads(tf.read_text()).get(f"fp32_k{r32['blocking'][0]}")
+    cpu = None
+    if not args.no_cpu_baseline:
+        try:
+            upd = 30
+            el, th = reference_sample(upd)
+            if el < 3.0:
+                upd = int(min(600, max(30, upd * 10.0 / max(el, 1e-3))))
+                el, th = reference_sample(upd)
+            cpu = {"value": CELLS * upd / el / 1e9, "unit": METRIC, "cores": th, "kind": "reference",
+                   "sample": f"{upd} updates of the {NX}x{NY} grid (reference evolve_wave_half, OpenMP, stepping loop only)"}
+        except Exception as exc:  # the compiled reference is absent on this machine
+            cpu = {"value": None, "unit": METRIC, "cores": 0, "kind": "reference", "sample": f"unavailable: {exc}"}
+    line = {
+        "metric": METRIC, "value": r32["value"], "unit": METRIC, "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": r32["ms"], "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded discs, pulse and source)",
+        "config": {"workload": f"single grid {NX}x{NY}, 64 discs n=1.5 via tcc table, absorbing, GAMMA 1e-4, "
+                               f"point source; step = {UPDATES_PER_STEP} updates + FP64 energy report",
+                   "updates_per_step": UPDATES_PER_STEP, "cells": CELLS, "parallelism": f"replicas x{world}",
+                   "l2": "flushed (256 MB write) before every timed step",
+                   "temporal_block": r32["blocking"][0], "tile": list(r32["blocking"][1:])},
+        "roofline": {"bound": "hbm", "achieved": r32["achieved_gbs"], "peak": hbm, "unit": "GB/s",
+                     "frac": r32["achieved_gbs"] / hbm, "traffic": traffic,
+                     "peak_source": f"{peak_src} hbm_gbs",
+                     "algorithmic_bytes_per_cell_update": r32["bytes_per_update"],
+                     "kernel": "k_step_fast<float>" if r32["blocking"][0] <= 1 else "k_step_tb<float>"},
+        "cpu_baseline": cpu,
+        "e2e": {"value": e2e_value, "unit": METRIC, "h2d_bytes_per_step": 2 * CELLS * 4,
+                "d2h_bytes_per_step": 2 * CELLS * 4 + 8},
+        "gpu_launches": int(r32["launches"]),
+        "clocks": r32["clocks"],
+    }
+    if r64:
+        line["fp64"] = {"value": r64["value"], "ms_per_step": r64["ms"], "achieved_gbs": r64["achieved_gbs"],
+                        "frac": r64["achieved_gbs"] / hbm, "temporal_block": r64["blocking"][0],
+                        "gpu_launches": int(r64["launches"]), "clocks": r64["clocks"],
+                        "bytes_per_cell_update": r64["bytes_per_update"]}
+    line["energy_final"] = {"fp32": r32["energy"], "fp64": r64["energy"] if r64 else None}
+    print(json.dumps(line))
+    return 0
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--k", type=int, default=0, help="temporal block depth (0 = autotuned)")
+    ap.add_argument("--fp32-only", action="store_true")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--ref-updates", type=int, default=20, help="updates per reference step")
+    args = ap.parse_args()
+    if args.warmup < 3:
+        print("warning: fewer than 3 warm-up steps", file=sys.stderr)
+    if args.impl == "reference":
+        return run_reference(args)
+    return run_ours(args)
+
+
+if __name__ == "__main__":
+    sys.exit(main())

@@ -208,16 +208,22 @@ wg_status wg_scene_launch_count(wg_scene *s, int64_t *n);
 /* Blow-up detector: *bad = number of non-finite phi values (0 = healthy). */
 wg_status wg_scene_check_finite(wg_scene *s, int64_t *bad);
 
-/* Turbo-style frame: P_AMPLITUDE colour map of phi (wave_common.c:1053-1065,
- * colors_waves.c:3-16,161-218, colormaps.c:2449-2482) downsampled by `size`,
- * written as rows of RGB8 (nx/size x ny/size x 3, row = j/size, bottom row first).
- * lut: the caller's 256x3 byte palette (the reference's turbo_srgb_bytes). */
+/* Colour-mapped frame: the P_AMPLITUDE colour map of phi (wave_common.c:1053-1065,
+ * 1750-1848; colors_waves.c:3-16,161-218; colormaps.c:2449-2482) at every size-th
+ * cell, as an RGB8 image of (ny/size) rows x (nx/size) columns, row r = j/size from
+ * the bottom (GL's origin), column = i/size.  Drawn cells (TWOSPEEDS or xy != 0) take
+ * palette entry min(255, (int)(256 * 0.5 * (1 + COLOR_RANGE*tanh(SLOPE*(VSHIFT +
+ * VSCALE*phi)/scale)))) of the caller's 256x3 byte palette `lut` (the reference's
+ * turbo_srgb_bytes), times the optional fades, rounded; other cells are black.
+ * rgb_host and/or rgb_device receive the image (either may be NULL). */
 typedef struct wg_frame_params {
     int32_t size;            /* downsampling (draw_wave_highres_palette's size=2) */
     int32_t fade;            /* apply fade_value */
     double vshift, vscale;   /* VSHIFT_AMPLITUDE, VSCALE_AMPLITUDE */
     double slope, color_range, scale; /* SLOPE, COLOR_RANGE, scale */
     double fade_value;
+    int32_t fade_in_obstacle; /* FADE_IN_OBSTACLE: times (tcc/COURANT^2)^0.1 (wave_common.c:1739-1748) */
+    int32_t reserved;
 } wg_frame_params;
 wg_status wg_scene_frame_rgb8(wg_scene *s, const wg_frame_params *fp, const uint8_t *lut,
                               uint8_t *rgb_host, void *rgb_device);

@@ -16,6 +16,10 @@ Test infrastructure only.  Steps:
    which lands outside row 0 when NX > NY, is guarded by ``if (NX <= NY)``.
 3. ``compile``: gcc -O2 -fopenmp -ffp-contract=off (no FMA contraction, no -march)
    of oracle/ref_driver.c around each unit, in parallel, into oracle/_ref/bin/.
+   The ``*__dropin`` variants are the same units with the reference's evolve_wave /
+   evolve_wave_half replaced by include/wavegpu_dropin.h, linked to libwavegpu.so:
+   the reference's own driver code stepping on the GPU (built once the library
+   exists).
 
 Usage: python oracle/build_ref.py [--only NAME ...] [--jobs N]
 """
@@ -39,6 +43,8 @@ SRC = OUT / "src"
 GEN = SRC / "gen"
 BIN = OUT / "bin"
 STUBS = HERE / "stubs"
+INCLUDE = HERE.parent / "include"
+LIBDIR = HERE.parent / "youtube-simulations_gb300"
 
 SOURCES = ["wave_billiard.c", "wave_energy.c", "global_pdes.c", "sub_maze.c", "sub_wave.c",
            "wave_common.c", "sub_wave_comp.c", "colors_waves.c", "colormaps.c",
@@ -133,7 +139,10 @@ def generate(name, spec):
         parts = [patch_defines(define_block(prog), macros), '#include "global_pdes.c"\n',
                  "double vabs(double x);\n",
                  extract_function(sub, "xy_to_ij"), extract_function(sub, "oscillating_bc")]
-        if kind == "wb_fn":
+        if kind == "wb_fn" and spec.get("dropin"):
+            # the reference with its stepper replaced by the GPU drop-in header
+            parts += [extract_function(common, "compute_energy"), '#include "wavegpu_dropin.h"\n']
+        elif kind == "wb_fn":
             parts += [extract_function(common, "compute_energy"),
                       extract_function(prog, "evolve_wave_half").replace(Q2_FROM, Q2_TO),
                       extract_function(prog, "evolve_wave")]
@@ -162,8 +171,11 @@ def compile_one(name, spec, cc="gcc"):
     cmd = [cc, "-O2", "-fopenmp", "-ffp-contract=off", "-w", "-std=gnu99",
            f"-I{STUBS}", f"-I{SRC}", f"-I{GEN}", f'-DREF_TU="{tu.name}"', *defs,
            str(HERE / "ref_driver.c"), "-o", str(exe), "-lm"]
-    if exe.exists() and exe.stat().st_mtime > max(tu.stat().st_mtime,
-                                                   (HERE / "ref_driver.c").stat().st_mtime):
+    if spec.get("dropin"):
+        cmd += [f"-I{INCLUDE}", f"-L{LIBDIR}", "-lwavegpu", f"-Wl,-rpath,{LIBDIR}"]
+    deps = [tu, HERE / "ref_driver.c"] + ([LIBDIR / "libwavegpu.so", INCLUDE / "wavegpu_dropin.h"]
+                                          if spec.get("dropin") else [])
+    if exe.exists() and exe.stat().st_mtime > max(d.stat().st_mtime for d in deps):
         return name, 0, ""
     r = subprocess.run(cmd, capture_output=True, text=True)
     return name, r.returncode, r.stderr[-2000:]
@@ -179,6 +191,9 @@ def build(only=None, jobs=None):
         print("build_ref: reference sources not present; skipping", file=sys.stderr)
         return False
     names = only or list(ref_variants.VARIANTS)
+    # drop-in builds need the GPU library (built first by the package's build)
+    if not (LIBDIR / "libwavegpu.so").exists():
+        names = [n for n in names if not ref_variants.VARIANTS[n].get("dropin")]
     for n in names:
         generate(n, ref_variants.VARIANTS[n])
     jobs = jobs or os.cpu_count() or 4

@@ -168,3 +168,38 @@ def init_neumann(params, domain, lam, xy, npoly=6, apoly=0.0, max_records=80000)
     if n < 0:
         raise OverflowError("too many Neumann points")
     return xy, recs[:n].copy()
+
+
+def frame_rgb8(params, phi, xy, lut, size=2, vshift=-0.2, vscale=1.0, slope=1.0, color_range=0.8, scale=1.0,
+               fade=False, fade_value=1.0, fade_in_obstacle=False, tcc=None):
+    """P_AMPLITUDE frame of draw_wave_highres_palette (wave_common.c:1053-1065,
+    1750-1848; colors_waves.c:3-16, 161-218; colormaps.c:2449-2482) with the palette
+    `lut` (256x3 bytes): rows j/size from the bottom, columns i/size."""
+    nx, ny = params.nx, params.ny
+    phi2 = np.asarray(phi, np.float64).reshape(nx, ny)
+    xy2 = np.asarray(xy).reshape(nx, ny)
+    w, h = nx // size, ny // size
+    ii = np.arange(w) * size
+    jj = np.arange(h) * size
+    v = phi2[np.ix_(ii, jj)].T                      # [row = j][col = i]
+    drawn = (xy2[np.ix_(ii, jj)].T != 0) | bool(params.twospeeds)
+    value = vshift + vscale * v
+    amp = color_range * np.tanh(slope * value / scale)
+    hue = (256.0 * (0.5 * (1.0 + amp))).astype(np.int64)
+    hue = np.clip(hue, 0, 255)
+    f = np.ones_like(value)
+    if fade_in_obstacle:
+        c2 = params.courant * params.courant
+        if tcc is None:
+            m = xy2[np.ix_(ii, jj)].T != 0
+            cc = np.where(m, c2, params.courantb * params.courantb)
+        else:
+            cc = np.asarray(tcc, np.float64).reshape(nx, ny)[np.ix_(ii, jj)].T
+        f = f * np.power(cc / c2, 0.1)
+    if fade:
+        f = f * fade_value
+    lut = np.asarray(lut, np.uint8).reshape(256, 3).astype(np.float64)
+    rgb = lut[hue] * f[..., None]
+    out = np.clip((rgb + 0.5).astype(np.int64), 0, 255).astype(np.uint8)
+    out[~drawn] = 0
+    return out

@@ -75,16 +75,16 @@ int main(int argc, char **argv)
     double *A[6];
     double *rows[6][NX];
     short int *xyrows[NX];
-    short int *xy = malloc(sizeof(short int) * cells);
+    short int *xy = calloc(cells, sizeof(short int));
     for (int k = 0; k < 6; k++) {
-        A[k] = malloc(sizeof(double) * cells);
-        rd(fi, A[k], sizeof(double) * cells);
+        A[k] = calloc(cells, sizeof(double));
+        if (mode != M_TIME) rd(fi, A[k], sizeof(double) * cells);
         for (int i = 0; i < NX; i++) rows[k][i] = A[k] + (size_t)i * NY;
     }
-    rd(fi, xy, sizeof(short int) * cells);
+    if (mode != M_TIME) rd(fi, xy, sizeof(short int) * cells);
     for (int i = 0; i < NX; i++) xyrows[i] = xy + (size_t)i * NY;
     if (n_nbc > N_NEUMANN_POINTS) { fprintf(stderr, "too many records\n"); return 3; }
-    rd(fi, drv_nbc, sizeof(t_neumann_bc) * n_nbc);
+    if (mode != M_TIME) rd(fi, drv_nbc, sizeof(t_neumann_bc) * n_nbc);
     fclose(fi);
     int64_t nrec = n_nbc;
     double **phi = rows[0], **psi = rows[1], **tmp = rows[2];
@@ -99,6 +99,50 @@ int main(int argc, char **argv)
     n_neumann_points = (int)nrec;
 #endif
 
+    if (mode == M_TIME) {
+#if defined(REF_FULL) && defined(REF_KIND_WB)
+        /* inputs made by the reference's own set-up: mask (init_wave_flat with the
+         * given circles), tables (init_ior_2d), one pulse (add_circular_wave at
+         * hd[2], hd[3]), psi = phi; then nsteps timed updates */
+        ncircles = (int)ncirc;
+        for (int c = 0; c < ncirc; c++) {
+            circles[c].xc = circ[3 * c];
+            circles[c].yc = circ[3 * c + 1];
+            circles[c].radius = circ[3 * c + 2];
+            circles[c].active = 1;
+        }
+        init_wave_flat(phi, psi, xyrows);
+        init_ior_2d(xyrows, tcc, tc, tg, 0.0);
+        add_circular_wave(1.0, hd[2], hd[3], phi, psi, xyrows);
+        for (int i = 0; i < NX; i++) memcpy(psi[i], phi[i], sizeof(double) * NY);
+        double **b[3] = {phi, psi, tmp};
+        int cur = 0, prv = 1, fre = 2;
+        double t0 = omp_get_wtime();
+        if (!src_on && nsteps % 3 == 0) {
+            for (int64_t s = 0; s < nsteps / 3; s++) evolve_wave(phi, psi, tmp, xyrows, tcc, tc, tg, drv_nbc);
+        } else {
+            for (int64_t s = 0; s < nsteps; s++) {
+                evolve_wave_half(b[cur], b[prv], b[fre], xyrows, tcc, tc, tg, drv_nbc);
+                if (src_on) b[fre][src_i][src_j] += src_amp * sin(6.283185307179586 * (double)(s + 1) / src_period);
+                int nc = fre, np = cur, nf = prv;
+                cur = nc; prv = np; fre = nf;
+            }
+        }
+        elapsed = omp_get_wtime() - t0;
+        double e = 0.0;
+        for (int i = 0; i < NX; i++)
+            for (int j = 0; j < NY; j++) e += compute_energy(b[cur], b[prv], xyrows, i, j);
+        int64_t threads = omp_get_max_threads();
+        wr(fo, &elapsed, sizeof elapsed);
+        wr(fo, &e, sizeof e);
+        wr(fo, &threads, sizeof threads);
+        fclose(fo);
+        return 0;
+#else
+        fprintf(stderr, "TIME needs a full build\n");
+        return 3;
+#endif
+    }
     if (mode == M_SETUP) {
 #if defined(REF_FULL) && defined(REF_KIND_WB)
         ncircles = (int)ncirc;

@@ -106,3 +106,7 @@ def macro_text(value):
     if isinstance(value, int):
         return str(value)
     return repr(float(value))
+
+# The reference with its stepper replaced by the GPU drop-in (include/wavegpu_dropin.h).
+for _n in ["s_dir", "s_per", "s_abs", "s_vph", "s_vph_beam", "s_topbot", "s_neu", "s_neu_ts", "s_square"]:
+    VARIANTS[_n + "__dropin"] = dict(VARIANTS[_n], dropin=True)

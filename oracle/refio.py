@@ -95,3 +95,33 @@ def run(variant, nx, ny, mode=STEP, nsteps=0, fields=None, xy=None, nbc=None, ci
     off += 8
     out["threads"] = int(np.frombuffer(raw, np.int64, 1, off)[0])
     return out
+
+
+def time_reference(variant, nx, ny, nsteps, circles, centre, src=None, threads=None, timeout=900):
+    """TIME mode: the reference builds its own inputs (init_wave_flat, init_ior_2d,
+    add_circular_wave) and times `nsteps` updates.  Returns (seconds, energy, threads)."""
+    circles = np.asarray(circles, np.float64)[:, :3]
+    hdr = np.zeros(16, np.int64)
+    hdr[:7] = [0x57415645, nx, ny, TIME, nsteps, 0, len(circles)]
+    hd = np.zeros(4)
+    hd[2], hd[3] = centre
+    if src is not None:
+        hdr[9:12] = [1, src[0], src[1]]
+        hd[0], hd[1] = src[2], src[3]
+    with tempfile.TemporaryDirectory() as td:
+        fin, fout = Path(td) / "in.bin", Path(td) / "out.bin"
+        with open(fin, "wb") as f:
+            f.write(hdr.tobytes())
+            f.write(hd.tobytes())
+            f.write(np.ascontiguousarray(circles).tobytes())
+        env = dict(os.environ)
+        if threads is not None:
+            env["OMP_NUM_THREADS"] = str(threads)
+        r = subprocess.run([str(BIN / f"ref_{variant}"), str(fin), str(fout)],
+                           capture_output=True, text=True, env=env, timeout=timeout)
+        if r.returncode != 0:
+            raise RuntimeError(f"ref_{variant} failed ({r.returncode}): {r.stderr[-1000:]}")
+        raw = fout.read_bytes()
+    el, e = np.frombuffer(raw, np.float64, 2, 0)
+    th = int(np.frombuffer(raw, np.int64, 1, 16)[0])
+    return float(el), float(e), th

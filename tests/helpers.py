@@ -54,3 +54,42 @@ def rel_err(a, b):
     a, b = np.asarray(a, np.float64), np.asarray(b, np.float64)
     scale = max(np.max(np.abs(b)), 1e-300)
     return float(np.max(np.abs(a - b)) / scale)
+
+
+def written_cells(p, xy):
+    """Cells the reference's stepper writes on every update (boundary lines with
+    xy != 0 or TWOSPEEDS, interior with xy > 0 or TWOSPEEDS)."""
+    xy2 = np.asarray(xy).reshape(p.nx, p.ny)
+    w = (xy2 > 0) | bool(p.twospeeds)
+    edge = np.zeros_like(w)
+    edge[0, :] = edge[-1, :] = edge[:, 0] = edge[:, -1] = True
+    w = np.where(edge, (xy2 != 0) | bool(p.twospeeds), w)
+    return w.reshape(-1)
+
+
+def equalize_unwritten(p, f, xy, nbc=None):
+    """Make phi = psi = tmp on cells no update writes, so that the in-place two-buffer
+    form of a native scene and the reference's three-buffer rotation hold the same
+    values there (both then keep them)."""
+    w = written_cells(p, xy).copy()
+    if nbc is not None and len(nbc):
+        act = nbc[nbc["active"] != 0]
+        w.reshape(p.nx, p.ny)[act["i"], act["j"]] = True
+    if p.oscillate_left:
+        beam = p.oscillation_schedule in (42, 43, 44, 51)
+
+        def y_to_j(y):
+            return int((y - p.ymin) / (p.ymax - p.ymin) * p.ny)
+        jmin, jmax = (y_to_j(p.oscil_ymid - p.oscil_ymax), y_to_j(p.oscil_ymid + p.oscil_ymax)) if beam else (0, p.ny - 1)
+        col = w.reshape(p.nx, p.ny)[0]
+        for j in range(p.ny - 1):
+            if jmin < j < jmax:
+                col[j] = True
+        if not beam:
+            col[0] = True
+            if p.nx <= p.ny:
+                col[p.nx - 1] = True
+    f = dict(f)
+    for k in ("psi", "tmp"):
+        f[k] = np.where(w, f[k], f["phi"])
+    return f

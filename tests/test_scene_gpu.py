@@ -1,0 +1,139 @@
+"""Native scenes (wg_scene_*) on the GPU against the oracle.
+
+FP64 scenes run the reference's operation order and must match the oracle bit for bit
+(1e-12 relative where oscillating_bc or the point source brings cos/exp/sin).
+FP32 scenes are held to the benchmark spec's tolerance: field error <= 1e-5 relative to the
+field maximum and energy difference <= 1e-5 relative after the run."""
+import numpy as np
+import pytest
+
+import oracle
+import ref_variants
+from helpers import equalize_unwritten, rel_err, variant_inputs
+from youtube_simulations_gb300 import params as P
+from youtube_simulations_gb300 import scenes
+from youtube_simulations_gb300 import wavegpu as W
+
+pytestmark = pytest.mark.gpu
+STEP_VARIANTS = [n for n, v in ref_variants.VARIANTS.items() if v["kind"] == "wb_fn"]
+
+
+def run_oracle(p, f, xy, nsteps, nbc=None):
+    new, prev, _, _ = oracle.run(p, f["phi"], f["psi"], f["tmp"], xy, f["tcc"], f["tc"], f["tgamma"], nsteps, nbc=nbc)
+    return new, prev
+
+
+def close(a, b, p, tol=1e-12):
+    if p.oscillate_left or p.src_on:
+        assert rel_err(a, b) <= tol
+    else:
+        assert np.array_equal(a, b)
+
+
+@pytest.mark.parametrize("variant", STEP_VARIANTS)
+def test_fp64_table_scene(variant):
+    p, f, xy, nbc = variant_inputs(variant, seed=21)
+    f = equalize_unwritten(p, f, xy, nbc)
+    new, prev = run_oracle(p, f, xy, 23, nbc)
+    with W.Scene(p, P.FP64, P.COEF_TABLE) as s:
+        s.set_blocking(1)
+        s.upload(f["phi"], f["psi"], xy, f["tcc"], f["tc"], f["tgamma"])
+        if nbc is not None:
+            s.set_neumann(nbc)
+        s.step(23)
+        phi, psi = s.download()
+        assert s.time == 23
+    close(phi, new, p)
+    close(psi, prev, p)
+
+
+@pytest.mark.parametrize("variant", [v for v in STEP_VARIANTS if not ref_variants.VARIANTS[v]["macros"]["BC_NEUMANN"]])
+def test_fp64_mask_scene(variant):
+    p, f, xy, _ = variant_inputs(variant, seed=22)
+    tcc, tc, tg = scenes.tables(p, xy)
+    f = dict(f, tcc=tcc, tc=tc, tgamma=tg)
+    f = equalize_unwritten(p, f, xy)
+    new, prev = run_oracle(p, f, xy, 31)
+    with W.Scene(p, P.FP64, P.COEF_MASK) as s:
+        s.set_blocking(1)
+        s.upload(f["phi"], f["psi"], xy)
+        s.step(31)
+        phi, psi = s.download()
+    close(phi, new, p)
+    close(psi, prev, p)
+
+
+@pytest.mark.parametrize("variant", ["s_dir", "s_per", "s_abs", "s_vph", "s_topbot", "s_neu"])
+@pytest.mark.parametrize("coef", [P.COEF_MASK, P.COEF_TABLE])
+def test_fp32_scene_tolerance(variant, coef):
+    p, f, xy, nbc = variant_inputs(variant, seed=23, smooth=True)
+    if coef == P.COEF_MASK and nbc is not None:
+        pytest.skip("Neumann ghosts need tables")
+    if coef == P.COEF_MASK:
+        tcc, tc, tg = scenes.tables(p, xy)
+        f = dict(f, tcc=tcc, tc=tc, tgamma=tg)
+    f = equalize_unwritten(p, f, xy, nbc)
+    new, prev = run_oracle(p, f, xy, 60, nbc)
+    with W.Scene(p, P.FP32, coef) as s:
+        s.set_blocking(1)
+        s.upload(f["phi"], f["psi"], xy, f["tcc"], f["tc"], f["tgamma"])
+        if nbc is not None:
+            s.set_neumann(nbc)
+        s.step(60)
+        phi, psi = s.download()
+        e32 = s.total_energy()
+    assert rel_err(phi, new) <= 1e-5
+    assert rel_err(psi, prev) <= 1e-5
+    e64 = oracle.energy_total(p, new, prev, xy)
+    assert abs(e32 - e64) <= 1e-5 * abs(e64)
+
+
+@pytest.mark.parametrize("prec", [P.FP64, P.FP32])
+def test_scene_energy_matches_oracle(prec):
+    p, f, xy, _ = variant_inputs("s_abs", seed=4)
+    with W.Scene(p, prec, P.COEF_TABLE) as s:
+        s.upload(f["phi"], f["psi"], xy, f["tcc"], f["tc"], f["tgamma"])
+        total, cols, boxes = s.energy(ileft=10, iright=50)
+        phi, psi = s.download()
+    # the oracle on the values the scene holds (FP32-rounded for an FP32 scene); an FP32
+    # scene evaluates each cell's energy in FP32 (sums in FP64), hence 1e-6 there
+    tol_t, tol_c = (1e-13, 1e-12) if prec == P.FP64 else (1e-6, 1e-6)
+    ref_total = oracle.energy_total(p, phi, psi, xy, compensated=True)
+    assert abs(total - ref_total) <= tol_t * abs(ref_total)
+    ref_cols = oracle.energy_x(p, phi, psi, xy)
+    assert np.max(np.abs(cols - ref_cols)) <= tol_c * np.max(np.abs(ref_cols))
+    ref_boxes = oracle.energy_tblr(p, phi, psi, xy, 10, 50)
+    assert np.max(np.abs(boxes - ref_boxes)) <= tol_c * np.max(np.abs(ref_boxes))
+
+
+def test_state_roundtrip_and_time():
+    p, f, xy, _ = variant_inputs("s_per", seed=9)
+    with W.Scene(p, P.FP32, P.COEF_MASK) as s:
+        s.upload(f["phi"], f["psi"], xy)
+        a = np.random.default_rng(0).standard_normal(p.nx * p.ny).astype(np.float32)
+        b = np.random.default_rng(1).standard_normal(p.nx * p.ny).astype(np.float32)
+        s.upload_state(a, b)
+        x, y = s.download(native=True)
+        assert np.array_equal(x, a) and np.array_equal(y, b)
+        s.time = 100
+        s.step(3)
+        assert s.time == 103
+
+
+def test_nonfinite_detector():
+    """Blow-up detection through a host-side injected NaN (no device fault)."""
+    p, f, xy, _ = variant_inputs("s_dir", seed=9)
+    phi = f["phi"].copy()
+    phi[p.ny * 10 + 10] = np.nan
+    with W.Scene(p, P.FP32, P.COEF_TABLE) as s:
+        s.upload(phi, f["psi"], xy, f["tcc"], f["tc"], f["tgamma"])
+        assert s.nonfinite() == 1
+        s.step(2)
+        assert s.nonfinite() > 1
+
+
+def test_mask_mode_rejects_ghost_values():
+    p, f, xy, nbc = variant_inputs("s_neu", seed=1)
+    with W.Scene(p, P.FP32, P.COEF_MASK) as s:
+        with pytest.raises(W.WaveGpuError):
+            s.upload(f["phi"], f["psi"], xy)

@@ -1,0 +1,505 @@
+// wg_batch.cu — many scenes of uneven sizes advanced together.
+//
+// Every active scene is cut into tiles of 8 rows x (64 threads x V) columns; a frame
+// of n updates is n launches of one persistent kernel (k_batch_step, sized to fill
+// every SM) whose CTAs take (scene, tile) work items from a device-side atomic counter,
+// plus one kernel that advances each scene's step counter.  The whole frame is
+// recorded once as a CUDA graph and replayed; the scene table, the work counts and the
+// per-scene time and buffer parity live in device memory, so admitting or removing
+// scenes changes data, not the graph.
+//
+// The per-cell arithmetic is the single-scene kernels' (k_step_bulk / fast_edge), so a
+// scene advanced in a batch is bit-identical to the same scene advanced alone.
+#include <algorithm>
+#include <cstring>
+#include <map>
+#include <vector>
+#include "wg_internal.h"
+#include "wg_scene.h"
+#include "wg_cells.cuh"
+
+namespace wg {
+
+constexpr int BT_ROWS = 8;       // tile rows
+constexpr int BT_THREADS = 64;   // threads along j per tile row (x V cells)
+
+struct __align__(16) SlotDev {   // one entry of the compact table of active scenes
+    DevParams p;
+    void *f[2];                  // the two field buffers; dyn.cur says which holds phi
+    uint32_t *act, *nz;
+    int slot;                    // index into the per-slot dynamic state
+    int tiles_j, tile_base, ntiles;
+};
+struct SlotDyn {
+    long long time;
+    int cur;
+    int pad;
+};
+struct BatchHdr {
+    int nactive, total_tiles;
+};
+
+// A boundary-line cell (reference rules) plus the point source; out of line so that
+// the tile loop below stays small.
+template <class T>
+__device__ __noinline__ T batch_edge(const DevParams &p, const FastArgs<T> &a, int i, int j, long long time, T y)
+{
+    T v = fast_edge<T, WG_COEF_MASK>(p, a, i, j, time, y);
+    if (p.src_on && i == p.src_i && j == p.src_j) v = (T)A_((double)v, point_source(p, time));
+    return v;
+}
+
+template <class T>
+__device__ __forceinline__ void batch_tile(const DevParams &p, const T *__restrict__ phi, T *__restrict__ out,
+                                           const uint32_t *__restrict__ act, const uint32_t *__restrict__ nz,
+                                           int i0, int jt, long long time)
+{
+    constexpr int V = Vec<T>::n;
+    FastArgs<T> a;
+    a.phi = phi;
+    a.psi = out;
+    a.out = out;
+    a.act = act;
+    a.nz = nz;
+    a.tcc = a.tc = a.tg = nullptr;
+    a.c2f = (float)p.c2;
+    a.c2bf = (float)p.c2b;
+    a.gamf = (float)p.gam;
+    a.gambf = (float)p.gamb;
+    a.kappaf = (float)p.kappa;
+    a.has_ghosts = 0;
+    a.do_source = 1;
+    const int j0 = (jt * BT_THREADS + (int)threadIdx.x) * V;
+    for (int rr = threadIdx.y; rr < BT_ROWS; rr += blockDim.y) {
+        const int i = i0 + rr;
+        if (i >= p.nx || j0 >= p.pitch) continue;
+        const size_t row = (size_t)i * p.pitch;
+        if (i == 0 || i == p.nx - 1) {
+            for (int k = 0; k < V; k++) {
+                const int j = j0 + k;
+                if (j >= p.ny) break;
+                out[row + j] = batch_edge<T>(p, a, i, j, time, out[row + j]);
+            }
+            continue;
+        }
+        T c[V], y[V], n[V], s[V];
+        vload(phi + row + j0, c);
+        vload(out + row + j0, y);
+        vload(phi + row + p.pitch + j0, n);
+        vload(phi + row - p.pitch + j0, s);
+        const T wl = (j0 > 0) ? phi[row + j0 - 1] : (T)0;
+        const T er = (j0 + V < p.pitch) ? phi[row + j0 + V] : (T)0;
+        const uint32_t word = act[(size_t)i * p.wpitch + (j0 >> 5)] >> (j0 & 31);
+        T o[V];
+#pragma unroll
+        for (int k = 0; k < V; k++) {
+            const int j = j0 + k;
+            T v = y[k];
+            const bool ac = (word >> k) & 1u;
+            if (j >= 1 && j < p.ny - 1 && (p.twospeeds || ac)) {
+                const T x = c[k];
+                const T w = (k == 0) ? wl : c[k - 1];
+                const T e = (k == V - 1) ? er : c[k + 1];
+                if (sizeof(T) == 8) {
+                    double delta = A_(A_(A_((double)n[k], (double)s[k]), (double)e), (double)w);
+                    delta = S_(delta, M_(4.0, (double)x));
+                    v = (T)upd64((double)x, (double)y[k], ac ? p.c2 : p.c2b, delta, p.kappa, ac ? p.gam : p.gamb);
+                } else {
+                    const float xf = (float)x;
+                    const float delta = (((float)n[k] - xf) + ((float)s[k] - xf)) + (((float)e - xf) + ((float)w - xf));
+                    v = (T)upd32(xf, (float)y[k], ac ? a.c2f : a.c2bf, delta, a.kappaf, ac ? a.gamf : a.gambf);
+                }
+                if (p.floor_clamp && ac) v = (T)floor_clamp(p, (double)v);
+            }
+            o[k] = v;
+        }
+        vstore(out + row + j0, o);
+        // this thread's boundary-line cells and an interior point source, after the store
+        if (j0 == 0) out[row] = batch_edge<T>(p, a, i, 0, time, y[0]);
+        if (p.ny - 1 >= j0 && p.ny - 1 < j0 + V) out[row + p.ny - 1] = batch_edge<T>(p, a, i, p.ny - 1, time, out[row + p.ny - 1]);
+        if (p.src_on && i == p.src_i && p.src_j >= j0 && p.src_j < j0 + V && p.src_j > 0 && p.src_j < p.ny - 1)
+            out[row + p.src_j] = (T)A_((double)out[row + p.src_j], point_source(p, time));
+    }
+}
+
+template <class T>
+__global__ void __launch_bounds__(256) k_batch_step(const BatchHdr *__restrict__ hdr, const SlotDev *__restrict__ tab,
+                                                    SlotDyn *__restrict__ dyn, int *__restrict__ counter, int u)
+{
+    __shared__ int item, entry;
+    __shared__ SlotDev sd;
+    const int total = hdr->total_tiles, nact = hdr->nactive;
+    const int tid = threadIdx.y * blockDim.x + threadIdx.x;
+    while (true) {
+        if (tid == 0) item = atomicAdd(counter + u, 1);
+        __syncthreads();
+        const int it = item;
+        if (it >= total) break;
+        if (tid == 0) {
+            int lo = 0, hi = nact - 1;  // last entry with tile_base <= it
+            while (lo < hi) {
+                const int mid = (lo + hi + 1) >> 1;
+                if (tab[mid].tile_base <= it) lo = mid; else hi = mid - 1;
+            }
+            entry = lo;
+        }
+        __syncthreads();
+        {   // cooperative copy of the scene's table entry into shared memory
+            const int *src = reinterpret_cast<const int *>(tab + entry);
+            int *dst = reinterpret_cast<int *>(&sd);
+            for (int w = tid; w < (int)(sizeof(SlotDev) / sizeof(int)); w += blockDim.x * blockDim.y) dst[w] = src[w];
+        }
+        __syncthreads();
+        const int local = it - sd.tile_base;
+        const int ti = local / sd.tiles_j, tj = local % sd.tiles_j;
+        const SlotDyn d = dyn[sd.slot];
+        const int phase = (d.cur + u) & 1;
+        batch_tile<T>(sd.p, (const T *)sd.f[phase], (T *)sd.f[1 - phase], sd.act, sd.nz, ti * BT_ROWS, tj,
+                      d.time + u + 1);
+        __syncthreads();  // sd and item are rewritten for the next work item
+    }
+}
+
+__global__ void k_batch_advance(const BatchHdr *__restrict__ hdr, const SlotDev *__restrict__ tab,
+                                SlotDyn *__restrict__ dyn, int n)
+{
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= hdr->nactive) return;
+    SlotDyn &d = dyn[tab[k].slot];
+    d.time += n;
+    d.cur = (d.cur + n) & 1;
+}
+
+}  // namespace wg
+
+using namespace wg;
+
+struct BatchSlotHost {
+    bool used = false;
+    wg_params prm;
+    DevParams dp;
+    void *f[2] = {nullptr, nullptr};
+    uint32_t *act = nullptr, *nz = nullptr;
+    double2 *ebot = nullptr, *etop = nullptr;
+    double *eout = nullptr;
+    size_t bytes = 0;
+};
+
+struct wg_batch {
+    int prec = WG_FP32;
+    size_t esz = 4;
+    cudaStream_t st = nullptr;
+    bool own_stream = false;
+    std::vector<BatchSlotHost> slots;
+    SlotDev *d_tab = nullptr;
+    int tab_cap = 0;
+    SlotDyn *d_dyn = nullptr;
+    int dyn_cap = 0;
+    BatchHdr *d_hdr = nullptr;
+    int *d_counter = nullptr;
+    int counter_cap = 0;
+    int nactive = 0;
+    long long total_cells = 0;
+    long long launches = 0;
+    int persistent_blocks = 0;
+    std::map<int, cudaGraphExec_t> graphs;  // one per frame length
+    double *h_out = nullptr;
+};
+
+namespace wg {
+
+static wg_status batch_refresh_table(wg_batch *b)
+{
+    constexpr int Vf = 4, Vd = 2;
+    const int V = (b->prec == WG_FP32) ? Vf : Vd;
+    std::vector<SlotDev> tab;
+    int base = 0;
+    long long cells = 0;
+    for (int k = 0; k < (int)b->slots.size(); k++) {
+        const BatchSlotHost &h = b->slots[k];
+        if (!h.used) continue;
+        SlotDev d;
+        memset(&d, 0, sizeof d);
+        d.p = h.dp;
+        d.f[0] = h.f[0];
+        d.f[1] = h.f[1];
+        d.act = h.act;
+        d.nz = h.nz;
+        d.slot = k;
+        d.tiles_j = (h.dp.pitch / V + BT_THREADS - 1) / BT_THREADS;
+        const int tiles_i = (h.prm.nx + BT_ROWS - 1) / BT_ROWS;
+        d.ntiles = tiles_i * d.tiles_j;
+        d.tile_base = base;
+        base += d.ntiles;
+        cells += (long long)h.prm.nx * h.prm.ny;
+        tab.push_back(d);
+    }
+    if ((int)tab.size() > b->tab_cap) {
+        if (b->d_tab) cudaFree(b->d_tab);
+        b->d_tab = nullptr;
+        const int cap = std::max(64, (int)tab.size() * 2);
+        WG_CUDA(cudaMalloc(&b->d_tab, sizeof(SlotDev) * cap));
+        b->tab_cap = cap;
+    }
+    // the graphs hold the table pointer: a reallocation invalidates them
+    if (!tab.empty())
+        WG_CUDA(cudaMemcpyAsync(b->d_tab, tab.data(), sizeof(SlotDev) * tab.size(), cudaMemcpyHostToDevice, b->st));
+    BatchHdr h{(int)tab.size(), base};
+    WG_CUDA(cudaMemcpyAsync(b->d_hdr, &h, sizeof h, cudaMemcpyHostToDevice, b->st));
+    WG_CUDA(cudaStreamSynchronize(b->st));
+    b->nactive = (int)tab.size();
+    b->total_cells = cells;
+    return WG_OK;
+}
+
+static void batch_drop_graphs(wg_batch *b)
+{
+    for (auto &g : b->graphs) cudaGraphExecDestroy(g.second);
+    b->graphs.clear();
+}
+
+template <class T>
+static void batch_enqueue_frame(wg_batch *b, int n)
+{
+    cudaMemsetAsync(b->d_counter, 0, sizeof(int) * n, b->st);
+    dim3 blk(BT_THREADS, 4);
+    for (int u = 0; u < n; u++) k_batch_step<T><<<b->persistent_blocks, blk, 0, b->st>>>(b->d_hdr, b->d_tab, b->d_dyn, b->d_counter, u);
+    const int cap = std::max(b->tab_cap, 1);
+    k_batch_advance<<<(cap + 255) / 256, 256, 0, b->st>>>(b->d_hdr, b->d_tab, b->d_dyn, n);
+}
+
+}  // namespace wg
+
+extern "C" {
+
+wg_status wg_batch_create(int32_t precision, void *stream, wg_batch **out)
+{
+    if (!out) { set_error("NULL argument"); return WG_ERR_INVALID; }
+    if (precision != WG_FP32 && precision != WG_FP64) { set_error("precision must be WG_FP32 or WG_FP64"); return WG_ERR_INVALID; }
+    wg_batch *b = new wg_batch();
+    b->prec = precision;
+    b->esz = precision == WG_FP32 ? 4 : 8;
+    cudaError_t e = cudaSuccess;
+    if (stream) b->st = (cudaStream_t)stream;
+    else {
+        e = cudaStreamCreateWithFlags(&b->st, cudaStreamNonBlocking);
+        b->own_stream = true;
+    }
+    if (e == cudaSuccess) e = cudaMalloc(&b->d_hdr, sizeof(BatchHdr));
+    if (e == cudaSuccess) e = cudaMemsetAsync(b->d_hdr, 0, sizeof(BatchHdr), b->st);
+    int dev = 0, sms = 0, per = 0;
+    if (e == cudaSuccess) e = cudaGetDevice(&dev);
+    if (e == cudaSuccess) e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    if (e == cudaSuccess)
+        e = (precision == WG_FP32)
+                ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_batch_step<float>, BT_THREADS * 4, 0)
+                : cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_batch_step<double>, BT_THREADS * 4, 0);
+    if (e == cudaSuccess) e = cudaHostAlloc(&b->h_out, 16 * sizeof(double), cudaHostAllocDefault);
+    if (e != cudaSuccess) {
+        wg_status r = cuda_fail(e, "wg_batch_create");
+        wg_batch_destroy(b);
+        return r;
+    }
+    b->persistent_blocks = std::max(1, sms * std::max(per, 1));
+    *out = b;
+    return WG_OK;
+}
+
+wg_status wg_batch_destroy(wg_batch *b)
+{
+    if (!b) return WG_OK;
+    if (b->st) cudaStreamSynchronize(b->st);
+    batch_drop_graphs(b);
+    for (auto &h : b->slots) {
+        if (!h.used) continue;
+        void *ptrs[] = {h.f[0], h.f[1], h.act, h.nz, h.ebot, h.etop, h.eout};
+        for (void *p : ptrs) if (p) cudaFree(p);
+    }
+    void *ptrs[] = {b->d_tab, b->d_dyn, b->d_hdr, b->d_counter};
+    for (void *p : ptrs) if (p) cudaFree(p);
+    if (b->h_out) cudaFreeHost(b->h_out);
+    if (b->own_stream && b->st) cudaStreamDestroy(b->st);
+    delete b;
+    return WG_OK;
+}
+
+wg_status wg_batch_add(wg_batch *b, const wg_params *p, const double *phi, const double *psi, const int16_t *xy,
+                       int32_t *slot)
+{
+    if (!b || !p || !phi || !psi || !xy || !slot) { set_error("NULL argument"); return WG_ERR_INVALID; }
+    wg_status st = validate_params(*p);
+    if (st) return st;
+    if (p->bc_neumann) { set_error("batches do not take Neumann records; use a scene"); return WG_ERR_INVALID; }
+    const size_t n = (size_t)p->nx * p->ny;
+    for (size_t c = 0; c < n; c++)
+        if (xy[c] != 0 && xy[c] != 1) { set_error("batch masks take values 0/1"); return WG_ERR_INVALID; }
+    int k = 0;
+    while (k < (int)b->slots.size() && b->slots[k].used) k++;
+    if (k == (int)b->slots.size()) b->slots.emplace_back();
+    BatchSlotHost &h = b->slots[k];
+    h = BatchSlotHost();
+    h.prm = *p;
+    const int pitch = pitch_for(p->ny, (int)b->esz);
+    h.dp = make_dev_params(*p, pitch);
+    const size_t fb = (size_t)p->nx * pitch * b->esz, mb = (size_t)p->nx * h.dp.wpitch * 4;
+    cudaError_t e = cudaSuccess;
+    for (int q = 0; q < 2 && e == cudaSuccess; q++) e = cudaMallocAsync(&h.f[q], fb, b->st);
+    if (e == cudaSuccess) e = cudaMallocAsync((void **)&h.act, mb, b->st);
+    if (e == cudaSuccess) e = cudaMallocAsync((void **)&h.nz, mb, b->st);
+    if (e == cudaSuccess) e = cudaMallocAsync((void **)&h.ebot, p->nx * sizeof(double2), b->st);
+    if (e == cudaSuccess) e = cudaMallocAsync((void **)&h.etop, p->nx * sizeof(double2), b->st);
+    if (e == cudaSuccess) e = cudaMallocAsync((void **)&h.eout, (p->nx + 8) * sizeof(double), b->st);
+    void *stage = nullptr;
+    if (e == cudaSuccess) e = cudaMallocAsync(&stage, n * sizeof(double), b->st);
+    if (e != cudaSuccess) {
+        void *ptrs[] = {h.f[0], h.f[1], h.act, h.nz, h.ebot, h.etop, h.eout, stage};
+        for (void *q : ptrs) if (q) cudaFreeAsync(q, b->st);
+        h = BatchSlotHost();
+        return cuda_fail(e, "wg_batch_add");
+    }
+    h.bytes = 2 * fb + 2 * mb;
+    // mask planes, then the two fields (FP64 host values rounded on the device)
+    WG_CUDA(cudaMemcpyAsync(stage, xy, n * sizeof(int16_t), cudaMemcpyHostToDevice, b->st));
+    launch_pack_mask(p->nx, p->ny, h.dp.wpitch, (const int16_t *)stage, h.act, h.nz, b->st);
+    const double *src[2] = {phi, psi};
+    for (int q = 0; q < 2; q++) {
+        WG_CUDA(cudaMemcpyAsync(stage, src[q], n * sizeof(double), cudaMemcpyHostToDevice, b->st));
+        if (b->prec == WG_FP32) launch_convert_in<float>(p->nx, p->ny, pitch, (const double *)stage, (float *)h.f[q], b->st);
+        else launch_convert_in<double>(p->nx, p->ny, pitch, (const double *)stage, (double *)h.f[q], b->st);
+    }
+    WG_CUDA(cudaFreeAsync(stage, b->st));
+    WG_CUDA(cudaGetLastError());
+    // dynamic state: time 0, phi in f[0]
+    if (k >= b->dyn_cap) {
+        const int cap = std::max(64, 2 * (k + 1));
+        SlotDyn *nd = nullptr;
+        WG_CUDA(cudaMalloc(&nd, sizeof(SlotDyn) * cap));
+        WG_CUDA(cudaMemsetAsync(nd, 0, sizeof(SlotDyn) * cap, b->st));
+        if (b->d_dyn) {
+            WG_CUDA(cudaMemcpyAsync(nd, b->d_dyn, sizeof(SlotDyn) * b->dyn_cap, cudaMemcpyDeviceToDevice, b->st));
+            WG_CUDA(cudaStreamSynchronize(b->st));
+            cudaFree(b->d_dyn);
+        }
+        b->d_dyn = nd;
+        b->dyn_cap = cap;
+        batch_drop_graphs(b);
+    }
+    SlotDyn zero{0, 0, 0};
+    WG_CUDA(cudaMemcpyAsync(b->d_dyn + k, &zero, sizeof zero, cudaMemcpyHostToDevice, b->st));
+    h.used = true;
+    const int old_cap = b->tab_cap;
+    if ((st = batch_refresh_table(b))) return st;
+    if (b->tab_cap != old_cap) batch_drop_graphs(b);
+    *slot = k;
+    return WG_OK;
+}
+
+wg_status wg_batch_remove(wg_batch *b, int32_t slot)
+{
+    if (!b || slot < 0 || slot >= (int)b->slots.size() || !b->slots[slot].used) {
+        set_error("unknown batch slot %d", slot);
+        return WG_ERR_NOTFOUND;
+    }
+    BatchSlotHost &h = b->slots[slot];
+    h.used = false;
+    wg_status st = batch_refresh_table(b);  // the kernels stop seeing the slot first
+    void *ptrs[] = {h.f[0], h.f[1], h.act, h.nz, h.ebot, h.etop, h.eout};
+    for (void *p : ptrs) if (p) WG_CUDA(cudaFreeAsync(p, b->st));
+    h = BatchSlotHost();
+    return st;
+}
+
+wg_status wg_batch_step(wg_batch *b, int32_t nsteps)
+{
+    if (!b || nsteps < 0) { set_error("bad arguments"); return WG_ERR_INVALID; }
+    if (nsteps == 0 || b->nactive == 0) return WG_OK;
+    if (nsteps > b->counter_cap) {
+        if (b->d_counter) cudaFree(b->d_counter);
+        b->d_counter = nullptr;
+        WG_CUDA(cudaMalloc(&b->d_counter, sizeof(int) * nsteps));
+        b->counter_cap = nsteps;
+        batch_drop_graphs(b);
+    }
+    auto it = b->graphs.find(nsteps);
+    if (it == b->graphs.end()) {
+        cudaGraph_t g;
+        WG_CUDA(cudaStreamBeginCapture(b->st, cudaStreamCaptureModeThreadLocal));
+        if (b->prec == WG_FP32) batch_enqueue_frame<float>(b, nsteps);
+        else batch_enqueue_frame<double>(b, nsteps);
+        WG_CUDA(cudaStreamEndCapture(b->st, &g));
+        cudaGraphExec_t ge;
+        cudaError_t e = cudaGraphInstantiate(&ge, g, 0);
+        cudaGraphDestroy(g);
+        if (e != cudaSuccess) return cuda_fail(e, "cudaGraphInstantiate");
+        it = b->graphs.emplace(nsteps, ge).first;
+    }
+    WG_CUDA(cudaGraphLaunch(it->second, b->st));
+    b->launches += nsteps + 1;
+    return WG_OK;
+}
+
+wg_status wg_batch_download(wg_batch *b, int32_t slot, double *phi, double *psi)
+{
+    if (!b || slot < 0 || slot >= (int)b->slots.size() || !b->slots[slot].used) {
+        set_error("unknown batch slot %d", slot);
+        return WG_ERR_NOTFOUND;
+    }
+    BatchSlotHost &h = b->slots[slot];
+    SlotDyn d;
+    WG_CUDA(cudaMemcpyAsync(&d, b->d_dyn + slot, sizeof d, cudaMemcpyDeviceToHost, b->st));
+    WG_CUDA(cudaStreamSynchronize(b->st));
+    const size_t n = (size_t)h.prm.nx * h.prm.ny;
+    double *stage = nullptr;
+    WG_CUDA(cudaMallocAsync((void **)&stage, n * sizeof(double), b->st));
+    double *dst[2] = {phi, psi};
+    for (int q = 0; q < 2; q++) {
+        if (!dst[q]) continue;
+        const void *src = h.f[q == 0 ? d.cur : 1 - d.cur];
+        if (b->prec == WG_FP32) launch_convert_out<float>(h.prm.nx, h.prm.ny, h.dp.pitch, (const float *)src, stage, b->st);
+        else launch_convert_out<double>(h.prm.nx, h.prm.ny, h.dp.pitch, (const double *)src, stage, b->st);
+        WG_CUDA(cudaMemcpyAsync(dst[q], stage, n * sizeof(double), cudaMemcpyDeviceToHost, b->st));
+    }
+    WG_CUDA(cudaFreeAsync(stage, b->st));
+    WG_CUDA(cudaStreamSynchronize(b->st));
+    return WG_OK;
+}
+
+wg_status wg_batch_energy(wg_batch *b, int32_t slot, double *total)
+{
+    if (!b || !total || slot < 0 || slot >= (int)b->slots.size() || !b->slots[slot].used) {
+        set_error("unknown batch slot %d", slot);
+        return WG_ERR_NOTFOUND;
+    }
+    BatchSlotHost &h = b->slots[slot];
+    SlotDyn d;
+    WG_CUDA(cudaMemcpyAsync(&d, b->d_dyn + slot, sizeof d, cudaMemcpyDeviceToHost, b->st));
+    WG_CUDA(cudaStreamSynchronize(b->st));
+    const void *phi = h.f[d.cur], *psi = h.f[1 - d.cur];
+    if (b->prec == WG_FP32)
+        launch_energy<float>(h.dp, (const float *)phi, (const float *)psi, nullptr, h.nz, h.ebot, h.etop, 0, 0, h.eout, b->st);
+    else
+        launch_energy<double>(h.dp, (const double *)phi, (const double *)psi, nullptr, h.nz, h.ebot, h.etop, 0, 0, h.eout, b->st);
+    b->launches += 2;
+    WG_CUDA(cudaGetLastError());
+    WG_CUDA(cudaMemcpyAsync(b->h_out, h.eout, sizeof(double), cudaMemcpyDeviceToHost, b->st));
+    WG_CUDA(cudaStreamSynchronize(b->st));
+    *total = b->h_out[0];
+    return WG_OK;
+}
+
+wg_status wg_batch_count(wg_batch *b, int32_t *n_active, int64_t *cells)
+{
+    if (!b) return WG_ERR_INVALID;
+    if (n_active) *n_active = b->nactive;
+    if (cells) *cells = b->total_cells;
+    return WG_OK;
+}
+
+wg_status wg_batch_launch_count(wg_batch *b, int64_t *n)
+{
+    if (!b || !n) return WG_ERR_INVALID;
+    *n = b->launches;
+    return WG_OK;
+}
+
+}  // extern "C"

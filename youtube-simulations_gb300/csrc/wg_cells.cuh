@@ -1,0 +1,91 @@
+// wg_cells.cuh — per-cell building blocks shared by the stepping kernels: field and
+// mask accessors, coefficient sources, 16-byte vector loads, and the boundary-line
+// rule of the native form.
+#pragma once
+#include "wg_internal.h"
+
+namespace wg {
+
+// ---------------------------------------------------------------------------
+// Accessors
+// ---------------------------------------------------------------------------
+template <class T>
+struct Field {
+    const T *a;
+    int pitch;
+    __device__ __forceinline__ T operator()(int i, int j) const { return a[(size_t)i * pitch + j]; }
+};
+struct ActI16 {
+    const int16_t *a;
+    int pitch;
+    __device__ __forceinline__ int operator()(int i, int j) const { return a[(size_t)i * pitch + j] != 0; }
+};
+struct ActBits {
+    const uint32_t *w;
+    int wpitch;
+    __device__ __forceinline__ int operator()(int i, int j) const
+    {
+        return (w[(size_t)i * wpitch + (j >> 5)] >> (j & 31)) & 1u;
+    }
+};
+template <class T>
+struct CoefTab {
+    const T *tcc_, *tc_, *tg_;
+    int pitch;
+    double gam;
+    __device__ __forceinline__ double tcc(int i, int j) const { return (double)tcc_[(size_t)i * pitch + j]; }
+    __device__ __forceinline__ double tc(int i, int j) const { return tc_ ? (double)tc_[(size_t)i * pitch + j] : 0.0; }
+    __device__ __forceinline__ double tg(int i, int j) const { return tg_ ? (double)tg_[(size_t)i * pitch + j] : gam; }
+};
+struct CoefMask {
+    ActBits act;
+    double c2, c2b, gam, gamb, c, cb;
+    __device__ __forceinline__ double tcc(int i, int j) const { return act(i, j) ? c2 : c2b; }
+    __device__ __forceinline__ double tc(int i, int j) const { return act(i, j) ? c : cb; }
+    __device__ __forceinline__ double tg(int i, int j) const { return act(i, j) ? gam : gamb; }
+};
+
+template <class T> struct Vec;
+template <> struct Vec<float> { using type = float4; static constexpr int n = 4; };
+template <> struct Vec<double> { using type = double2; static constexpr int n = 2; };
+
+template <class T>
+__device__ __forceinline__ void vload(const T *ptr, T (&v)[Vec<T>::n])
+{
+    typename Vec<T>::type t = *reinterpret_cast<const typename Vec<T>::type *>(ptr);
+    const T *s = reinterpret_cast<const T *>(&t);
+#pragma unroll
+    for (int k = 0; k < Vec<T>::n; k++) v[k] = s[k];
+}
+template <class T>
+__device__ __forceinline__ void vstore(T *ptr, const T (&v)[Vec<T>::n])
+{
+    typename Vec<T>::type t;
+    T *d = reinterpret_cast<T *>(&t);
+#pragma unroll
+    for (int k = 0; k < Vec<T>::n; k++) d[k] = v[k];
+    *reinterpret_cast<typename Vec<T>::type *>(ptr) = t;
+}
+
+// Boundary-line cell of the native form, reference rules.  Returns the value to
+// store (the old psi value y when the reference writes nothing).
+template <class T, int COEF>
+__device__ inline T fast_edge(const DevParams &p, const FastArgs<T> &a, int i, int j, long long time, T y)
+{
+    Field<T> PHI{a.phi, p.pitch}, PSI{a.psi, p.pitch};
+    ActBits ACT{a.act, p.wpitch}, NZ{a.nz, p.wpitch};
+    double v;
+    bool w;
+    if (COEF == WG_COEF_MASK) {
+        CoefMask CF{ACT, p.c2, p.c2b, p.gam, p.gamb, p.courant, p.courantb};
+        w = edge_cell<T>(p, time, i, j, PHI, PSI, ACT, CF, &v);
+    } else {
+        CoefTab<T> CF{a.tcc, a.tc, a.tg, p.pitch, p.gam};
+        w = edge_cell<T>(p, time, i, j, PHI, PSI, ACT, CF, &v);
+    }
+    if (!w) v = (double)y;
+    if (p.floor_clamp && NZ(i, j)) v = floor_clamp(p, v);
+    return (T)v;
+}
+
+}  // namespace wg

@@ -1,0 +1,298 @@
+// wg_device.cuh — device-side parameters and the per-cell rules of the reference's
+// stepper (wave_billiard.c:302-610), shared by every stepping kernel.
+//
+// Arithmetic of the FP64 forms uses __dadd_rn/__dsub_rn/__dmul_rn so that nothing is
+// contracted into an FMA and every operation happens in the reference's order: the
+// device result is then bit-identical to the CPU reference built without FMA.
+#pragma once
+#include <cstdint>
+#include <cuda_runtime.h>
+
+namespace wg {
+
+// Scene parameters as the kernels see them (host-precomputed integers included).
+struct DevParams {
+    int nx, ny;          // grid
+    int pitch;           // elements per row in device memory (multiple of 32)
+    int wpitch;          // 32-bit mask words per row (pitch / 32)
+    int b_cond, twospeeds, osc_left, osc_topbot, sched, floor_clamp, beam;
+    int bc_jmin, bc_jmax;          // OSCILLATE_LEFT beam range (wave_billiard.c:320-339)
+    int osc_beam_jmax;             // xy_to_ij(0, OSCIL_YMAX)[1] (sub_wave.c:12032)
+    int osc_sine_jmax, osc_sine_jmin;  // xy_to_ij(0, OSCIL_YMID +- OSCIL_YMAX)[1]
+    int src_on, src_i, src_j;
+    int corner2_on;                // the reference's phi_out[0][NX-1] write is in bounds
+    double tb_shift;
+    double kappa, kappa_sides, kappa_topbot, gamma_sides, gamma_topbot, vmax;
+    double c2, c2b, gam, gamb, courant, courantb;   // WG_COEF_MASK coefficients
+    double omega, omega_b, amplitude, damping, achirp, yshift, ivar, ishift, wpshift;
+    double ymin, ymax;
+    double src_amp, src_period;
+    double e_scale2, ehalf_c2, ehalf_c2b;  // E_SCALE^2, (0.5*COURANT)*COURANT, (0.5*COURANTB)*COURANTB
+};
+
+// ---------------------------------------------------------------------------
+// Exactly rounded double operations (never contracted).
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ double A_(double a, double b) { return __dadd_rn(a, b); }
+__device__ __forceinline__ double S_(double a, double b) { return __dsub_rn(a, b); }
+__device__ __forceinline__ double M_(double a, double b) { return __dmul_rn(a, b); }
+__device__ __forceinline__ double D_(double a, double b) { return __ddiv_rn(a, b); }
+
+// -y + 2*x + cc*delta - KAPPA*x - g*(x-y)   (wave_billiard.c:373)
+__device__ __forceinline__ double upd64(double x, double y, double cc, double delta, double kappa, double g)
+{
+    double r = A_(-y, M_(2.0, x));
+    r = A_(r, M_(cc, delta));
+    r = S_(r, M_(kappa, x));
+    return S_(r, M_(g, S_(x, y)));
+}
+
+// x - tc*(x - nb) - K*x - G*(x-y)   (wave_billiard.c:418)
+__device__ __forceinline__ double absorb64(double x, double y, double tc, double nb, double k, double g)
+{
+    double r = S_(x, M_(tc, S_(x, nb)));
+    r = S_(r, M_(k, x));
+    return S_(r, M_(g, S_(x, y)));
+}
+
+// FP32 update in increment form: out = x + ((1-g)(x-y) + cc*delta - kappa*x) with the
+// Laplacian as differences from the centre.  Same mathematics as upd64.
+__device__ __forceinline__ float upd32(float x, float y, float cc, float delta, float kappa, float g)
+{
+    float w = x - y;
+    float inc = fmaf(cc, delta, fmaf(-g, w, w) - kappa * x);
+    return x + inc;
+}
+__device__ __forceinline__ float absorb32(float x, float y, float tc, float nb, float k, float g)
+{
+    return x - (tc * (x - nb) + k * x + g * (x - y));
+}
+
+// oscillating_bc (sub_wave.c:11965-12162) with the reference's constants.
+__device__ inline double osc_bc(const DevParams &p, int time, int j)
+{
+    const double PID = 1.570796327, DPI = 6.283185307;
+    const int NY = p.ny;
+    const double YSH = p.yshift, OM = p.omega, AMP = p.amplitude, DAMP = p.damping;
+    double t, t1, phase, a, env, amp, dist2;
+    const double tOM = M_((double)time, OM);
+    switch (p.sched) {
+    case 0:  // OSC_PERIODIC
+        if (YSH > 0.0) t = S_(tOM, D_(M_((double)j, YSH), (double)NY));
+        else t = A_(tOM, D_(M_((double)(NY - j), YSH), (double)NY));
+        if (t < 0.0) return 0.0;
+        return M_(M_(AMP, cos(t)), exp(M_(-t, DAMP)));
+    case 1:  // OSC_SLOWING
+        a = 0.0025;
+        t = tOM;
+        if (YSH > 0.0) t = S_(t, D_(M_((double)j, YSH), (double)NY));
+        phase = S_(t, M_(M_(a, t), t));
+        return M_(M_(AMP, cos(phase)), exp(M_(-phase, DAMP)));
+    case 2:   // OSC_WAVE_PACKET
+    case 21:  // OSC_WAVE_PACKETS
+        t = tOM;
+        if (YSH > 0.0) t = S_(t, D_(M_((double)j, YSH), (double)NY));
+        t1 = t;
+        if (p.sched == 21) t1 = S_(t, M_((double)((int)A_(D_(t, p.wpshift), 0.5)), p.wpshift));
+        a = D_(sqrt(p.ivar), OM);
+        phase = M_(AMP, cos(t));
+        env = M_(exp(D_(M_(-S_(t1, p.ishift), S_(t1, p.ishift)), M_(a, a))), sqrt(D_(DPI, a)));
+        return M_(phase, env);
+    case 3:  // OSC_CHIRP
+        t = tOM;
+        if (YSH > 0.0) t = S_(t, D_(M_((double)j, YSH), (double)NY));
+        phase = A_(t, M_(M_(p.achirp, t), t));
+        return M_(M_(AMP, sin(phase)), exp(M_(-phase, DAMP)));
+    case 4:   // OSC_BEAM
+    case 5: { // OSC_BEAM_TWOPERIODS
+        int jmax = p.osc_beam_jmax, jmin = NY - jmax;
+        double h = S_(p.ymax, p.ymin);
+        if (j < jmin) dist2 = D_(M_((double)(jmin - 1 - j), h), (double)NY);
+        else if (j > jmax) dist2 = D_(M_((double)(j - jmax), h), (double)NY);
+        else dist2 = 0.0;
+        dist2 = M_(M_(500.0, dist2), dist2);
+        t = tOM;
+        if (YSH > 0.0) t = S_(t, D_(M_((double)j, YSH), (double)NY));
+        if (p.sched == 4) amp = M_(M_(AMP, cos(t)), exp(M_(-t, DAMP)));
+        else amp = M_(M_(AMP, A_(M_(0.5, cos(t)), M_(0.5, cos(M_(sqrt(7.0), t))))), exp(M_(-t, DAMP)));
+        return M_(amp, exp(D_(-dist2, p.ivar)));
+    }
+    case 41: {  // OSC_BEAM_GAUSSIAN
+        dist2 = D_(M_((double)(j - NY / 2), S_(p.ymax, p.ymin)), (double)NY);
+        dist2 = M_(dist2, dist2);
+        t = tOM;
+        if (YSH > 0.0) t = S_(t, D_(M_((double)j, YSH), (double)NY));
+        amp = M_(M_(AMP, cos(t)), exp(M_(-t, DAMP)));
+        return M_(amp, exp(D_(-dist2, p.ivar)));
+    }
+    case 42: case 43: case 44: case 51: {  // beam modulated by a sine in y
+        int jmax = p.osc_sine_jmax, jmin = p.osc_sine_jmin, jmid = (jmin + jmax) / 2;
+        dist2 = D_((double)(j - jmid), (double)(jmax - jmid));
+        if (j > jmax) return 0.0;
+        if (j < jmin) return 0.0;
+        t = tOM;
+        if (YSH > 0.0) t = S_(t, D_(M_((double)j, YSH), (double)NY));
+        if (p.sched == 42) {
+            amp = M_(M_(AMP, cos(t)), exp(M_(-t, DAMP)));
+        } else if (p.sched == 43) {
+            a = D_(p.ivar, M_(OM, OM));
+            amp = M_(M_(AMP, cos(t)), exp(D_(M_(-S_(t, p.ishift), S_(t, p.ishift)), a)));
+        } else if (p.sched == 51) {
+            amp = M_(M_(AMP, A_(M_(0.5, cos(t)), M_(0.5, cos(M_(sqrt(7.0), t))))), exp(M_(-t, DAMP)));
+        } else {
+            phase = A_(t, M_(M_(p.achirp, t), t));
+            amp = M_(M_(AMP, sin(phase)), exp(M_(-phase, DAMP)));
+        }
+        return M_(amp, cos(M_(PID, dist2)));
+    }
+    case 6:
+    case 61:
+        t = A_(tOM, D_(M_((double)(NY - j), YSH), (double)NY));
+        t1 = A_(tOM, D_(M_((double)j, YSH), (double)NY));
+        if (p.sched == 6) amp = (j < NY / 2) ? cos(t) : cos(t1);
+        else {
+            amp = 0.0;
+            if (t > 0.0) amp = A_(amp, cos(t));
+            if (t1 > 0.0) amp = A_(amp, cos(t1));
+        }
+        return M_(AMP, amp);
+    case 7:
+        if (j > NY / 2) t = A_(tOM, D_(M_((double)(NY - j), YSH), (double)NY));
+        else t = A_(M_((double)time, p.omega_b), D_(M_((double)(NY - j), YSH), (double)NY));
+        return M_(M_(AMP, cos(t)), exp(M_(-t, DAMP)));
+    default:
+        return 0.0;
+    }
+}
+
+__device__ __forceinline__ double point_source(const DevParams &p, long long t)
+{
+    return M_(p.src_amp, sin(D_(M_(6.283185307179586, (double)t), p.src_period)));
+}
+
+__device__ __forceinline__ bool left_bc(const DevParams &p, int j)
+{
+    return p.osc_left && j < p.ny - 1 && j > p.bc_jmin && j < p.bc_jmax;
+}
+
+// Any boundary-line cell of the reference (left/right columns, top/bottom rows),
+// computed with the reference's rules.  Returns true when the reference writes the
+// cell; *out then holds the value (corner oscillation included, FLOOR not).
+// Accessors: PHI(i,j), PSI(i,j) field reads; ACT(i,j) -> "xy != 0"; TCC/TC/TG tables.
+template <class T, class Phi, class Act, class Coef>
+__device__ inline bool edge_cell(const DevParams &p, long long time, int i, int j,
+                                 const Phi &PHI, const Phi &PSI, const Act &ACT, const Coef &CF,
+                                 double *out)
+{
+    const int NX = p.nx, NY = p.ny;
+    bool written = false;
+    double v = 0.0;
+    if (j == NY - 1 || j == 0) {
+        const int jb = j, jn = (j == NY - 1) ? NY - 2 : 1, jw = (j == NY - 1) ? 0 : NY - 1;
+        if (p.twospeeds || ACT(i, jb)) {
+            double x = (double)PHI(i, jb), y = (double)PSI(i, jb);
+            if (p.osc_topbot && ((double)i < p.tb_shift) && (i < NX - 1) && (i > 0)) {
+                double delta = A_(A_((double)PHI(i + 1, jb), (double)PHI(i - 1, jb)), -M_(2.0, x));
+                v = upd64(x, y, CF.tcc(i, jb), delta, p.kappa, CF.tg(i, jb));
+            } else {
+                int ip, im;
+                double delta;
+                switch (p.b_cond) {
+                case 0:
+                    ip = i + 1; if (ip == NX) ip = NX - 1;
+                    im = i - 1; if (im == -1) im = 0;
+                    delta = S_(A_(A_((double)PHI(ip, jb), (double)PHI(im, jb)), (double)PHI(i, jn)), M_(3.0, x));
+                    v = upd64(x, y, CF.tcc(i, jb), delta, p.kappa, CF.tg(i, jb));
+                    break;
+                case 1:
+                    ip = (i + 1) % NX; im = (i - 1) % NX; if (im < 0) im += NX;
+                    delta = S_(A_(A_(A_((double)PHI(ip, jb), (double)PHI(im, jb)), (double)PHI(i, jn)), (double)PHI(i, jw)), M_(4.0, x));
+                    v = upd64(x, y, CF.tcc(i, jb), delta, p.kappa, CF.tg(i, jb));
+                    break;
+                case 2:
+                    v = absorb64(x, y, CF.tc(i, jb), (double)PHI(i, jn), p.kappa_topbot, p.gamma_topbot);
+                    break;
+                default:
+                    ip = i + 1; if (ip == NX) ip = NX - 1;
+                    im = i - 1; if (im == -1) im = 0;
+                    if (i == 0) v = absorb64(x, y, CF.tc(0, jb), (double)PHI(1, jb), p.kappa_sides, p.gamma_sides);
+                    else {
+                        delta = S_(A_(A_(A_((double)PHI(ip, jb), (double)PHI(im, jb)), (double)PHI(i, jn)), (double)PHI(i, jw)), M_(4.0, x));
+                        v = upd64(x, y, CF.tcc(i, jb), delta, p.kappa, CF.tg(i, jb));
+                    }
+                    break;
+                }
+            }
+            written = true;
+        }
+    } else if (i == 0 || i == NX - 1) {
+        const bool left = (i == 0);
+        if (left && left_bc(p, j)) {
+            v = osc_bc(p, (int)time, j);
+            written = true;
+        } else if (p.twospeeds || ACT(i, j)) {
+            const int in = left ? 1 : NX - 2, iw = left ? NX - 1 : 0;
+            double x = (double)PHI(i, j), y = (double)PSI(i, j), delta;
+            switch (p.b_cond) {
+            case 0:
+                delta = S_(A_(A_((double)PHI(in, j), (double)PHI(i, j + 1)), (double)PHI(i, j - 1)), M_(3.0, x));
+                v = upd64(x, y, CF.tcc(i, j), delta, p.kappa, CF.tg(i, j));
+                break;
+            case 1:
+                delta = S_(A_(A_(A_((double)PHI(in, j), (double)PHI(iw, j)), (double)PHI(i, j + 1)), (double)PHI(i, j - 1)), M_(4.0, x));
+                v = upd64(x, y, CF.tcc(i, j), delta, p.kappa, CF.tg(i, j));
+                break;
+            default:
+                v = absorb64(x, y, CF.tc(i, j), (double)PHI(in, j), p.kappa_sides, p.gamma_sides);
+                break;
+            }
+            written = true;
+        }
+    }
+    // oscillating corners (wave_billiard.c:586-590); the second write of the
+    // reference is phi_out[0][NX-1], kept only where that cell exists (NX <= NY).
+    if (p.osc_left && !p.beam && i == 0) {
+        if (j == 0) { v = osc_bc(p, (int)time, 0); written = true; }
+        else if (p.corner2_on && j == NX - 1) { v = osc_bc(p, (int)time, NX - 1); written = true; }
+    }
+    *out = v;
+    return written;
+}
+
+__device__ __forceinline__ double floor_clamp(const DevParams &p, double v)
+{
+    if (v > p.vmax) return p.vmax;
+    if (v < -p.vmax) return -p.vmax;
+    return v;
+}
+
+// compute_energy (wave_common.c:453-472) from double values of the five cells.
+__device__ __forceinline__ double cell_energy(const DevParams &p, double x, double psi, double e, double w,
+                                              double n, double s, int xy_nonzero)
+{
+    double v = S_(x, psi);
+    double a = S_(e, x), b = S_(x, w);
+    double gx2 = A_(M_(a, a), M_(b, b));
+    double c = S_(n, x), d = S_(x, s);
+    double gy2 = A_(M_(c, c), M_(d, d));
+    if (xy_nonzero) return M_(p.e_scale2, A_(M_(v, v), M_(p.ehalf_c2, A_(gx2, gy2))));
+    if (p.twospeeds) return M_(p.e_scale2, A_(M_(v, v), M_(p.ehalf_c2b, A_(gx2, gy2))));
+    return 0.0;
+}
+
+// Neumaier-compensated accumulator.
+struct Neu {
+    double s, c;
+    __device__ __forceinline__ Neu() : s(0.0), c(0.0) {}
+    __device__ __forceinline__ void add(double x)
+    {
+        double t = A_(s, x);
+        if (fabs(s) >= fabs(x)) c = A_(c, A_(S_(s, t), x));
+        else c = A_(c, A_(S_(x, t), s));
+        s = t;
+    }
+    __device__ __forceinline__ void merge(const Neu &o) { add(o.s); c = A_(c, o.c); }
+    __device__ __forceinline__ double value() const { return A_(s, c); }
+};
+
+}  // namespace wg

@@ -1,0 +1,60 @@
+// wg_internal.h — declarations shared by the library's translation units.
+#pragma once
+#include <cuda_runtime.h>
+#include <string>
+#include "../../include/wavegpu.h"
+#include "wg_device.cuh"
+
+namespace wg {
+
+template <class T>
+struct FastArgs {
+    const T *phi;        // level t
+    const T *psi;        // level t-1 (read at the cell itself only)
+    T *out;              // level t+1 (== psi for the in-place form)
+    const uint32_t *act; // "active" plane: bulk xy > 0, boundary lines xy != 0
+    const uint32_t *nz;  // "nonzero" plane: xy != 0
+    const T *tcc, *tc, *tg;  // WG_COEF_TABLE tables (tg may be null: uniform)
+    float c2f, c2bf, gamf, gambf, kappaf;
+    int has_ghosts;      // the mask has cells < 0 (Neumann ghosts)
+    int do_source;       // add the point source in this kernel
+};
+
+// error state (thread-local message)
+void set_error(const char *fmt, ...);
+wg_status cuda_fail(cudaError_t e, const char *what);
+#define WG_CUDA(call)                                       \
+    do {                                                    \
+        cudaError_t e_ = (call);                            \
+        if (e_ != cudaSuccess) return cuda_fail(e_, #call); \
+    } while (0)
+
+DevParams make_dev_params(const wg_params &p, int pitch);
+wg_status validate_params(const wg_params &p);
+int pitch_for(int ny, int elem_bytes);
+
+// launchers (wg_kernels.cu)
+void launch_step_exact(const DevParams &p, const double *phi, const double *psi, double *out, const int16_t *xy,
+                       const double *tcc, const double *tc, const double *tg, long long time, int do_source,
+                       cudaStream_t st);
+void launch_step_exact_energy(const DevParams &p, const double *phi, const double *psi, double *out,
+                              const int16_t *xy, long long time, cudaStream_t st);
+void launch_neumann_exact(const DevParams &p, const double *phi, double *out, const int16_t *xy,
+                          const wg_neumann_bc *rec, int n, cudaStream_t st);
+template <class T> void launch_point_source(const DevParams &p, T *out, long long time, cudaStream_t st);
+template <class T> void launch_step_fast(const DevParams &p, const FastArgs<T> &a, int coef_mode, long long time,
+                                         cudaStream_t st);
+template <class T> void launch_neumann_fast(const DevParams &p, const T *phi, T *out, const int4 *idx,
+                                            const double2 *w, int n, cudaStream_t st);
+template <class T> void launch_energy(const DevParams &p, const T *phi, const T *psi, const int16_t *xy,
+                                      const uint32_t *nz, double2 *bot, double2 *top, int ileft, int iright,
+                                      double *out, cudaStream_t st);
+template <class T> void launch_count_nonfinite(int nx, int ny, int pitch, const T *a, unsigned long long *count,
+                                               cudaStream_t st);
+void launch_pack_mask(int nx, int ny, int wpitch, const int16_t *xy, uint32_t *act, uint32_t *nz, cudaStream_t st);
+template <class T> void launch_convert_in(int nx, int ny, int pitch, const double *src, T *dst, cudaStream_t st);
+template <class T> void launch_convert_out(int nx, int ny, int pitch, const T *src, double *dst, cudaStream_t st);
+void launch_cell_energy(const DevParams &p, const double *phi, const double *psi, const int16_t *xy, int i, int j,
+                        double *out, cudaStream_t st);
+
+}  // namespace wg

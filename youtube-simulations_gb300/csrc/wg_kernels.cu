@@ -1,0 +1,563 @@
+// wg_kernels.cu — single-update stepping kernels, Neumann gather, point source,
+// energy reductions and small utility kernels for sm_103a.
+//
+//  k_step_exact   drop-in form: int16 mask, FP64 tables, three buffers, writes exactly
+//                 the cells wave_billiard.c:302-610 writes (bit-identical FP64).
+//  k_step_bulk    native form, interior rows: 1-bit masks, 16-byte vector loads along
+//                 j, in place (the new level overwrites psi), FP64 (reference
+//                 operation order) or FP32 (increment form).
+//  k_step_edge    native form, the four boundary lines and the point source.
+//  k_neumann      Neumann gather of wave_billiard.c:379-389 for the active records.
+//  k_energy_cols  compute_energy (wave_common.c:453-472) per cell, one warp per
+//                 column, FP64 Neumaier sums of j < ny/2 and j >= ny/2.
+//  k_energy_final total and the six compute_energy_tblr boxes from the columns.
+#include "wg_internal.h"
+#include "wg_cells.cuh"
+
+namespace wg {
+
+// ---------------------------------------------------------------------------
+// Exact drop-in kernel
+// ---------------------------------------------------------------------------
+__global__ void __launch_bounds__(256) k_step_exact(DevParams p, const double *__restrict__ phi,
+                                                    const double *__restrict__ psi, double *__restrict__ out,
+                                                    const int16_t *__restrict__ xy, const double *__restrict__ tcc,
+                                                    const double *__restrict__ tc, const double *__restrict__ tg,
+                                                    long long time, int do_source)
+{
+    const int j = blockIdx.x * blockDim.x + threadIdx.x;
+    const int i = blockIdx.y * blockDim.y + threadIdx.y;
+    if (i >= p.nx || j >= p.ny) return;
+    const size_t c = (size_t)i * p.pitch + j;
+    const int m = xy[c];
+    double v = 0.0;
+    bool w;
+    if (i == 0 || i == p.nx - 1 || j == 0 || j == p.ny - 1) {
+        Field<double> PHI{phi, p.pitch}, PSI{psi, p.pitch};
+        ActI16 ACT{xy, p.pitch};
+        CoefTab<double> CF{tcc, tc, tg, p.pitch, 0.0};
+        w = edge_cell<double>(p, time, i, j, PHI, PSI, ACT, CF, &v);
+    } else {
+        w = p.twospeeds || m > 0;
+        if (w) {
+            const double x = phi[c], y = psi[c];
+            double delta = A_(A_(A_(phi[c + p.pitch], phi[c - p.pitch]), phi[c + 1]), phi[c - 1]);
+            delta = S_(delta, M_(4.0, x));
+            v = upd64(x, y, tcc[c], delta, p.kappa, tg[c]);
+        }
+    }
+    if (p.floor_clamp && m != 0) {
+        if (!w) { v = out[c]; w = true; }
+        v = floor_clamp(p, v);
+    }
+    if (do_source && p.src_on && i == p.src_i && j == p.src_j) {
+        if (!w) { v = out[c]; w = true; }
+        v = A_(v, point_source(p, time));
+    }
+    if (w) out[c] = v;
+}
+
+// wave_energy's stepper (wave_energy.c:662-913) on the half domain j < ny/2, with
+// its tables built from the mask (wave_energy.c:670-697).  The OSCILLATE_TOPBOT
+// branch of that file reads outside its tables and is rejected on the host.
+__global__ void __launch_bounds__(256) k_step_exact_energy(DevParams p, const double *__restrict__ phi,
+                                                           const double *__restrict__ psi, double *__restrict__ out,
+                                                           const int16_t *__restrict__ xy, long long time)
+{
+    const int j = blockIdx.x * blockDim.x + threadIdx.x;
+    const int i = blockIdx.y * blockDim.y + threadIdx.y;
+    const int NX = p.nx, jmid = p.ny / 2;
+    if (i >= NX || j >= jmid) return;
+    const int P = p.pitch;
+    auto PHI = [&](int a, int b) { return phi[(size_t)a * P + b]; };
+    auto XY = [&](int a, int b) { return (int)xy[(size_t)a * P + b]; };
+    auto TCC = [&](int a, int b) { return XY(a, b) ? p.c2 : (p.twospeeds ? p.c2b : 0.0); };
+    auto TC = [&](int a, int b) { return XY(a, b) ? p.courant : (p.twospeeds ? p.courantb : 0.0); };
+    auto TG = [&](int a, int b) { return XY(a, b) ? p.gam : (p.twospeeds ? p.gamb : 0.0); };
+    const size_t c = (size_t)i * P + j;
+    const int m = XY(i, j);
+    const bool active = p.twospeeds || m != 0;
+    const double x = phi[c], y = psi[c];
+    double v = 0.0, delta;
+    bool w = false;
+    if (j == jmid - 1 || j == 0) {
+        const int jb = j, jn = (j == 0) ? 1 : jmid - 2, jw = (j == 0) ? jmid - 1 : 0;
+        if (i == 0 && j == jmid - 1 && p.osc_left) { v = osc_bc(p, (int)time, j); w = true; }
+        if (active) {
+            int ip, im;
+            switch (p.b_cond) {
+            case 0:
+                ip = i + 1; if (ip == NX) ip = NX - 1;
+                im = i - 1; if (im == -1) im = 0;
+                delta = S_(A_(A_(PHI(ip, jb), PHI(im, jb)), PHI(i, jn)), M_(3.0, x));
+                v = upd64(x, y, TCC(i, jb), delta, p.kappa, TG(i, jb));
+                break;
+            case 1:
+                ip = (i + 1) % NX; im = (i - 1) % NX; if (im < 0) im += NX;
+                delta = S_(A_(A_(A_(PHI(ip, jb), PHI(im, jb)), PHI(i, jn)), PHI(i, jw)), M_(4.0, x));
+                v = upd64(x, y, TCC(i, jb), delta, p.kappa, TG(i, jb));
+                break;
+            case 2:
+                v = absorb64(x, y, TC(i, jb), PHI(i, jn), p.kappa_topbot, p.gamma_topbot);
+                break;
+            default:
+                ip = i + 1; if (ip == NX) ip = NX - 1;
+                im = i - 1; if (im == -1) im = 0;
+                if (i == 0) v = absorb64(x, y, TC(0, jb), PHI(1, jb), p.kappa_sides, p.gamma_sides);
+                else {
+                    delta = S_(A_(A_(A_(PHI(ip, jb), PHI(im, jb)), PHI(i, jn)), PHI(i, jw)), M_(4.0, x));
+                    v = upd64(x, y, TCC(i, jb), delta, p.kappa, TG(i, jb));
+                }
+                break;
+            }
+            w = true;
+        }
+    } else if (i == 0 && p.osc_left) {
+        v = osc_bc(p, (int)time, j);
+        w = true;
+    } else if (i == 0 || i == NX - 1) {
+        if (active) {
+            const int in = (i == 0) ? 1 : NX - 2, iw = (i == 0) ? NX - 1 : 0;
+            switch (p.b_cond) {
+            case 0:
+                delta = S_(A_(A_(PHI(in, j), PHI(i, j + 1)), PHI(i, j - 1)), M_(3.0, x));
+                v = upd64(x, y, TCC(i, j), delta, p.kappa, TG(i, j));
+                break;
+            case 1:
+                delta = S_(A_(A_(A_(PHI(in, j), PHI(iw, j)), PHI(i, j + 1)), PHI(i, j - 1)), M_(4.0, x));
+                v = upd64(x, y, TCC(i, j), delta, p.kappa, TG(i, j));
+                break;
+            default:
+                v = absorb64(x, y, TC(i, j), PHI(in, j), p.kappa_sides, p.gamma_sides);
+                break;
+            }
+            w = true;
+        }
+    } else if (active) {
+        delta = S_(A_(A_(A_(PHI(i + 1, j), PHI(i - 1, j)), PHI(i, j + 1)), PHI(i, j - 1)), M_(4.0, x));
+        v = upd64(x, y, TCC(i, j), delta, p.kappa, TG(i, j));
+        w = true;
+    }
+    if (p.floor_clamp && m != 0) {
+        if (!w) { v = out[c]; w = true; }
+        v = floor_clamp(p, v);
+    }
+    if (w) out[c] = v;
+}
+
+__global__ void k_cell_energy(DevParams p, const double *phi, const double *psi, const int16_t *xy, int i, int j,
+                              double *out)
+{
+    const int NX = p.nx, NY = p.ny, P = p.pitch;
+    const int ip = (i + 1 == NX) ? NX - 1 : i + 1, im = (i == 0) ? 0 : i - 1;
+    const int jp = (j + 1 == NY) ? NY - 1 : j + 1, jm = (j == 0) ? 0 : j - 1;
+    const size_t c = (size_t)i * P + j;
+    *out = cell_energy(p, phi[c], psi[c], phi[(size_t)ip * P + j], phi[(size_t)im * P + j], phi[(size_t)i * P + jp],
+                       phi[(size_t)i * P + jm], xy[c] != 0);
+}
+
+// Neumann gather for active records (drop-in form; records pre-validated to lie in
+// 1..nx-2 x 1..ny-2 with in-range neighbours).
+__global__ void k_neumann_exact(DevParams p, const double *__restrict__ phi, double *__restrict__ out,
+                                const int16_t *__restrict__ xy, const wg_neumann_bc *__restrict__ rec, int n)
+{
+    const int q = blockIdx.x * blockDim.x + threadIdx.x;
+    if (q >= n) return;
+    const wg_neumann_bc r = rec[q];
+    if (!r.active) return;
+    const size_t c = (size_t)r.i * p.pitch + r.j;
+    double v = M_(r.nx, phi[(size_t)r.nbi1 * p.pitch + r.nbj1]);
+    v = A_(v, M_(r.ny, phi[(size_t)r.nbi2 * p.pitch + r.nbj2]));
+    if (p.floor_clamp && xy[c] != 0) v = floor_clamp(p, v);
+    out[c] = v;
+}
+
+template <class T>
+__global__ void k_point_source(DevParams p, T *out, long long time)
+{
+    const size_t c = (size_t)p.src_i * p.pitch + p.src_j;
+    out[c] = (T)A_((double)out[c], point_source(p, time));
+}
+
+// ---------------------------------------------------------------------------
+// Fast native kernel
+// ---------------------------------------------------------------------------
+// Interior rows 1..nx-2 of one update, in place (the new level overwrites psi): each
+// thread updates V = 16/sizeof(T) consecutive cells of row i with every load (three
+// phi rows, psi, tcc, the j-1 / j+V neighbours, the mask word) issued before the
+// first use.  Boundary-line cells (j = 0, j = ny-1) and padding are written back
+// unchanged; k_step_edge computes them afterwards.
+template <class T, int COEF>
+__global__ void __launch_bounds__(256) k_step_bulk(const __grid_constant__ DevParams p,
+                                                   const __grid_constant__ FastArgs<T> a)
+{
+    constexpr int V = Vec<T>::n;
+    const int i = 1 + blockIdx.y * blockDim.y + threadIdx.y;
+    const int j0 = (blockIdx.x * blockDim.x + threadIdx.x) * V;
+    if (i >= p.nx - 1 || j0 >= p.pitch) return;
+    const size_t row = (size_t)i * p.pitch;
+    T c[V], y[V], n[V], s[V], cc[V];
+    vload(a.phi + row + j0, c);
+    vload(a.psi + row + j0, y);
+    vload(a.phi + row + p.pitch + j0, n);
+    vload(a.phi + row - p.pitch + j0, s);
+    if (COEF == WG_COEF_TABLE) vload(a.tcc + row + j0, cc);
+    const T wl = (j0 > 0) ? a.phi[row + j0 - 1] : (T)0;
+    const T er = (j0 + V < p.pitch) ? a.phi[row + j0 + V] : (T)0;
+    const uint32_t word = a.act[(size_t)i * p.wpitch + (j0 >> 5)] >> (j0 & 31);
+    uint32_t nzw = 0;
+    if (p.floor_clamp && a.has_ghosts) nzw = a.nz[(size_t)i * p.wpitch + (j0 >> 5)] >> (j0 & 31);
+    T out[V];
+#pragma unroll
+    for (int k = 0; k < V; k++) {
+        const int j = j0 + k;
+        T v = y[k];
+        const bool act = (word >> k) & 1u;
+        if (j >= 1 && j < p.ny - 1 && (p.twospeeds || act)) {
+            const T x = c[k];
+            const T w = (k == 0) ? wl : c[k - 1];
+            const T e = (k == V - 1) ? er : c[k + 1];
+            if (sizeof(T) == 8) {
+                double delta = A_(A_(A_((double)n[k], (double)s[k]), (double)e), (double)w);
+                delta = S_(delta, M_(4.0, (double)x));
+                const double ccv = (COEF == WG_COEF_TABLE) ? (double)cc[k] : (act ? p.c2 : p.c2b);
+                double g;
+                if (COEF == WG_COEF_TABLE) g = a.tg ? (double)a.tg[row + j] : p.gam;
+                else g = act ? p.gam : p.gamb;
+                v = (T)upd64((double)x, (double)y[k], ccv, delta, p.kappa, g);
+            } else {
+                const float xf = (float)x;
+                const float delta = (((float)n[k] - xf) + ((float)s[k] - xf)) + (((float)e - xf) + ((float)w - xf));
+                const float ccv = (COEF == WG_COEF_TABLE) ? (float)cc[k] : (act ? a.c2f : a.c2bf);
+                float g;
+                if (COEF == WG_COEF_TABLE) g = a.tg ? (float)a.tg[row + j] : a.gamf;
+                else g = act ? a.gamf : a.gambf;
+                v = (T)upd32(xf, (float)y[k], ccv, delta, a.kappaf, g);
+            }
+            if (p.floor_clamp && (act || ((nzw >> k) & 1u))) v = (T)floor_clamp(p, (double)v);
+        } else if (p.floor_clamp && ((nzw >> k) & 1u) && j >= 1 && j < p.ny - 1) {
+            v = (T)floor_clamp(p, (double)v);
+        }
+        out[k] = v;
+    }
+    vstore(a.out + row + j0, out);
+}
+
+// The four boundary lines of one update (one thread per cell, reference rules) and,
+// in the last thread, the point source when it lies inside; runs after k_step_bulk
+// on the same in-place level (boundary cells read only phi and their own psi).
+template <class T, int COEF>
+__global__ void __launch_bounds__(256) k_step_edge(const __grid_constant__ DevParams p,
+                                                   const __grid_constant__ FastArgs<T> a, long long time)
+{
+    const int idx = blockIdx.x * blockDim.x + threadIdx.x;
+    const int NX = p.nx, NY = p.ny;
+    const int nedge = 2 * NX + 2 * (NY - 2);
+    int i, j;
+    if (idx < NX) { i = idx; j = 0; }
+    else if (idx < 2 * NX) { i = idx - NX; j = NY - 1; }
+    else if (idx < 2 * NX + (NY - 2)) { i = 0; j = idx - 2 * NX + 1; }
+    else if (idx < nedge) { i = NX - 1; j = idx - 2 * NX - (NY - 2) + 1; }
+    else {
+        if (idx == nedge && a.do_source && p.src_on && p.src_i > 0 && p.src_i < NX - 1 && p.src_j > 0 &&
+            p.src_j < NY - 1) {
+            const size_t o = (size_t)p.src_i * p.pitch + p.src_j;
+            a.out[o] = (T)A_((double)a.out[o], point_source(p, time));
+        }
+        return;
+    }
+    const size_t o = (size_t)i * p.pitch + j;
+    T v = fast_edge<T, COEF>(p, a, i, j, time, a.psi[o]);
+    if (a.do_source && p.src_on && i == p.src_i && j == p.src_j) v = (T)A_((double)v, point_source(p, time));
+    a.out[o] = v;
+}
+
+// Native Neumann gather: active records only, in place on the new level.
+template <class T>
+__global__ void k_neumann_fast(DevParams p, const T *__restrict__ phi, T *__restrict__ out,
+                               const int4 *__restrict__ idx, const double2 *__restrict__ w, int n)
+{
+    const int q = blockIdx.x * blockDim.x + threadIdx.x;
+    if (q >= n) return;
+    const int4 r = idx[q];       // cell, nb1, nb2 (element offsets), flags (bit0 floor)
+    const double2 cw = w[q];
+    double v = M_(cw.x, (double)phi[r.y]);
+    v = A_(v, M_(cw.y, (double)phi[r.z]));
+    if (p.floor_clamp && (r.w & 1)) v = floor_clamp(p, v);
+    out[r.x] = (T)v;
+}
+
+// ---------------------------------------------------------------------------
+// Energy
+// ---------------------------------------------------------------------------
+template <class T>
+__device__ __forceinline__ void warp_merge(Neu &a)
+{
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1) {
+        Neu o;
+        o.s = __shfl_down_sync(0xffffffffu, a.s, off);
+        o.c = __shfl_down_sync(0xffffffffu, a.c, off);
+        a.merge(o);
+    }
+}
+
+// compute_energy in FP32 for FP32 fields (same formula and order as cell_energy).
+__device__ __forceinline__ float cell_energy32(float es2, float hc2, float hc2b, int twospeeds, float x, float psi,
+                                               float e, float w, float n, float s, int m)
+{
+    float v = x - psi;
+    float a = e - x, b = x - w, c = n - x, d = x - s;
+    float g = (a * a + b * b) + (c * c + d * d);
+    if (m) return es2 * (v * v + hc2 * g);
+    if (twospeeds) return es2 * (v * v + hc2b * g);
+    return 0.0f;
+}
+
+// One warp per column i.  MASK: 0 = int16 (xy != 0), 1 = "nonzero" bit plane.
+// Per cell compute_energy (wave_common.c:453-472): FP64 for FP64 fields, FP32 for
+// FP32 fields.  Each lane sums its cells in FP64; lanes and columns are combined
+// with Neumaier-compensated FP64 sums.  Outputs the j < ny/2 and j >= ny/2 sums.
+template <class T, int MASK>
+__global__ void __launch_bounds__(256) k_energy_cols(const __grid_constant__ DevParams p, const T *__restrict__ phi,
+                                                     const T *__restrict__ psi, const int16_t *__restrict__ xy,
+                                                     const uint32_t *__restrict__ nz, double2 *__restrict__ bot,
+                                                     double2 *__restrict__ top)
+{
+    const int i = blockIdx.x * (blockDim.x / 32) + threadIdx.x / 32;
+    const int lane = threadIdx.x & 31;
+    if (i >= p.nx) return;
+    const int NX = p.nx, NY = p.ny, jmid = NY / 2;
+    const size_t row = (size_t)i * p.pitch;
+    const int ip = (i + 1 == NX) ? NX - 1 : i + 1, im = (i == 0) ? 0 : i - 1;
+    const T *re = phi + (size_t)ip * p.pitch, *rw = phi + (size_t)im * p.pitch, *rc = phi + row, *ry = psi + row;
+    const float es2 = (float)p.e_scale2, hc2 = (float)p.ehalf_c2, hc2b = (float)p.ehalf_c2b;
+    double pb = 0.0, pt = 0.0;
+    for (int j = lane; j < NY; j += 32) {
+        const int jp = (j + 1 == NY) ? NY - 1 : j + 1, jm = (j == 0) ? 0 : j - 1;
+        int m;
+        if (MASK == 0) m = xy[row + j] != 0;
+        else m = (nz[(size_t)i * p.wpitch + (j >> 5)] >> (j & 31)) & 1u;
+        double en;
+        if (sizeof(T) == 8)
+            en = cell_energy(p, (double)rc[j], (double)ry[j], (double)re[j], (double)rw[j], (double)rc[jp],
+                             (double)rc[jm], m);
+        else
+            en = (double)cell_energy32(es2, hc2, hc2b, p.twospeeds, (float)rc[j], (float)ry[j], (float)re[j],
+                                       (float)rw[j], (float)rc[jp], (float)rc[jm], m);
+        if (j < jmid) pb += en; else pt += en;
+    }
+    Neu sb, st;
+    sb.add(pb);
+    st.add(pt);
+    warp_merge<T>(sb);
+    warp_merge<T>(st);
+    if (lane == 0) {
+        bot[i] = make_double2(sb.s, sb.c);
+        top[i] = make_double2(st.s, st.c);
+    }
+}
+
+// out[0] = total, out[1..6] = boxes (top left/mid/right, bottom left/mid/right),
+// out[7..7+nx) = column sums over j < ny/2.  One block of 1024 threads.
+__global__ void __launch_bounds__(1024) k_energy_final(int nx, int ileft, int iright, const double2 *__restrict__ bot,
+                                                       const double2 *__restrict__ top, double *__restrict__ out)
+{
+    __shared__ double sh_s[7][32], sh_c[7][32];
+    Neu acc[7];  // 0 total, 1..3 top boxes, 4..6 bottom boxes
+    for (int i = threadIdx.x; i < nx; i += blockDim.x) {
+        const double2 b = bot[i], t = top[i];
+        Neu nb, nt;
+        nb.s = b.x; nb.c = b.y;
+        nt.s = t.x; nt.c = t.y;
+        out[7 + i] = nb.value();
+        const int box = (i < ileft) ? 0 : (i < iright ? 1 : 2);
+        acc[0].merge(nb);
+        acc[0].merge(nt);
+        acc[1 + box].merge(nt);
+        acc[4 + box].merge(nb);
+    }
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+#pragma unroll
+    for (int k = 0; k < 7; k++) {
+        warp_merge<double>(acc[k]);
+        if (lane == 0) { sh_s[k][wid] = acc[k].s; sh_c[k][wid] = acc[k].c; }
+    }
+    __syncthreads();
+    if (wid == 0) {
+        const int nw = blockDim.x >> 5;
+#pragma unroll
+        for (int k = 0; k < 7; k++) {
+            Neu a;
+            if (lane < nw) { a.s = sh_s[k][lane]; a.c = sh_c[k][lane]; }
+            warp_merge<double>(a);
+            if (lane == 0) out[k] = a.value();
+        }
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Utilities
+// ---------------------------------------------------------------------------
+template <class T>
+__global__ void k_count_nonfinite(int nx, int ny, int pitch, const T *__restrict__ a, unsigned long long *count)
+{
+    unsigned long long local = 0;
+    const size_t total = (size_t)nx * pitch;
+    for (size_t c = blockIdx.x * (size_t)blockDim.x + threadIdx.x; c < total; c += (size_t)gridDim.x * blockDim.x) {
+        const int j = (int)(c % pitch);
+        if (j < ny && !isfinite((double)a[c])) local++;
+    }
+    if (local) atomicAdd(count, local);
+}
+
+// Packs the int16 mask into the "active" plane (bulk test xy > 0, boundary-line test
+// xy != 0) and the "nonzero" plane (xy != 0).  One thread per 32-bit word.
+__global__ void k_pack_mask(int nx, int ny, int wpitch, const int16_t *__restrict__ xy, uint32_t *__restrict__ act,
+                            uint32_t *__restrict__ nz)
+{
+    const int wj = blockIdx.x * blockDim.x + threadIdx.x;
+    const int i = blockIdx.y;
+    if (wj >= wpitch || i >= nx) return;
+    uint32_t a = 0, z = 0;
+    for (int b = 0; b < 32; b++) {
+        const int j = wj * 32 + b;
+        if (j >= ny) break;
+        const int m = xy[(size_t)i * ny + j];
+        const bool edge = (i == 0 || i == nx - 1 || j == 0 || j == ny - 1);
+        if (edge ? (m != 0) : (m > 0)) a |= 1u << b;
+        if (m != 0) z |= 1u << b;
+    }
+    act[(size_t)i * wpitch + wj] = a;
+    nz[(size_t)i * wpitch + wj] = z;
+}
+
+// Dense FP64 [nx][ny] -> pitched T [nx][pitch] (padding zeroed).
+template <class T>
+__global__ void k_convert_in(int nx, int ny, int pitch, const double *__restrict__ src, T *__restrict__ dst)
+{
+    const int j = blockIdx.x * blockDim.x + threadIdx.x;
+    const int i = blockIdx.y;
+    if (j >= pitch || i >= nx) return;
+    dst[(size_t)i * pitch + j] = (j < ny) ? (T)src[(size_t)i * ny + j] : (T)0;
+}
+template <class T>
+__global__ void k_convert_out(int nx, int ny, int pitch, const T *__restrict__ src, double *__restrict__ dst)
+{
+    const int j = blockIdx.x * blockDim.x + threadIdx.x;
+    const int i = blockIdx.y;
+    if (j >= ny || i >= nx) return;
+    dst[(size_t)i * ny + j] = (double)src[(size_t)i * pitch + j];
+}
+
+// ---------------------------------------------------------------------------
+// Host launchers
+// ---------------------------------------------------------------------------
+void launch_step_exact(const DevParams &p, const double *phi, const double *psi, double *out, const int16_t *xy,
+                       const double *tcc, const double *tc, const double *tg, long long time, int do_source,
+                       cudaStream_t st)
+{
+    dim3 blk(64, 4), grd((p.ny + 63) / 64, (p.nx + 3) / 4);
+    k_step_exact<<<grd, blk, 0, st>>>(p, phi, psi, out, xy, tcc, tc, tg, time, do_source);
+}
+
+void launch_step_exact_energy(const DevParams &p, const double *phi, const double *psi, double *out,
+                              const int16_t *xy, long long time, cudaStream_t st)
+{
+    dim3 blk(64, 4), grd((p.ny / 2 + 63) / 64, (p.nx + 3) / 4);
+    k_step_exact_energy<<<grd, blk, 0, st>>>(p, phi, psi, out, xy, time);
+}
+
+void launch_cell_energy(const DevParams &p, const double *phi, const double *psi, const int16_t *xy, int i, int j,
+                        double *out, cudaStream_t st)
+{
+    k_cell_energy<<<1, 1, 0, st>>>(p, phi, psi, xy, i, j, out);
+}
+
+void launch_neumann_exact(const DevParams &p, const double *phi, double *out, const int16_t *xy,
+                          const wg_neumann_bc *rec, int n, cudaStream_t st)
+{
+    if (n <= 0) return;
+    k_neumann_exact<<<(n + 255) / 256, 256, 0, st>>>(p, phi, out, xy, rec, n);
+}
+
+template <class T>
+void launch_point_source(const DevParams &p, T *out, long long time, cudaStream_t st)
+{
+    k_point_source<T><<<1, 1, 0, st>>>(p, out, time);
+}
+template void launch_point_source<float>(const DevParams &, float *, long long, cudaStream_t);
+template void launch_point_source<double>(const DevParams &, double *, long long, cudaStream_t);
+
+template <class T>
+void launch_step_fast(const DevParams &p, const FastArgs<T> &a, int coef_mode, long long time, cudaStream_t st)
+{
+    constexpr int V = Vec<T>::n;
+    dim3 blk(64, 4), grd((p.pitch / V + 63) / 64, (p.nx - 2 + 3) / 4);
+    const int nedge = 2 * p.nx + 2 * (p.ny - 2) + 1;
+    if (coef_mode == WG_COEF_MASK) {
+        k_step_bulk<T, WG_COEF_MASK><<<grd, blk, 0, st>>>(p, a);
+        k_step_edge<T, WG_COEF_MASK><<<(nedge + 255) / 256, 256, 0, st>>>(p, a, time);
+    } else {
+        k_step_bulk<T, WG_COEF_TABLE><<<grd, blk, 0, st>>>(p, a);
+        k_step_edge<T, WG_COEF_TABLE><<<(nedge + 255) / 256, 256, 0, st>>>(p, a, time);
+    }
+}
+template void launch_step_fast<float>(const DevParams &, const FastArgs<float> &, int, long long, cudaStream_t);
+template void launch_step_fast<double>(const DevParams &, const FastArgs<double> &, int, long long, cudaStream_t);
+
+template <class T>
+void launch_neumann_fast(const DevParams &p, const T *phi, T *out, const int4 *idx, const double2 *w, int n,
+                         cudaStream_t st)
+{
+    if (n <= 0) return;
+    k_neumann_fast<T><<<(n + 255) / 256, 256, 0, st>>>(p, phi, out, idx, w, n);
+}
+template void launch_neumann_fast<float>(const DevParams &, const float *, float *, const int4 *, const double2 *, int, cudaStream_t);
+template void launch_neumann_fast<double>(const DevParams &, const double *, double *, const int4 *, const double2 *, int, cudaStream_t);
+
+template <class T>
+void launch_energy(const DevParams &p, const T *phi, const T *psi, const int16_t *xy, const uint32_t *nz,
+                   double2 *bot, double2 *top, int ileft, int iright, double *out, cudaStream_t st)
+{
+    const int warps = 8;
+    dim3 grd((p.nx + warps - 1) / warps);
+    if (xy) k_energy_cols<T, 0><<<grd, warps * 32, 0, st>>>(p, phi, psi, xy, nz, bot, top);
+    else k_energy_cols<T, 1><<<grd, warps * 32, 0, st>>>(p, phi, psi, xy, nz, bot, top);
+    k_energy_final<<<1, 1024, 0, st>>>(p.nx, ileft, iright, bot, top, out);
+}
+template void launch_energy<float>(const DevParams &, const float *, const float *, const int16_t *, const uint32_t *, double2 *, double2 *, int, int, double *, cudaStream_t);
+template void launch_energy<double>(const DevParams &, const double *, const double *, const int16_t *, const uint32_t *, double2 *, double2 *, int, int, double *, cudaStream_t);
+
+template <class T>
+void launch_count_nonfinite(int nx, int ny, int pitch, const T *a, unsigned long long *count, cudaStream_t st)
+{
+    k_count_nonfinite<T><<<4 * 152, 256, 0, st>>>(nx, ny, pitch, a, count);
+}
+template void launch_count_nonfinite<float>(int, int, int, const float *, unsigned long long *, cudaStream_t);
+template void launch_count_nonfinite<double>(int, int, int, const double *, unsigned long long *, cudaStream_t);
+
+void launch_pack_mask(int nx, int ny, int wpitch, const int16_t *xy, uint32_t *act, uint32_t *nz, cudaStream_t st)
+{
+    dim3 grd((wpitch + 127) / 128, nx);
+    k_pack_mask<<<grd, 128, 0, st>>>(nx, ny, wpitch, xy, act, nz);
+}
+
+template <class T>
+void launch_convert_in(int nx, int ny, int pitch, const double *src, T *dst, cudaStream_t st)
+{
+    dim3 grd((pitch + 255) / 256, nx);
+    k_convert_in<T><<<grd, 256, 0, st>>>(nx, ny, pitch, src, dst);
+}
+template <class T>
+void launch_convert_out(int nx, int ny, int pitch, const T *src, double *dst, cudaStream_t st)
+{
+    dim3 grd((ny + 255) / 256, nx);
+    k_convert_out<T><<<grd, 256, 0, st>>>(nx, ny, pitch, src, dst);
+}
+template void launch_convert_in<float>(int, int, int, const double *, float *, cudaStream_t);
+template void launch_convert_in<double>(int, int, int, const double *, double *, cudaStream_t);
+template void launch_convert_out<float>(int, int, int, const float *, double *, cudaStream_t);
+template void launch_convert_out<double>(int, int, int, const double *, double *, cudaStream_t);
+
+}  // namespace wg

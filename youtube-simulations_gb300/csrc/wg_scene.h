@@ -1,0 +1,55 @@
+// wg_scene.h — the native scene object and the temporal-blocking entry points.
+#pragma once
+#include <vector>
+#include "wg_internal.h"
+
+#define WG_TB_MAX_K 16
+
+struct wg_scene {
+    wg_params prm;
+    wg::DevParams dp;
+    int prec = WG_FP64, coef = WG_COEF_MASK;
+    cudaStream_t st = nullptr;
+    bool own_stream = false;
+    size_t esz = 8;
+    int pitch = 0;
+    void *f[2] = {nullptr, nullptr};  // f[cur] = phi (level t), f[1-cur] = psi (level t-1)
+    void *g[2] = {nullptr, nullptr};  // output pair of a temporally blocked pass (FP32)
+    int cur = 0;
+    uint32_t *act = nullptr, *nz = nullptr;
+    int has_ghosts = 0;
+    std::vector<int16_t> xy_host;
+    void *tcc = nullptr, *tc = nullptr, *tg = nullptr;
+    int4 *nidx = nullptr;
+    double2 *nw = nullptr;
+    int nrec = 0;
+    long long time = 0, launches = 0;
+    double2 *ebot = nullptr, *etop = nullptr;
+    double *eout = nullptr, *hout = nullptr;
+    unsigned long long *dcount = nullptr;
+    int *dflag = nullptr;          // set by a kernel whose bounded wait gave up
+    void *dstage = nullptr;
+    size_t dstage_bytes = 0;
+    void *hstage = nullptr;
+    size_t hstage_bytes = 0;
+    uint8_t *rgb = nullptr, *lut = nullptr;
+    size_t rgb_bytes = 0;
+    int tb_k = 0, tile_i = 0, tile_j = 0;
+    float *bv_osc = nullptr, *bv_src = nullptr;  // boundary values of the current step() call
+    size_t bv_cap = 0;
+    long long bv_t0 = 0;
+    bool uploaded = false;
+};
+
+namespace wg {
+wg_status scene_alloc_dense_stage(wg_scene *s, size_t bytes);
+size_t scene_device_bytes(const wg_params &p, int prec, int coef);
+template <class T> wg_status scene_step_impl(wg_scene *s, int nsteps);
+// temporal blocking (wg_tb.cu)
+bool tb_supported(const wg_scene *s);
+template <class T> wg_status tb_pass(wg_scene *s, int k);
+int tb_pass_depth(int k, int remaining);
+wg_status tb_prepare(wg_scene *s, int n);
+wg_status scene_check_flag(wg_scene *s);
+void autotune_scene(wg_scene *s);
+}  // namespace wg

@@ -1,0 +1,582 @@
+// wg_tb.cu — temporal blocking of the FP32 leapfrog stepper, and its autotuner.
+//
+// k_step_tb<COEF>: one CTA owns an extended tile of L rows (i) x W columns (j, W =
+// blockDim.x = 128 or 256; L = 16..64), i.e. a core of (L-2K) x (W-2K) cells plus a
+// halo of K.  Both time levels of the tile sit in shared memory; K in-place leapfrog
+// updates run on the shrinking region [s, L-s) x [s, W-s) (the new level overwrites
+// psi at the cell itself, as in the single-step form, so a sub-step has no hazards),
+// each thread marching down its column with the i+-1 neighbours in a register window
+// (4 shared loads and 1 shared store per cell update).  Then the core of both levels
+// is stored.  HBM traffic per K updates: one read of phi, psi (and the tcc table) over
+// the extended tile and one write of both levels over the core.
+//
+// The per-cell rules are the reference's (wave_billiard.c:361-590) for the boundary
+// conditions whose stencils stay inside the tile: the mirror "Dirichlet" box edges,
+// absorbing edges, OSCILLATE_LEFT / OSCILLATE_TOPBOT, FLOOR and the point source.
+// Periodic and VPER_HABS boundaries (which read the opposite side of the grid) and
+// Neumann gathers use the single-step kernel.
+#include <algorithm>
+#include <map>
+#include <mutex>
+#include <tuple>
+#include "wg_scene.h"
+#include "wg_tma.cuh"
+
+namespace wg {
+
+
+constexpr int TB_AW = 12;  // mask words loaded per tile row (covers 256 + 3*32 columns)
+
+struct TbArgs {
+    const float *phi, *psi;   // levels t, t-1
+    float *phi_out, *psi_out; // levels t+K, t+K-1 (distinct buffers)
+    const uint32_t *act;      // active plane
+    const float *tcc, *tc;    // tables (WG_COEF_TABLE)
+    float c2, c2b, gam, gamb, kappa, ks, kt, gs, gt, vmax, courant, courantb;
+    long long t0;             // step counter before the pass
+    const float *osc;         // oscillating_bc values of the pass, [K][ny]
+    const float *src;         // point-source increments of the pass, [K]
+    int *err;                 // set to 1 when a bounded wait gives up
+};
+
+// FP32 value of one boundary-line or point-source cell after update t, with the
+// reference rules for non-wrapping boundaries (wave_billiard.c:393-590): the mirror
+// "Dirichlet" edge and OSCILLATE_TOPBOT rows are the bulk update with the missing
+// neighbours replaced by the cell itself, absorbing edges use their inward neighbour,
+// oscillating cells take the precomputed oscillating_bc value.  Returns the old psi
+// value y where the reference writes nothing.
+template <int COEF>
+__device__ __forceinline__ float tb_general(const DevParams &p, const TbArgs &a, int gi, int gj, int s, float x,
+                                            float y, float nip, float nim, float njp, float njm, float cc, int act)
+{
+    const int NX = p.nx, NY = p.ny;
+    const bool bi = (gi == 0 || gi == NX - 1), bj = (gj == 0 || gj == NY - 1);
+    int mode = 0;  // 0 leapfrog (mirrored neighbours), 1 absorbing, 2 oscillating value
+    float nb = 0.f, kk = 0.f, gg = 0.f;
+    if (bj) {
+        if (p.osc_topbot && ((double)gi < p.tb_shift) && gi < NX - 1 && gi > 0) {
+            njp = x;
+            njm = x;
+        } else if (p.b_cond == WG_BC_DIRICHLET) {
+            if (gi == NX - 1) nip = x;
+            if (gi == 0) nim = x;
+            if (gj == NY - 1) njp = x; else njm = x;
+        } else {
+            mode = 1;
+            nb = (gj == NY - 1) ? njm : njp;
+            kk = a.kt;
+            gg = a.gt;
+        }
+    } else if (bi) {
+        if (gi == 0 && left_bc(p, gj)) {
+            mode = 2;
+        } else if (p.b_cond == WG_BC_DIRICHLET) {
+            if (gi == 0) nim = x; else nip = x;
+        } else {
+            mode = 1;
+            nb = (gi == 0) ? nip : nim;
+            kk = a.ks;
+            gg = a.gs;
+        }
+    }
+    if (p.osc_left && !p.beam && gi == 0 && (gj == 0 || (p.corner2_on && gj == NX - 1))) mode = 2;
+    const bool w = (mode == 2) || p.twospeeds || act;
+    float v = y;
+    if (w) {
+        if (mode == 0) {
+            const float ccv = (COEF == WG_COEF_TABLE) ? cc : (act ? a.c2 : a.c2b);
+            const float g = (COEF == WG_COEF_TABLE) ? a.gam : (act ? a.gam : a.gamb);
+            v = upd32(x, y, ccv, ((nip - x) + (nim - x)) + ((njp - x) + (njm - x)), a.kappa, g);
+        } else if (mode == 1) {
+            const float tcv = (COEF == WG_COEF_TABLE) ? a.tc[(size_t)gi * p.pitch + gj] : (act ? a.courant : a.courantb);
+            v = absorb32(x, y, tcv, nb, kk, gg);
+        } else {
+            v = a.osc[(size_t)(s - 1) * NY + gj];
+        }
+        if (p.floor_clamp && act) v = fminf(fmaxf(v, -a.vmax), a.vmax);
+    }
+    if (p.src_on && gi == p.src_i && gj == p.src_j) v += a.src[s - 1];
+    return v;
+}
+
+// One sub-step down this thread's column for a tile with no boundary-line or source
+// cell: rows [s, L-s), the i+-1 neighbours in a register window, shared-memory
+// addressing by constant offsets.  ACT: the cell's mask bit selects coefficients
+// and whether it is written (otherwise every cell is written with its tcc).
+template <int COEF, bool ACT>
+__device__ __forceinline__ void tb_rows_interior(const DevParams &p, const TbArgs &a, const float *__restrict__ P,
+                                                 float *__restrict__ Q, const float *__restrict__ Cs, int Bw, int c,
+                                                 int r0, int r1, uint64_t actb)
+{
+    int idx = r0 * Bw + c;
+    float up = P[idx - Bw], mid = P[idx];
+    uint64_t am = actb >> r0;
+    const int n = r1 - r0;
+#pragma unroll 4
+    for (int q = 0; q < n; q++, idx += Bw) {
+        const float dn = P[idx + Bw], e = P[idx + 1], w = P[idx - 1], y = Q[idx];
+        const float delta = ((dn - mid) + (up - mid)) + ((e - mid) + (w - mid));
+        float v;
+        if (!ACT) {
+            v = upd32(mid, y, Cs[idx], delta, a.kappa, a.gam);
+        } else {
+            const bool act = am & 1u;
+            am >>= 1;
+            const float ccv = (COEF == WG_COEF_TABLE) ? Cs[idx] : (act ? a.c2 : a.c2b);
+            const float g = (COEF == WG_COEF_TABLE) ? a.gam : (act ? a.gam : a.gamb);
+            v = y;
+            if (p.twospeeds || act) {
+                v = upd32(mid, y, ccv, delta, a.kappa, g);
+                if (p.floor_clamp && act) v = fminf(fmaxf(v, -a.vmax), a.vmax);
+            }
+        }
+        Q[idx] = v;
+        up = mid;
+        mid = dn;
+    }
+}
+
+// oscillating_bc(t0 + s, j) for s = 1..n (when OSCILLATE_LEFT) and the point-source
+// increment of update t0 + s, rounded to FP32, for the passes of one step() call.
+__global__ void k_boundary_values(const __grid_constant__ DevParams p, long long t0, int n, float *osc, float *src)
+{
+    const int idx = blockIdx.x * blockDim.x + threadIdx.x;
+    if (p.osc_left && idx < n * p.ny) {
+        const int s = idx / p.ny, j = idx % p.ny;
+        osc[idx] = (float)osc_bc(p, (int)(t0 + s + 1), j);
+    }
+    if (p.src_on && idx < n) src[idx] = (float)point_source(p, t0 + idx + 1);
+}
+
+// Shared-memory layout of one tile: F0, F1 (both levels), Cs (tcc, table mode),
+// Aw (the active-plane words covering the tile), one mbarrier.
+struct TbLayout {
+    int f0, f1, cs, aw, bar, bytes, tma_bytes;
+};
+__host__ __device__ inline TbLayout tb_layout(int coef, int L, int Bw)
+{
+    TbLayout t;
+    const int fb = L * Bw * 4;
+    t.f0 = 0;
+    t.f1 = fb;
+    t.cs = 2 * fb;
+    t.aw = (coef == WG_COEF_TABLE ? 3 : 2) * fb;
+    t.bar = t.aw + ((L * TB_AW * 4 + 15) / 16) * 16;
+    t.bytes = t.bar + 16;
+    t.tma_bytes = (coef == WG_COEF_TABLE ? 3 : 2) * fb + L * TB_AW * 4;
+    return t;
+}
+
+template <int COEF>
+__global__ void __launch_bounds__(256) k_step_tb(const __grid_constant__ DevParams p, const __grid_constant__ TbArgs a,
+                                                 const __grid_constant__ CUtensorMap m_phi,
+                                                 const __grid_constant__ CUtensorMap m_psi,
+                                                 const __grid_constant__ CUtensorMap m_tcc,
+                                                 const __grid_constant__ CUtensorMap m_act, int K, int Kh, int L)
+{
+    extern __shared__ __align__(1024) unsigned char smem[];
+    const int Bw = blockDim.x;
+    const TbLayout lay = tb_layout(COEF, L, Bw);
+    float *F0 = (float *)(smem + lay.f0), *F1 = (float *)(smem + lay.f1), *Cs = (float *)(smem + lay.cs);
+    const uint32_t *Aw = (const uint32_t *)(smem + lay.aw);
+    uint64_t *bar = (uint64_t *)(smem + lay.bar);
+    const int c = threadIdx.x;
+    const int core_w = Bw - 2 * Kh, core_h = L - 2 * K;
+    const int x0 = blockIdx.x * core_w - Kh;   // first column of the tile (a multiple of 4)
+    const int gi0 = blockIdx.y * core_h - K;   // first row of the tile
+    const int w0 = (x0 >> 5) & ~3;             // first mask word of the tile (a multiple of 4)
+    const int gj = x0 + c;
+    const bool col_ok = gj >= 0 && gj < p.ny;
+    const bool col_special = (gj == 0 || gj == p.ny - 1);
+
+    // TMA destinations must be 128-byte aligned; refuse (flag) rather than issue otherwise
+    if (smem_u32(smem) & 127u) {
+        if (c == 0) atomicExch(a.err, 2);
+        return;
+    }
+    // TMA: the extended tile of phi, psi (tcc) and the mask words, zero outside the grid
+    if (c == 0) {
+        mbar_init(bar, 1);
+        mbar_fence_init();
+    }
+    __syncthreads();
+    if (c == 0) {
+        mbar_arrive_expect_tx(bar, (unsigned)lay.tma_bytes);
+        tma_load_2d(F0, &m_phi, x0, gi0, bar);
+        tma_load_2d(F1, &m_psi, x0, gi0, bar);
+        if (COEF == WG_COEF_TABLE) tma_load_2d(Cs, &m_tcc, x0, gi0, bar);
+        tma_load_2d((void *)Aw, &m_act, w0, gi0, bar);
+    }
+    const bool ok = mbar_wait_bounded(bar, 0, 1u << 24);
+    if (__syncthreads_or(!ok)) {
+        // the copies did not land in time: flag it, let them drain (bounded), leave
+        if (c == 0) atomicExch(a.err, 1);
+        mbar_wait_bounded(bar, 0, 1u << 24);
+        return;
+    }
+
+    uint64_t actb = 0;
+    if (col_ok) {
+        const int wi = (gj >> 5) - w0;
+#pragma unroll 8
+        for (int r = 0; r < L; r++) actb |= (uint64_t)((Aw[r * TB_AW + wi] >> (gj & 31)) & 1u) << r;
+    }
+
+    // a tile with no boundary line and no source cell runs the lean interior loop
+    const bool interior_tile = gi0 >= 1 && gi0 + L <= p.nx - 1 && x0 >= 1 && x0 + Bw <= p.ny - 1 &&
+                               !(p.src_on && p.src_i >= gi0 && p.src_i < gi0 + L && p.src_j >= x0 && p.src_j < x0 + Bw);
+    const bool no_act = COEF == WG_COEF_TABLE && p.twospeeds && !p.floor_clamp;
+
+    for (int s = 1; s <= K; s++) {
+        const float *P = (s & 1) ? F0 : F1;  // phi level t+s-1
+        float *Q = (s & 1) ? F1 : F0;        // psi level t+s-2, becomes level t+s
+        const bool in_region = c >= Kh - K + s && c < Bw - Kh + K - s;
+        if (interior_tile) {
+            if (in_region) {
+                if (no_act) tb_rows_interior<COEF, false>(p, a, P, Q, Cs, Bw, c, s, L - s, actb);
+                else tb_rows_interior<COEF, true>(p, a, P, Q, Cs, Bw, c, s, L - s, actb);
+            }
+        } else if (col_ok && in_region && !col_special) {
+            // a boundary tile, interior column: lean segments between the special rows
+            // (gi = 0, gi = nx-1, the source row), the special rows one at a time
+            const int lo = max(s, -gi0), hi = min(L - s, p.nx - gi0);
+            const int ra = -gi0, rb = p.nx - 1 - gi0;
+            const int rs = (p.src_on && gj == p.src_j) ? p.src_i - gi0 : -1;
+            int r = lo;
+            while (r < hi) {
+                if (r == ra || r == rb || r == rs) {
+                    const int gi = gi0 + r;
+                    const float cc = (COEF == WG_COEF_TABLE) ? Cs[r * Bw + c] : 0.f;
+                    Q[r * Bw + c] = tb_general<COEF>(p, a, gi, gj, s, P[r * Bw + c], Q[r * Bw + c], P[(r + 1) * Bw + c],
+                                                     P[(r - 1) * Bw + c], P[r * Bw + c + 1], P[r * Bw + c - 1], cc,
+                                                     (int)((actb >> r) & 1u));
+                    r++;
+                } else {
+                    int nxt = hi;
+                    if (ra > r && ra < nxt) nxt = ra;
+                    if (rb > r && rb < nxt) nxt = rb;
+                    if (rs > r && rs < nxt) nxt = rs;
+                    if (no_act) tb_rows_interior<COEF, false>(p, a, P, Q, Cs, Bw, c, r, nxt, actb);
+                    else tb_rows_interior<COEF, true>(p, a, P, Q, Cs, Bw, c, r, nxt, actb);
+                    r = nxt;
+                }
+            }
+        } else if (col_ok && in_region) {
+            int r = s;
+            float up = P[(r - 1) * Bw + c], mid = P[r * Bw + c];
+#pragma unroll 4
+            for (; r < L - s; r++) {
+                const float dn = P[(r + 1) * Bw + c];
+                const int gi = gi0 + r;
+                if (gi >= 0 && gi < p.nx) {
+                    const float e = P[r * Bw + c + 1], w = P[r * Bw + c - 1];
+                    const float y = Q[r * Bw + c];
+                    const float cc = (COEF == WG_COEF_TABLE) ? Cs[r * Bw + c] : 0.f;
+                    const int act = (int)((actb >> r) & 1u);
+                    float v = y;
+                    if (col_special || gi == 0 || gi == p.nx - 1 || (p.src_on && gi == p.src_i && gj == p.src_j)) {
+                        v = tb_general<COEF>(p, a, gi, gj, s, mid, y, dn, up, e, w, cc, act);
+                    } else if (p.twospeeds || act) {
+                        const float ccv = (COEF == WG_COEF_TABLE) ? cc : (act ? a.c2 : a.c2b);
+                        const float g = (COEF == WG_COEF_TABLE) ? a.gam : (act ? a.gam : a.gamb);
+                        v = upd32(mid, y, ccv, ((dn - mid) + (up - mid)) + ((e - mid) + (w - mid)), a.kappa, g);
+                        if (p.floor_clamp && act) v = fminf(fmaxf(v, -a.vmax), a.vmax);
+                    }
+                    Q[r * Bw + c] = v;
+                }
+                up = mid;
+                mid = dn;
+            }
+        }
+        __syncthreads();
+    }
+
+    // store the core: level t+K and t+K-1
+    if (col_ok && c >= Kh && c < Bw - Kh) {
+        const float *newest = (K & 1) ? F1 : F0, *prev = (K & 1) ? F0 : F1;
+#pragma unroll 4
+        for (int r = K; r < L - K; r++) {
+            const int gi = gi0 + r;
+            if (gi < p.nx) {
+                const size_t o = (size_t)gi * p.pitch + gj;
+                a.phi_out[o] = newest[r * Bw + c];
+                a.psi_out[o] = prev[r * Bw + c];
+            }
+        }
+    }
+}
+
+static int tb_halo(int K) { return (K + 3) & ~3; }
+
+static bool tb_shape_ok(int K, int L, int W)
+{
+    return K >= 2 && K <= 8 && (W == 128 || W == 256) && L >= 16 && L <= 64 && (L % 2 == 0) && L - 2 * K >= 8 &&
+           W - 2 * tb_halo(K) >= 32 && tb_layout(WG_COEF_TABLE, L, W).bytes <= 200 * 1024;
+}
+
+// cuTensorMapEncodeTiled through the runtime's driver entry point (no libcuda link)
+typedef CUresult (*EncodeTiledFn)(CUtensorMap *, CUtensorMapDataType, cuuint32_t, void *, const cuuint64_t *,
+                                  const cuuint64_t *, const cuuint32_t *, const cuuint32_t *, CUtensorMapInterleave,
+                                  CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+
+static EncodeTiledFn encode_fn()
+{
+    static EncodeTiledFn fn = nullptr;
+    static std::once_flag once;
+    std::call_once(once, [] {
+        void *f = nullptr;
+        cudaDriverEntryPointQueryResult q;
+        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &f, 12000, cudaEnableDefault, &q) ==
+                cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+            fn = (EncodeTiledFn)f;
+    });
+    return fn;
+}
+
+// 2-D map over a pitched array of 4-byte elements: dims {cols, rows}, row stride bytes
+static bool make_map(CUtensorMap *m, const void *base, bool is_float, uint64_t cols, uint64_t rows, uint64_t stride,
+                     uint32_t box_cols, uint32_t box_rows)
+{
+    EncodeTiledFn fn = encode_fn();
+    if (!fn) return false;
+    cuuint64_t dims[2] = {cols, rows};
+    cuuint64_t strides[1] = {stride};
+    cuuint32_t box[2] = {box_cols, box_rows};
+    cuuint32_t es[2] = {1, 1};
+    return fn(m, is_float ? CU_TENSOR_MAP_DATA_TYPE_FLOAT32 : CU_TENSOR_MAP_DATA_TYPE_UINT32, 2, const_cast<void *>(base),
+              dims, strides, box, es, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
+              CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
+}
+
+struct TbMaps {
+    CUtensorMap phi, psi, tcc, act;
+};
+
+static bool tb_maps(wg_scene *s, const TbArgs &a, int L, int W, TbMaps *m)
+{
+    const uint64_t stride = (uint64_t)s->pitch * 4;
+    bool ok = make_map(&m->phi, a.phi, true, s->prm.ny, s->prm.nx, stride, W, L) &&
+              make_map(&m->psi, a.psi, true, s->prm.ny, s->prm.nx, stride, W, L) &&
+              make_map(&m->act, s->act, false, s->dp.wpitch, s->prm.nx, (uint64_t)s->dp.wpitch * 4, TB_AW, L);
+    if (ok && s->coef == WG_COEF_TABLE) ok = make_map(&m->tcc, a.tcc, true, s->prm.ny, s->prm.nx, stride, W, L);
+    else m->tcc = m->phi;
+    return ok;
+}
+
+static bool launch_tb(wg_scene *s, const TbArgs &a, int K, int L, int W)
+{
+    if (!tb_shape_ok(K, L, W)) return false;
+    const int Kh = tb_halo(K);
+    TbMaps m;
+    if (!tb_maps(s, a, L, W, &m)) {
+        set_error("cuTensorMapEncodeTiled failed");
+        return false;
+    }
+    const DevParams &p = s->dp;
+    dim3 grd((p.ny + (W - 2 * Kh) - 1) / (W - 2 * Kh), (p.nx + (L - 2 * K) - 1) / (L - 2 * K));
+    const size_t sm = tb_layout(s->coef, L, W).bytes;
+    static std::once_flag attr_once;  // raise the dynamic shared-memory limit once per process
+    std::call_once(attr_once, [] {
+        cudaFuncSetAttribute(k_step_tb<WG_COEF_TABLE>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
+        cudaFuncSetAttribute(k_step_tb<WG_COEF_MASK>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
+    });
+    if (s->coef == WG_COEF_TABLE)
+        k_step_tb<WG_COEF_TABLE><<<grd, W, sm, s->st>>>(p, a, m.phi, m.psi, m.tcc, m.act, K, Kh, L);
+    else
+        k_step_tb<WG_COEF_MASK><<<grd, W, sm, s->st>>>(p, a, m.phi, m.psi, m.tcc, m.act, K, Kh, L);
+    return true;
+}
+
+static bool tb_depth_ok(int k) { return k >= 2 && k <= 8; }
+
+bool tb_supported(const wg_scene *s)
+{
+    return s->prec == WG_FP32 && (s->prm.b_cond == WG_BC_DIRICHLET || s->prm.b_cond == WG_BC_ABSORBING) &&
+           s->nrec == 0 && !s->has_ghosts && (s->coef == WG_COEF_MASK || s->tg == nullptr);
+}
+
+static wg_status ensure_tb_buffers(wg_scene *s)
+{
+    const size_t fb = (size_t)s->prm.nx * s->pitch * s->esz;
+    for (int k = 0; k < 2; k++)
+        if (!s->g[k]) {
+            WG_CUDA(cudaMalloc(&s->g[k], fb));
+            WG_CUDA(cudaMemsetAsync(s->g[k], 0, fb, s->st));
+        }
+    return WG_OK;
+}
+
+wg_status tb_prepare(wg_scene *s, int n)
+{
+    if (!s->prm.oscillate_left && !s->prm.src_on) return WG_OK;
+    const size_t need = (size_t)n * (s->prm.oscillate_left ? s->prm.ny : 1);
+    if (need > s->bv_cap) {
+        if (s->bv_osc) cudaFree(s->bv_osc);
+        if (s->bv_src) cudaFree(s->bv_src);
+        s->bv_osc = s->bv_src = nullptr;
+        s->bv_cap = 0;
+        WG_CUDA(cudaMalloc(&s->bv_osc, need * sizeof(float)));
+        WG_CUDA(cudaMalloc(&s->bv_src, need * sizeof(float)));
+        s->bv_cap = need;
+    }
+    s->bv_t0 = s->time;
+    const int threads = 256, blocks = (int)((need + threads - 1) / threads);
+    k_boundary_values<<<blocks, threads, 0, s->st>>>(s->dp, s->time, n, s->bv_osc, s->bv_src);
+    s->launches++;
+    WG_CUDA(cudaGetLastError());
+    return WG_OK;
+}
+
+static TbArgs tb_args(wg_scene *s)
+{
+    TbArgs a;
+    a.phi = (const float *)s->f[s->cur];
+    a.psi = (const float *)s->f[1 - s->cur];
+    a.phi_out = (float *)s->g[0];
+    a.psi_out = (float *)s->g[1];
+    a.act = s->act;
+    a.tcc = (const float *)s->tcc;
+    a.tc = (const float *)s->tc;
+    a.c2 = (float)s->dp.c2;
+    a.c2b = (float)s->dp.c2b;
+    a.gam = (float)s->dp.gam;
+    a.gamb = (float)s->dp.gamb;
+    a.kappa = (float)s->dp.kappa;
+    a.ks = (float)s->dp.kappa_sides;
+    a.kt = (float)s->dp.kappa_topbot;
+    a.gs = (float)s->dp.gamma_sides;
+    a.gt = (float)s->dp.gamma_topbot;
+    a.vmax = (float)s->dp.vmax;
+    a.courant = (float)s->dp.courant;
+    a.courantb = (float)s->dp.courantb;
+    a.t0 = s->time;
+    const long long off = s->time - s->bv_t0;
+    a.osc = s->bv_osc ? s->bv_osc + off * s->prm.ny : nullptr;
+    a.src = s->bv_src ? s->bv_src + off : nullptr;
+    a.err = s->dflag;
+    return a;
+}
+
+template <>
+wg_status tb_pass<float>(wg_scene *s, int k)
+{
+    wg_status st = ensure_tb_buffers(s);
+    if (st) return st;
+    if (!tb_depth_ok(k)) { set_error("temporal block depth %d outside 2..8", k); return WG_ERR_INVALID; }
+    const int W = s->tile_j > 0 ? s->tile_j : 256, L = s->tile_i > 0 ? s->tile_i : 32;
+    TbArgs a = tb_args(s);
+    if (!launch_tb(s, a, k, L, W)) {
+        if (wg_last_error()[0] == 0) set_error("unsupported temporal block (depth %d, tile %d x %d)", k, L, W);
+        return WG_ERR_INVALID;
+    }
+    s->launches++;
+    // the pass's outputs become the scene's fields; the inputs become the next outputs
+    std::swap(s->f[s->cur], s->g[0]);
+    std::swap(s->f[1 - s->cur], s->g[1]);
+    s->time += k;
+    return WG_OK;
+}
+
+template <>
+wg_status tb_pass<double>(wg_scene *, int)
+{
+    set_error("temporal blocking is FP32 only");
+    return WG_ERR_STATE;
+}
+
+int tb_pass_depth(int k, int remaining)
+{
+    // largest compiled depth <= min(k, remaining); 0 = use single updates
+    const int m = std::min(std::min(k, remaining), 8);
+    return m >= 2 ? m : 0;
+}
+
+// ---------------------------------------------------------------------------
+// Autotuner: temporal-block depth and tile width per size class, measured once per
+// (size class, coefficient mode) with CUDA events on a copy of the scene's state.
+// ---------------------------------------------------------------------------
+static std::mutex g_tune_mu;
+static std::map<std::tuple<int, int, int, int>, std::tuple<int, int, int>> g_tune;
+
+static std::tuple<int, int, int, int> size_class(const wg_scene *s)
+{
+    auto lg = [](int v) { int c = 0; while ((1 << (c + 1)) <= v) c++; return c; };
+    return {lg(s->prm.nx), lg(s->prm.ny), s->coef, s->prm.b_cond};
+}
+
+void autotune_scene(wg_scene *s)
+{
+    if (!tb_supported(s)) {
+        s->tb_k = 1;
+        s->tile_i = s->tile_j = 0;
+        return;
+    }
+    const auto key = size_class(s);
+    {
+        std::lock_guard<std::mutex> lk(g_tune_mu);
+        auto it = g_tune.find(key);
+        if (it != g_tune.end()) {
+            std::tie(s->tb_k, s->tile_i, s->tile_j) = it->second;
+            return;
+        }
+    }
+    // save the state, time the candidates, restore the state
+    const size_t fb = (size_t)s->prm.nx * s->pitch * s->esz;
+    void *save[2] = {nullptr, nullptr};
+    bool ok = ensure_tb_buffers(s) == WG_OK;
+    for (int k = 0; k < 2 && ok; k++) ok = cudaMalloc(&save[k], fb) == cudaSuccess;
+    int best_k = 1, best_l = 0, best_w = 0;
+    if (ok) {
+        cudaMemcpyAsync(save[0], s->f[0], fb, cudaMemcpyDeviceToDevice, s->st);
+        cudaMemcpyAsync(save[1], s->f[1], fb, cudaMemcpyDeviceToDevice, s->st);
+        const long long t_save = s->time;
+        const int cur_save = s->cur;
+        cudaEvent_t e0, e1;
+        cudaEventCreate(&e0);
+        cudaEventCreate(&e1);
+        const int updates = 24;
+        float best = 1e30f;
+        struct Cand { int k, l, w; };
+        const Cand cands[] = {{1, 0, 0},    {2, 16, 256}, {3, 16, 256}, {4, 16, 256}, {4, 24, 256},
+                              {6, 24, 256}, {4, 32, 256}, {6, 32, 256}, {4, 32, 128}, {6, 32, 128}};
+        for (const Cand &c : cands) {
+            s->tb_k = c.k;
+            s->tile_i = c.l;
+            s->tile_j = c.w;
+            float ms_best = 1e30f;
+            for (int rep = 0; rep < 3; rep++) {
+                cudaEventRecord(e0, s->st);
+                scene_step_impl<float>(s, updates);
+                cudaEventRecord(e1, s->st);
+                cudaEventSynchronize(e1);
+                float ms = 0.f;
+                cudaEventElapsedTime(&ms, e0, e1);
+                if (rep > 0) ms_best = std::min(ms_best, ms);
+            }
+            if (ms_best < best * 0.97f) {
+                best = ms_best;
+                best_k = c.k;
+                best_l = c.l;
+                best_w = c.w;
+            }
+        }
+        cudaEventDestroy(e0);
+        cudaEventDestroy(e1);
+        s->cur = cur_save;
+        cudaMemcpyAsync(s->f[0], save[0], fb, cudaMemcpyDeviceToDevice, s->st);
+        cudaMemcpyAsync(s->f[1], save[1], fb, cudaMemcpyDeviceToDevice, s->st);
+        cudaStreamSynchronize(s->st);
+        s->time = t_save;
+    }
+    for (void *p : save)
+        if (p) cudaFree(p);
+    cudaGetLastError();
+    s->tb_k = best_k;
+    s->tile_i = best_l;
+    s->tile_j = best_w;
+    std::lock_guard<std::mutex> lk(g_tune_mu);
+    g_tune[key] = {best_k, best_l, best_w};
+}
+
+}  // namespace wg

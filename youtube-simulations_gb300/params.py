@@ -92,4 +92,5 @@ class WgFrameParams(ctypes.Structure):
         ("vshift", ctypes.c_double), ("vscale", ctypes.c_double),
         ("slope", ctypes.c_double), ("color_range", ctypes.c_double),
         ("scale", ctypes.c_double), ("fade_value", ctypes.c_double),
+        ("fade_in_obstacle", ctypes.c_int32), ("reserved", ctypes.c_int32),
     ]
