@@ -1,0 +1,55 @@
+"""Pins the oracle against outputs of the reference itself, recorded in
+tests/golden/reference_outputs.json by tests/golden/make_golden.py (the compiled
+reference run on the seeded inputs of tests/helpers.variant_inputs).  Runs without the
+reference checkout.  Exact hash equality is required; where a record involves
+oscillating_bc (cos/exp of the platform's libm), a different libm may move last bits,
+and the sums must then agree to 1e-12 relative."""
+import hashlib
+import json
+from pathlib import Path
+
+import numpy as np
+import pytest
+
+import oracle
+from helpers import variant_inputs
+
+GOLDEN = json.loads((Path(__file__).resolve().parent / "golden" / "reference_outputs.json").read_text())
+
+
+def digest(*arrays):
+    h = hashlib.sha256()
+    for a in arrays:
+        if a is None:
+            continue
+        h.update(np.ascontiguousarray(a).tobytes())
+    return h.hexdigest()
+
+
+@pytest.mark.parametrize("key", sorted(GOLDEN))
+def test_oracle_matches_recorded_reference(key):
+    rec = GOLDEN[key]
+    name, nsteps = rec["variant"], rec["nsteps"]
+    p, f, xy, nbc = variant_inputs(name, seed=rec["seed"])
+    assert digest(f["phi"], f["psi"], f["tmp"], f["tcc"], f["tc"], f["tgamma"], xy, nbc) == rec["input_sha256"]
+    if name.startswith("e_"):
+        bufs = [f["phi"].copy(), f["psi"].copy(), f["tmp"].copy()]
+        cur, prv, fre = 0, 1, 2
+        for s in range(1, nsteps + 1):
+            oracle.evolve_wave_half_energy(p, s, bufs[cur], bufs[prv], bufs[fre], xy)
+            cur, prv, fre = fre, cur, prv
+        got = dict(phi=bufs[cur], psi=bufs[prv], tmp=bufs[fre])
+    else:
+        new, prev, third, _ = oracle.run(p, f["phi"], f["psi"], f["tmp"], xy, f["tcc"], f["tc"], f["tgamma"],
+                                         nsteps, nbc=nbc)
+        got = dict(phi=new, psi=prev, tmp=third)
+        e = oracle.energy_total(p, new, prev, xy, compensated=False)
+        if not p.oscillate_left:
+            assert e.hex() == rec["energy"]
+    for k in ("phi", "psi", "tmp"):
+        if p.oscillate_left:
+            scale = max(rec["max_abs"][k], 1e-300)
+            assert abs(float(np.sum(got[k])) - rec["sum"][k]) <= 1e-12 * scale * got[k].size
+            assert abs(float(np.sum(got[k] ** 2)) - rec["sumsq"][k]) <= 1e-12 * max(rec["sumsq"][k], 1e-300)
+        else:
+            assert digest(got[k]) == rec["output_sha256"][k], k

@@ -13,7 +13,7 @@ from helpers import params_of, variant_inputs
 
 pytestmark = pytest.mark.skipif(not refio.available("s_dir"), reason="compiled reference absent")
 
-STEP_VARIANTS = [n for n, v in ref_variants.VARIANTS.items() if v["kind"] == "wb_fn"]
+STEP_VARIANTS = [n for n, v in ref_variants.VARIANTS.items() if v["kind"] == "wb_fn" and not v.get("dropin")]
 ENERGY_VARIANTS = [n for n, v in ref_variants.VARIANTS.items() if v["kind"] == "we_fn"]
 OSC_VARIANTS = [n for n, v in ref_variants.VARIANTS.items() if v["kind"] == "osc"]
 

@@ -15,7 +15,7 @@ from youtube_simulations_gb300 import scenes
 from youtube_simulations_gb300 import wavegpu as W
 
 pytestmark = pytest.mark.gpu
-STEP_VARIANTS = [n for n, v in ref_variants.VARIANTS.items() if v["kind"] == "wb_fn"]
+STEP_VARIANTS = [n for n, v in ref_variants.VARIANTS.items() if v["kind"] == "wb_fn" and not v.get("dropin")]
 
 
 def run_oracle(p, f, xy, nsteps, nbc=None):
