@@ -101,12 +101,19 @@ def dist_env():
 # ---------------------------------------------------------------------------
 # Reference arm: the reference's own CPU stepper
 # ---------------------------------------------------------------------------
+_REF_META = {}
+
+
 def reference_sample(updates, threads=None):
+    """Times `updates` updates of the reference's own stepper (compiled from its sources,
+    OpenMP on the host cores) on the workload's grid, discs, pulse and source."""
     sys.path.insert(0, str(ROOT / "oracle"))
     import refio
-    from youtube_simulations_gb300 import scenes
-    sc = scenes.config2(seed=0, nx=NX, ny=NY)
-    m = sc.meta
+    if not _REF_META:
+        _package()
+        from youtube_simulations_gb300 import scenes
+        _REF_META.update(scenes.config2(seed=0, nx=NX, ny=NY).meta)
+    m = _REF_META
     src = (m["source"][0], m["source"][1], 0.05, m["period"])
     el, _, th = refio.time_reference("c2", NX, NY, updates, m["discs"], m["centre"], src=src, threads=threads)
     return el, th
@@ -124,12 +131,14 @@ def run_reference(args):
         return 0
     threads = os.cpu_count()
     upd = args.ref_updates
-    for _ in range(args.warmup):
-        reference_sample(3, threads)
-    times = []
-    for _ in range(args.steps):
-        el, th = reference_sample(upd, threads)
-        times.append(el)
+    _package()
+    from youtube_simulations_gb300 import scenes
+    m = scenes.config2(seed=0, nx=NX, ny=NY).meta
+    src = (m["source"][0], m["source"][1], 0.05, m["period"])
+    # one process: the reference's own set-up once, then warm-up and timed segments
+    segs, _, th = refio.time_reference("c2", NX, NY, upd, m["discs"], m["centre"], src=src, threads=threads,
+                                       segments=args.warmup + args.steps + 1)
+    times = segs[-args.steps:] if len(segs) > args.steps else segs
     total = sum(times)
     value = CELLS * upd * len(times) / total / 1e9
     line = {"metric": METRIC, "value": value, "unit": METRIC, "n_gpus": args.gpus, "steps": args.steps,
@@ -189,6 +198,7 @@ def run_ours(args):
         barrier()
         l0 = s.launches()
         step_ms, energy_ms = 0.0, 0.0
+        energies = []
         clocks = Clocks(local)
         clocks.start()
         wall0 = time.perf_counter()
@@ -198,7 +208,7 @@ def run_ours(args):
             e0.record(stream)
             s.step(UPDATES_PER_STEP)
             e1.record(stream)
-            s.total_energy()
+            energies.append(s.total_energy())
             e2.record(stream)
             e2.synchronize()
             step_ms += e0.elapsed_time(e1)
@@ -206,14 +216,15 @@ def run_ours(args):
         barrier()
         wall = time.perf_counter() - wall0
         ck = clocks.stop()
-        return step_ms, energy_ms, wall, s.launches() - l0, ck
+        return step_ms, energy_ms, wall, s.launches() - l0, ck, energies
 
     results = {}
+    finals = {}
     for prec in (["fp32", "fp64"] if not args.fp32_only else ["fp32"]):
         s = make_scene(prec)
-        step_ms, energy_ms, wall, launches, ck = timed(s, args.steps, args.warmup)
+        step_ms, energy_ms, wall, launches, ck, energies = timed(s, args.steps, args.warmup)
         k, ti, tj = s.blocking()
-        e_final = s.total_energy()
+        finals[prec] = s.download()[0]
         s.close()
         t_ms = step_ms + energy_ms
         if world > 1:
@@ -221,13 +232,24 @@ def run_ours(args):
             torch.distributed.all_reduce(tt, op=torch.distributed.ReduceOp.MAX)
             t_ms = float(tt.item())
         updates = args.steps * UPDATES_PER_STEP
-        kernel_launches_per_step = UPDATES_PER_STEP / max(k, 1)
-        per_launch_s = step_ms / 1e3 / (args.steps * kernel_launches_per_step)
+        main_launches = args.steps * (UPDATES_PER_STEP // k if k > 1 else UPDATES_PER_STEP)
+        per_launch_s = step_ms / 1e3 / main_launches
         algo = bytes_per_cell_update(prec, "table") * CELLS * max(k, 1)
         results[prec] = dict(value=world * CELLS * updates / (t_ms / 1e3) / 1e9, ms=t_ms / args.steps,
                              step_ms=step_ms, energy_ms=energy_ms, wall=wall, launches=launches, clocks=ck,
                              blocking=(k, ti, tj), achieved_gbs=algo / per_launch_s / 1e9,
-                             bytes_per_update=bytes_per_cell_update(prec, "table"), energy=e_final)
+                             bytes_per_update=bytes_per_cell_update(prec, "table"), energies=energies)
+    accuracy = None
+    if "fp64" in results:
+        e32, e64 = results["fp32"]["energies"], results["fp64"]["energies"]
+        drift = max(abs(a - b) / abs(b) for a, b in zip(e32, e64))
+        f32, f64 = finals["fp32"], finals["fp64"]
+        accuracy = {"field_rel_err": float(abs(f32 - f64).max() / abs(f64).max()),
+                    "field_max_abs_err": float(abs(f32 - f64).max()),
+                    "energy_rel_drift_max": float(drift),
+                    "energy_rel_drift_final": float(abs(e32[-1] - e64[-1]) / abs(e64[-1])),
+                    "updates": args.steps * UPDATES_PER_STEP,
+                    "against": "the FP64 GPU form on the same run (bit-identical to the FP64 oracle in the parity tests)"}
 
     # end to end through the C ABI with pinned host buffers (FP32)
     s = make_scene("fp32")
@@ -243,7 +265,7 @@ def run_ours(args):
         W.check(lib.wg_scene_download(s.h, h_phi.data_ptr(), h_psi.data_ptr(), P.FP32))
     barrier()
     e2e_ms = 0.0
-    for _ in range(args.steps):
+    for _ in range(args.e2e_steps):
         flush.zero_()
         e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
         e0.record(stream)
@@ -260,7 +282,10 @@ def run_ours(args):
         tt = torch.tensor([e2e_ms], device=dev)
         torch.distributed.all_reduce(tt, op=torch.distributed.ReduceOp.MAX)
         e2e_ms = float(tt.item())
-    e2e_value = world * CELLS * args.steps * UPDATES_PER_STEP / (e2e_ms / 1e3) / 1e9
+    e2e_value = world * CELLS * args.e2e_steps * UPDATES_PER_STEP / (e2e_ms / 1e3) / 1e9
+
+    batch_res = run_batch(args, P, scenes, W, stream, rank) if not args.no_batch else None
+    serve_res = run_serving(args, P, scenes, W, stream, rank) if not args.no_serving else None
 
     if rank != 0:
         return 0
@@ -312,21 +337,113 @@ def run_ours(args):
                         "frac": r64["achieved_gbs"] / hbm, "temporal_block": r64["blocking"][0],
                         "gpu_launches": int(r64["launches"]), "clocks": r64["clocks"],
                         "bytes_per_cell_update": r64["bytes_per_update"]}
-    line["energy_final"] = {"fp32": r32["energy"], "fp64": r64["energy"] if r64 else None}
+    line["accuracy"] = accuracy
+    if batch_res:
+        line["batch"] = batch_res
+    if serve_res:
+        line["serving"] = serve_res
     print(json.dumps(line))
     return 0
+
+
+def run_batch(args, P, scenes, W, stream, rank):
+    """Uneven batch: 256 seeded instances, sizes log-uniform between 256x256 and
+    1280x720, ellipse/stadium/polygon/disc-array masks, Dirichlet or periodic 50/50,
+    COURANT U(0.05, 0.15), one pulse each; frames of 10 updates replayed as CUDA graphs."""
+    import numpy as np
+    import torch
+    rng = np.random.default_rng(1000 + rank)
+    members = [scenes.batch_member(rng) for _ in range(args.batch_instances)]
+    out = {}
+    for prec in ("fp32", "fp64"):
+        b = W.Batch(P.FP32 if prec == "fp32" else P.FP64, stream=stream.cuda_stream)
+        for m in members:
+            b.add(m.params, m.phi, m.psi, m.xy)
+        n_active, cells = b.count()
+        frames = args.batch_frames if prec == "fp32" else max(2, args.batch_frames // 5)
+        for _ in range(3):
+            b.step(10)
+        torch.cuda.synchronize()
+        l0 = b.launches()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for _ in range(frames):
+            b.step(10)
+        e1.record(stream)
+        e1.synchronize()
+        ms = e0.elapsed_time(e1)
+        e_check = b.energy(0)
+        out[prec] = {"value": cells * 10 * frames / (ms / 1e3) / 1e9, "unit": METRIC, "ms_per_frame": ms / frames,
+                     "gpu_launches": b.launches() - l0, "frames": frames}
+        b.close()
+    out["instances"] = n_active
+    out["cells"] = cells
+    out["workload"] = ("uneven batch: 256 instances log-uniform 256x256..1280x720, mixed masks, Dirichlet/periodic, "
+                       "one persistent kernel per update over a tile work queue, frame of 10 updates as a CUDA graph")
+    out["energy_check_instance0"] = e_check
+    return out
+
+
+def run_serving(args, P, scenes, W, stream, rank):
+    """Serving loop under a stated load: requests with sizes log-uniform between 256x256
+    and 2560x1440 and U(50, 500) frames of 10 updates each arrive as a seeded Poisson
+    process (rate per tick); the server admits them under a 150 GB HBM budget into the
+    running batch and returns a turbo-style RGB8 frame per scene per tick."""
+    import numpy as np
+    rng = np.random.default_rng(2000 + rank)
+    lut = np.random.default_rng(5).integers(0, 256, size=(256, 3), dtype=np.uint8)
+    n_req = args.serve_requests
+    arrivals = np.cumsum(rng.exponential(1.0 / args.serve_rate, n_req)).astype(int)
+    reqs = []
+    for k in range(n_req):
+        m = scenes.batch_member(rng, smin=(256, 256), smax=(2560, 1440))
+        frames = int(rng.integers(args.serve_frames_min, args.serve_frames_max + 1))
+        reqs.append((m, frames))
+    out = {}
+    srv = W.Server(lut, precision=P.FP32, steps_per_frame=10, hbm_budget=150 << 30, stream=stream.cuda_stream)
+    t0 = time.perf_counter()
+    tick, k = 0, 0
+    while k < n_req or srv.stats()["completed"] < n_req:
+        while k < n_req and arrivals[k] <= tick:
+            m, frames = reqs[k]
+            srv.submit(m.params, m.phi, m.psi, m.xy, frames)
+            k += 1
+        srv.tick()
+        tick += 1
+    wall = time.perf_counter() - t0
+    st = srv.stats()
+    srv.close()
+    out = {"frame_latency_p50_ms": st["frame_latency_p50_ms"], "frame_latency_p99_ms": st["frame_latency_p99_ms"],
+           "frame_latency_max_ms": st["frame_latency_max_ms"], "first_frame_p50_ms": st["first_frame_p50_ms"],
+           "first_frame_p99_ms": st["first_frame_p99_ms"], "frames": st["frames"], "ticks": st["ticks"],
+           "value": st["cell_updates"] / st["busy_seconds"] / 1e9, "unit": METRIC, "dtype": "f32",
+           "bytes_peak": st["bytes_peak"], "wall_s": wall,
+           "load": f"{n_req} requests, Poisson arrivals at {args.serve_rate} per tick, sizes log-uniform "
+                   f"256x256..2560x1440, U({args.serve_frames_min},{args.serve_frames_max}) frames of 10 updates, "
+                   "150 GB budget, RGB8 frames (size 2) to host each tick",
+           "latency": "per frame: tick start to every resident scene's RGB8 frame in host memory"}
+    return out
 
 
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--steps", type=int, default=100)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--k", type=int, default=0, help="temporal block depth (0 = autotuned)")
     ap.add_argument("--fp32-only", action="store_true")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--ref-updates", type=int, default=20, help="updates per reference step")
+    ap.add_argument("--e2e-steps", type=int, default=20)
+    ap.add_argument("--no-batch", action="store_true")
+    ap.add_argument("--no-serving", action="store_true")
+    ap.add_argument("--batch-instances", type=int, default=256)
+    ap.add_argument("--batch-frames", type=int, default=20)
+    ap.add_argument("--serve-requests", type=int, default=32)
+    ap.add_argument("--serve-rate", type=float, default=0.25)
+    ap.add_argument("--serve-frames-min", type=int, default=50)
+    ap.add_argument("--serve-frames-max", type=int, default=500)
     args = ap.parse_args()
     if args.warmup < 3:
         print("warning: fewer than 3 warm-up steps", file=sys.stderr)

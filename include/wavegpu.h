@@ -247,6 +247,50 @@ wg_status wg_batch_energy(wg_batch *b, int32_t slot, double *total);
 wg_status wg_batch_count(wg_batch *b, int32_t *n_active, int64_t *cells);
 wg_status wg_batch_launch_count(wg_batch *b, int64_t *n);
 
+/* ------------------------------------------------------------------------- */
+/* 4. Serving loop: continuous batching of scene requests under an HBM budget  */
+/* ------------------------------------------------------------------------- */
+typedef struct wg_server wg_server;
+typedef struct wg_server_config {
+    int32_t precision;        /* WG_FP32 or WG_FP64 */
+    int32_t steps_per_frame;  /* leapfrog updates per returned frame */
+    int32_t max_scenes;       /* resident scenes at most */
+    int32_t reserved;
+    uint64_t hbm_budget;      /* device bytes the resident scenes may hold */
+    wg_frame_params frame;    /* colour map of the returned frames */
+    uint8_t lut[768];         /* 256x3 palette bytes (the reference's turbo_srgb_bytes) */
+} wg_server_config;
+typedef struct wg_server_stats {
+    int64_t submitted, admitted, completed, queued, resident, frames, ticks;
+    double cell_updates;                  /* cell updates performed */
+    double busy_seconds;                  /* wall time inside wg_server_tick */
+    double frame_latency_p50_ms, frame_latency_p99_ms, frame_latency_max_ms;
+    double first_frame_p50_ms, first_frame_p99_ms;  /* submit -> first frame on the host */
+    uint64_t bytes_resident, bytes_peak;
+} wg_server_stats;
+enum { WG_REQ_QUEUED = 0, WG_REQ_RESIDENT = 1, WG_REQ_DONE = 2 };
+
+wg_status wg_server_create(const wg_server_config *cfg, void *stream, wg_server **out);
+wg_status wg_server_destroy(wg_server *s);
+/* Queues a scene request (mask values 0/1; the arrays are copied).  It is admitted at a
+ * later tick, first come first served, as soon as its device bytes fit the budget. */
+wg_status wg_server_submit(wg_server *s, const wg_params *p, const double *phi, const double *psi,
+                           const int16_t *xy, int32_t frames, int32_t keep_result, int64_t *request_id);
+/* One tick: admit what fits, advance every resident scene by one frame (one CUDA-graph
+ * launch for all of them), render and copy every scene's frame to host memory, retire
+ * finished requests.  *frames_out = frames produced. */
+wg_status wg_server_tick(wg_server *s, int32_t *frames_out);
+/* The latest frame of a request (valid until the next tick). */
+wg_status wg_server_frame(wg_server *s, int64_t request_id, uint8_t *rgb, int32_t *frame_index,
+                          int32_t *width, int32_t *height);
+/* Final phi/psi of a finished request submitted with keep_result. */
+wg_status wg_server_result(wg_server *s, int64_t request_id, double *phi, double *psi);
+wg_status wg_server_request_state(wg_server *s, int64_t request_id, int32_t *state, int32_t *frames_done);
+wg_status wg_server_get_stats(wg_server *s, wg_server_stats *out);
+/* Device bytes a request of these parameters holds while resident (what admission
+ * charges against the budget). */
+wg_status wg_server_request_bytes(wg_server *s, const wg_params *p, uint64_t *bytes);
+
 #ifdef __cplusplus
 }
 #endif

@@ -117,18 +117,20 @@ int main(int argc, char **argv)
         for (int i = 0; i < NX; i++) memcpy(psi[i], phi[i], sizeof(double) * NY);
         double **b[3] = {phi, psi, tmp};
         int cur = 0, prv = 1, fre = 2;
-        double t0 = omp_get_wtime();
-        if (!src_on && nsteps % 3 == 0) {
-            for (int64_t s = 0; s < nsteps / 3; s++) evolve_wave(phi, psi, tmp, xyrows, tcc, tc, tg, drv_nbc);
-        } else {
-            for (int64_t s = 0; s < nsteps; s++) {
+        const int64_t nseg = h[13] > 0 ? h[13] : 1;  /* timed segments of nsteps updates */
+        int64_t done = 0;
+        double *seg = calloc(nseg, sizeof(double));
+        for (int64_t g = 0; g < nseg; g++) {
+            double t0 = omp_get_wtime();
+            for (int64_t s = 0; s < nsteps; s++, done++) {
                 evolve_wave_half(b[cur], b[prv], b[fre], xyrows, tcc, tc, tg, drv_nbc);
-                if (src_on) b[fre][src_i][src_j] += src_amp * sin(6.283185307179586 * (double)(s + 1) / src_period);
+                if (src_on) b[fre][src_i][src_j] += src_amp * sin(6.283185307179586 * (double)(done + 1) / src_period);
                 int nc = fre, np = cur, nf = prv;
                 cur = nc; prv = np; fre = nf;
             }
+            seg[g] = omp_get_wtime() - t0;
+            elapsed += seg[g];
         }
-        elapsed = omp_get_wtime() - t0;
         double e = 0.0;
         for (int i = 0; i < NX; i++)
             for (int j = 0; j < NY; j++) e += compute_energy(b[cur], b[prv], xyrows, i, j);
@@ -136,6 +138,7 @@ int main(int argc, char **argv)
         wr(fo, &elapsed, sizeof elapsed);
         wr(fo, &e, sizeof e);
         wr(fo, &threads, sizeof threads);
+        wr(fo, seg, sizeof(double) * nseg);
         fclose(fo);
         return 0;
 #else

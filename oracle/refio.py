@@ -97,12 +97,15 @@ def run(variant, nx, ny, mode=STEP, nsteps=0, fields=None, xy=None, nbc=None, ci
     return out
 
 
-def time_reference(variant, nx, ny, nsteps, circles, centre, src=None, threads=None, timeout=900):
+def time_reference(variant, nx, ny, nsteps, circles, centre, src=None, threads=None, timeout=900, segments=1):
     """TIME mode: the reference builds its own inputs (init_wave_flat, init_ior_2d,
-    add_circular_wave) and times `nsteps` updates.  Returns (seconds, energy, threads)."""
+    add_circular_wave) once and times `segments` runs of `nsteps` updates each.
+    Returns (seconds, energy, threads), or with segments > 1 (per-segment seconds,
+    energy, threads)."""
     circles = np.asarray(circles, np.float64)[:, :3]
     hdr = np.zeros(16, np.int64)
     hdr[:7] = [0x57415645, nx, ny, TIME, nsteps, 0, len(circles)]
+    hdr[13] = segments
     hd = np.zeros(4)
     hd[2], hd[3] = centre
     if src is not None:
@@ -124,4 +127,6 @@ def time_reference(variant, nx, ny, nsteps, circles, centre, src=None, threads=N
         raw = fout.read_bytes()
     el, e = np.frombuffer(raw, np.float64, 2, 0)
     th = int(np.frombuffer(raw, np.int64, 1, 16)[0])
+    if segments > 1:
+        return np.frombuffer(raw, np.float64, segments, 24).tolist(), float(e), th
     return float(el), float(e), th

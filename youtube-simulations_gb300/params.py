@@ -94,3 +94,24 @@ class WgFrameParams(ctypes.Structure):
         ("scale", ctypes.c_double), ("fade_value", ctypes.c_double),
         ("fade_in_obstacle", ctypes.c_int32), ("reserved", ctypes.c_int32),
     ]
+
+
+class WgServerConfig(ctypes.Structure):
+    _fields_ = [
+        ("precision", ctypes.c_int32), ("steps_per_frame", ctypes.c_int32),
+        ("max_scenes", ctypes.c_int32), ("reserved", ctypes.c_int32),
+        ("hbm_budget", ctypes.c_uint64), ("frame", WgFrameParams),
+        ("lut", ctypes.c_uint8 * 768),
+    ]
+
+
+class WgServerStats(ctypes.Structure):
+    _fields_ = [
+        ("submitted", ctypes.c_int64), ("admitted", ctypes.c_int64), ("completed", ctypes.c_int64),
+        ("queued", ctypes.c_int64), ("resident", ctypes.c_int64), ("frames", ctypes.c_int64),
+        ("ticks", ctypes.c_int64), ("cell_updates", ctypes.c_double), ("busy_seconds", ctypes.c_double),
+        ("frame_latency_p50_ms", ctypes.c_double), ("frame_latency_p99_ms", ctypes.c_double),
+        ("frame_latency_max_ms", ctypes.c_double), ("first_frame_p50_ms", ctypes.c_double),
+        ("first_frame_p99_ms", ctypes.c_double), ("bytes_resident", ctypes.c_uint64),
+        ("bytes_peak", ctypes.c_uint64),
+    ]

@@ -85,6 +85,15 @@ SIGNATURES = {
     "wg_batch_energy": (_I32, [_V, _I32, ctypes.POINTER(_D)]),
     "wg_batch_count": (_I32, [_V, ctypes.POINTER(_I32), ctypes.POINTER(_I64)]),
     "wg_batch_launch_count": (_I32, [_V, ctypes.POINTER(_I64)]),
+    "wg_server_create": (_I32, [_V, _V, ctypes.POINTER(_V)]),
+    "wg_server_destroy": (_I32, [_V]),
+    "wg_server_submit": (_I32, [_V, _V, _V, _V, _V, _I32, _I32, ctypes.POINTER(_I64)]),
+    "wg_server_tick": (_I32, [_V, ctypes.POINTER(_I32)]),
+    "wg_server_frame": (_I32, [_V, _I64, _V, ctypes.POINTER(_I32), ctypes.POINTER(_I32), ctypes.POINTER(_I32)]),
+    "wg_server_result": (_I32, [_V, _I64, _V, _V]),
+    "wg_server_request_state": (_I32, [_V, _I64, ctypes.POINTER(_I32), ctypes.POINTER(_I32)]),
+    "wg_server_get_stats": (_I32, [_V, _V]),
+    "wg_server_request_bytes": (_I32, [_V, _V, ctypes.POINTER(ctypes.c_uint64)]),
 }
 
 
@@ -391,3 +400,80 @@ class Batch:
         n = _I64()
         check(lib().wg_batch_launch_count(self.h, ctypes.byref(n)))
         return n.value
+
+
+class Server:
+    """Serving loop (wg_server_*): requests admitted under an HBM budget into a running
+    batch, one frame per tick for every resident scene, RGB8 frames to host memory."""
+
+    def __init__(self, lut, precision=P.FP32, steps_per_frame=10, max_scenes=512, hbm_budget=150 << 30,
+                 size=2, vshift=-0.2, vscale=1.0, slope=1.0, color_range=0.8, scale=1.0, stream=None):
+        cfg = P.WgServerConfig()
+        cfg.precision, cfg.steps_per_frame, cfg.max_scenes, cfg.hbm_budget = precision, steps_per_frame, max_scenes, hbm_budget
+        cfg.frame = P.WgFrameParams(size, 0, vshift, vscale, slope, color_range, scale, 1.0, 0, 0)
+        lut = np.ascontiguousarray(lut, np.uint8).reshape(-1)
+        ctypes.memmove(cfg.lut, lut.ctypes.data, 768)
+        h = ctypes.c_void_p()
+        check(lib().wg_server_create(ctypes.byref(cfg), None if stream is None else ctypes.c_void_p(stream),
+                                     ctypes.byref(h)))
+        self.h, self.params = h, {}
+
+    def close(self):
+        if self.h:
+            lib().wg_server_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    def submit(self, params, phi, psi, xy, frames, keep=False):
+        a = np.ascontiguousarray(phi, np.float64).reshape(-1)
+        b = np.ascontiguousarray(psi, np.float64).reshape(-1)
+        m = np.ascontiguousarray(xy, np.int16).reshape(-1)
+        rid = _I64()
+        check(lib().wg_server_submit(self.h, ctypes.byref(params), a.ctypes.data, b.ctypes.data, m.ctypes.data,
+                                     int(frames), int(keep), ctypes.byref(rid)))
+        self.params[rid.value] = params.copy()
+        return rid.value
+
+    def tick(self):
+        n = _I32()
+        check(lib().wg_server_tick(self.h, ctypes.byref(n)))
+        return n.value
+
+    def state(self, rid):
+        st, fd = _I32(), _I32()
+        check(lib().wg_server_request_state(self.h, int(rid), ctypes.byref(st), ctypes.byref(fd)))
+        return st.value, fd.value
+
+    def frame(self, rid):
+        w, h, idx = _I32(), _I32(), _I32()
+        check(lib().wg_server_frame(self.h, int(rid), None, ctypes.byref(idx), ctypes.byref(w), ctypes.byref(h)))
+        out = np.empty((h.value, w.value, 3), np.uint8)
+        check(lib().wg_server_frame(self.h, int(rid), out.ctypes.data, ctypes.byref(idx), None, None))
+        return idx.value, out
+
+    def result(self, rid):
+        p = self.params[rid]
+        phi, psi = np.empty(p.nx * p.ny), np.empty(p.nx * p.ny)
+        check(lib().wg_server_result(self.h, int(rid), phi.ctypes.data, psi.ctypes.data))
+        return phi, psi
+
+    def request_bytes(self, params):
+        n = ctypes.c_uint64()
+        check(lib().wg_server_request_bytes(self.h, ctypes.byref(params), ctypes.byref(n)))
+        return n.value
+
+    def stats(self):
+        st = P.WgServerStats()
+        check(lib().wg_server_get_stats(self.h, ctypes.byref(st)))
+        return {name: getattr(st, name) for name, _ in st._fields_}
