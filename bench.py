@@ -425,6 +425,38 @@ def run_serving(args, P, scenes, W, stream, rank):
     return out
 
 
+def run_probe(args):
+    """Small, fixed cases for kernel captures (ncu): the config-2 scene with a given
+    precision and temporal blocking, stepped `--probe-updates` times, or a 64-instance
+    batch stepped 4 frames of 10 updates."""
+    import numpy as np
+    _package()
+    from youtube_simulations_gb300 import params as P
+    from youtube_simulations_gb300 import scenes
+    from youtube_simulations_gb300 import wavegpu as W
+    if args.probe == "batch":
+        rng = np.random.default_rng(1000)
+        b = W.Batch(P.FP32)
+        for _ in range(64):
+            m = scenes.batch_member(rng)
+            b.add(m.params, m.phi, m.psi, m.xy)
+        for _ in range(4):
+            b.step(10)
+        print(json.dumps({"probe": "batch", "instances": b.count()[0], "energy0": b.energy(0)}))
+        b.close()
+        return 0
+    sc = scenes.config2(seed=0, nx=NX, ny=NY)
+    prec = P.FP64 if args.probe == "fp64" else P.FP32
+    s = W.Scene(sc.params, prec, P.COEF_TABLE)
+    s.upload(sc.phi, sc.psi, sc.xy, sc.tcc, sc.tc, sc.tgamma)
+    k, L, Wd = args.probe_block
+    s.set_blocking(k, L if k > 1 else 0, Wd if k > 1 else 0)
+    s.step(args.probe_updates)
+    print(json.dumps({"probe": args.probe, "blocking": s.blocking(), "time": s.time, "energy": s.total_energy()}))
+    s.close()
+    return 0
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -436,6 +468,9 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--ref-updates", type=int, default=20, help="updates per reference step")
     ap.add_argument("--e2e-steps", type=int, default=20)
+    ap.add_argument("--probe", choices=["fp32", "fp64", "batch"], help="run a small fixed case for kernel captures")
+    ap.add_argument("--probe-block", type=int, nargs=3, default=[3, 16, 256], metavar=("K", "L", "W"))
+    ap.add_argument("--probe-updates", type=int, default=24)
     ap.add_argument("--no-batch", action="store_true")
     ap.add_argument("--no-serving", action="store_true")
     ap.add_argument("--batch-instances", type=int, default=256)
@@ -447,6 +482,8 @@ def main():
     args = ap.parse_args()
     if args.warmup < 3:
         print("warning: fewer than 3 warm-up steps", file=sys.stderr)
+    if args.probe:
+        return run_probe(args)
     if args.impl == "reference":
         return run_reference(args)
     return run_ours(args)
