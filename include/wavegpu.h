@@ -164,6 +164,25 @@ wg_status wg_compute_energy_x_all(double **phi, double **psi, int16_t **xy_in, d
 wg_status wg_compute_energy_tblr(double **phi, double **psi, int16_t **xy_in,
                                  int32_t ileft, int32_t iright, double energies[6]);
 
+/* Energy diagnostics over device fields the caller owns, without any allocation.
+ * No counterpart in the reference: it is for callers that cannot allocate device
+ * memory at the time they need the diagnostics, e.g. a host program that carves all
+ * of its device memory out of its own arena at start-up, or a service that must not
+ * call cudaMalloc (which can block on device-wide synchronisation) while it serves.
+ * phi, psi: FP64 fields [nx][pitch] in device memory; xy: int16 mask [nx][pitch] in
+ * device memory (pitch >= ny, in elements); out: nx + 7 doubles in device memory that
+ * receive out[0] = total, out[1..6] = the six compute_energy_tblr boxes for
+ * ileft/iright, out[7 + i] = compute_energy_x(i).  The work is enqueued on `stream`
+ * (cudaStream_t; NULL = the default stream) and the call returns without waiting.
+ * Per-column partial sums go to a fixed scratch array in the library's device memory
+ * (WG_NOALLOC_MAX_NX columns at most; larger nx is refused with WG_ERR_INVALID).
+ * The first call on a device looks up that array's address; make it before any
+ * stream capture.  All calls share the array: calls that overlap on the GPU race. */
+#define WG_NOALLOC_MAX_NX 16384
+wg_status wg_compute_energy_device_noalloc(const wg_params *p, const double *phi, const double *psi,
+                                           const int16_t *xy, int32_t pitch, int32_t ileft, int32_t iright,
+                                           double *out, void *stream);
+
 /* ------------------------------------------------------------------------- */
 /* 2. Native handle API: resident scenes                                       */
 /* ------------------------------------------------------------------------- */

@@ -59,6 +59,7 @@ SIGNATURES = {
     "wg_compute_energy": (_I32, [_PP, _PP, _PP, _I32, _I32, ctypes.POINTER(_D)]),
     "wg_compute_energy_x_all": (_I32, [_PP, _PP, _PP, _V]),
     "wg_compute_energy_tblr": (_I32, [_PP, _PP, _PP, _I32, _I32, _V]),
+    "wg_compute_energy_device_noalloc": (_I32, [_V, _V, _V, _V, _I32, _I32, _I32, _V, _V]),
     "wg_scene_create": (_I32, [_V, _I32, _I32, _V, ctypes.POINTER(_V)]),
     "wg_scene_destroy": (_I32, [_V]),
     "wg_scene_bytes": (_I32, [_V, _I32, _I32, ctypes.POINTER(ctypes.c_size_t)]),
