@@ -24,6 +24,8 @@ void set_error(const char *fmt, ...)
     g_err = buf;
 }
 
+void clear_error() { g_err.clear(); }
+
 wg_status cuda_fail(cudaError_t e, const char *what)
 {
     set_error("CUDA error %s (%s) in %s", cudaGetErrorName(e), cudaGetErrorString(e), what);

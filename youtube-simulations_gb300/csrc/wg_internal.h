@@ -22,6 +22,7 @@ struct FastArgs {
 
 // error state (thread-local message)
 void set_error(const char *fmt, ...);
+void clear_error();
 wg_status cuda_fail(cudaError_t e, const char *what);
 #define WG_CUDA(call)                                       \
     do {                                                    \

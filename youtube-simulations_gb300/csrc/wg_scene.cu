@@ -225,7 +225,7 @@ wg_status wg_scene_destroy(wg_scene *s)
     for (auto &f : s->f) if (f) cudaFree(f);
     for (auto &g : s->g) if (g) cudaFree(g);
     void *dev[] = {s->act, s->nz, s->tcc, s->tc, s->tg, s->nidx, s->nw, s->ebot, s->etop, s->eout, s->dcount,
-                   s->dstage, s->rgb, s->lut, s->bv_osc, s->bv_src, s->dflag};
+                   s->dstage, s->rgb, s->lut, s->bv_osc, s->bv_src, s->dflag, s->tb_ctr};
     for (void *d : dev) if (d) cudaFree(d);
     if (s->hout) cudaFreeHost(s->hout);
     if (s->hstage) cudaFreeHost(s->hstage);
@@ -428,8 +428,12 @@ wg_status wg_scene_sync(wg_scene *s)
 wg_status wg_scene_set_blocking(wg_scene *s, int32_t k, int32_t tile_i, int32_t tile_j)
 {
     if (!s || k < 0 || k > WG_TB_MAX_K) { set_error("temporal block depth must be 0..%d", WG_TB_MAX_K); return WG_ERR_INVALID; }
-    if (tile_j != 0 && tile_j != 128 && tile_j != 256) { set_error("tile width must be 128 or 256"); return WG_ERR_INVALID; }
-    if (tile_i != 0 && (tile_i < 16 || tile_i > 64 || tile_i - 2 * k < 8)) {
+    if (tile_j != 0 && tile_j != 1 && tile_j != 128 && tile_j != 256) {
+        set_error("tile width must be 1 (skewed strips), 128 or 256");
+        return WG_ERR_INVALID;
+    }
+    if (tile_j == 1 && (tile_i < 8 || tile_i > 4096 || k > 4)) { set_error("skewed strips: 8..4096 rows, depth <= 4"); return WG_ERR_INVALID; }
+    if (tile_j > 1 && tile_i != 0 && (tile_i < 16 || tile_i > 64 || tile_i - 2 * k < 8)) {
         set_error("tile height must be 16..64 with at least 8 core rows");
         return WG_ERR_INVALID;
     }

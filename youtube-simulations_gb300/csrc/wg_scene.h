@@ -35,6 +35,7 @@ struct wg_scene {
     uint8_t *rgb = nullptr, *lut = nullptr;
     size_t rgb_bytes = 0;
     int tb_k = 0, tile_i = 0, tile_j = 0;
+    int *tb_ctr = nullptr;  // tile counter of the persistent skewed kernel
     float *bv_osc = nullptr, *bv_src = nullptr;  // boundary values of the current step() call
     size_t bv_cap = 0;
     long long bv_t0 = 0;

@@ -306,6 +306,387 @@ __global__ void __launch_bounds__(256) k_step_tb(const __grid_constant__ DevPara
     }
 }
 
+// One FP32 cell of level s at (gi, gj) from level s-1 (x, its neighbours n = i+1,
+// sv = i-1, e = j+1, w = j-1) and level s-2 (y).  cc is the cell's tcc, tcv its tc (table
+// mode).  GEN = false: a cell off the boundary lines and the source; PLAIN additionally
+// promises twospeeds and no FLOOR clamp, so every such cell takes the leapfrog update.
+template <int COEF, bool GEN, bool PLAIN>
+__device__ __forceinline__ float skew_cell(const DevParams &p, const TbArgs &a, int gi, int gj, int s, float x, float y,
+                                           float n, float sv, float e, float w, float cc, float tcv, bool act)
+{
+    const float ccv = (COEF == WG_COEF_TABLE) ? cc : (act ? a.c2 : a.c2b);
+    const float g = (COEF == WG_COEF_TABLE) ? a.gam : (act ? a.gam : a.gamb);
+    if (!GEN && PLAIN) return upd32(x, y, ccv, ((n - x) + (sv - x)) + ((e - x) + (w - x)), a.kappa, g);
+    if (!GEN) {
+        float v = y;
+        if (p.twospeeds || act) {
+            v = upd32(x, y, ccv, ((n - x) + (sv - x)) + ((e - x) + (w - x)), a.kappa, g);
+            if (p.floor_clamp && act) v = fminf(fmaxf(v, -a.vmax), a.vmax);
+        }
+        return v;
+    }
+    const int NX = p.nx, NY = p.ny;
+    const bool bi0 = gi == 0, bi1 = gi == NX - 1, bj0 = gj == 0, bj1 = gj == NY - 1;
+    int mode = 0;  // 0 leapfrog with mirrored neighbours, 1 absorbing, 2 oscillating value
+    float nb = 0.f, kk = 0.f, gg = 0.f;
+    if (bj0 || bj1) {
+        if (p.osc_topbot && gi > 0 && gi < NX - 1 && ((double)gi < p.tb_shift)) {
+            e = x;
+            w = x;
+        } else if (p.b_cond == WG_BC_DIRICHLET) {
+            if (bi1) n = x;
+            if (bi0) sv = x;
+            if (bj1) e = x; else w = x;
+        } else {
+            mode = 1;
+            nb = bj1 ? w : e;
+            kk = a.kt;
+            gg = a.gt;
+        }
+    } else if (bi0 || bi1) {
+        if (bi0 && left_bc(p, gj)) {
+            mode = 2;
+        } else if (p.b_cond == WG_BC_DIRICHLET) {
+            if (bi0) sv = x; else n = x;
+        } else {
+            mode = 1;
+            nb = bi0 ? n : sv;
+            kk = a.ks;
+            gg = a.gs;
+        }
+    }
+    if (p.osc_left && !p.beam && bi0 && (bj0 || (p.corner2_on && gj == NX - 1))) mode = 2;
+    float v = y;
+    if (mode == 2 || p.twospeeds || act) {
+        if (mode == 0) {
+            v = upd32(x, y, ccv, ((n - x) + (sv - x)) + ((e - x) + (w - x)), a.kappa, g);
+        } else if (mode == 1) {
+            v = absorb32(x, y, (COEF == WG_COEF_TABLE) ? tcv : (act ? a.courant : a.courantb), nb, kk, gg);
+        } else {
+            v = a.osc[(size_t)(s - 1) * NY + gj];
+        }
+        if (p.floor_clamp && act) v = fminf(fmaxf(v, -a.vmax), a.vmax);
+    }
+    if (p.src_on && gi == p.src_i && gj == p.src_j) v += a.src[s - 1];
+    return v;
+}
+
+
+// ---------------------------------------------------------------------------
+// Time-skewed streaming (k_step_skew): every warp owns a tile of 128 columns (four
+// adjacent columns j per lane, loaded as float4; a column halo of H = K rounded up to 4
+// on each side) and a strip of S rows (i), and marches down the strip once.  At input
+// row m it computes level s at row m - s for s = 1..K (level 0 = phi(t), level -1 =
+// psi(t-1)), so each level keeps only a window of three rows in registers.  Column
+// neighbours inside a lane are registers; across lanes they are one warp shuffle each
+// way.  Input rows are prefetched QD rows ahead.  The loop is unrolled by 3, the period
+// of the row windows, so that rotating them is register renaming.  Core columns
+// [H, 128-H) store level K (new phi) and level K-1 (new psi) of the rows in the strip.
+//
+// Tiles that reach an edge row or column or hold the point source (EDGE) take three
+// extra steps after the common update: the lane holding column 0 or ny-1 redoes that
+// cell by the column rule; rows 0 and nx-1 (warp-uniform) are redone by the general
+// rule; the source cell gets its increment.  Cells outside the domain keep whatever
+// they got: no cell inside reads them and none is stored.
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ float pick4(float a0, float a1, float a2, float a3, int c)
+{
+    return c == 0 ? a0 : (c == 1 ? a1 : (c == 2 ? a2 : a3));
+}
+
+// Column 0 (right = false) or ny-1 (right = true) at a row 1..nx-2: the boundary rule of
+// evolve_wave_half for the top/bottom lines (wave_billiard.c:366-452, B_COND Dirichlet or
+// absorbing, OSCILLATE_TOPBOT), same branches as skew_cell's general form.
+template <int COEF>
+__device__ __forceinline__ float col_edge_cell(const DevParams &p, const TbArgs &a, int gi, float x, float y, float n,
+                                               float sv, float e, float w, float cc, float tcv, bool act, bool right)
+{
+    const float ccv = (COEF == WG_COEF_TABLE) ? cc : (act ? a.c2 : a.c2b);
+    const float g = (COEF == WG_COEF_TABLE) ? a.gam : (act ? a.gam : a.gamb);
+    int mode = 0;
+    if (p.osc_topbot && ((double)gi < p.tb_shift)) {
+        e = x;
+        w = x;
+    } else if (p.b_cond == WG_BC_DIRICHLET) {
+        if (right) e = x; else w = x;
+    } else {
+        mode = 1;
+    }
+    float v = y;
+    if (p.twospeeds || act) {
+        if (mode == 0)
+            v = upd32(x, y, ccv, ((n - x) + (sv - x)) + ((e - x) + (w - x)), a.kappa, g);
+        else
+            v = absorb32(x, y, (COEF == WG_COEF_TABLE) ? tcv : (act ? a.courant : a.courantb), right ? w : e, a.kt, a.gt);
+        if (p.floor_clamp && act) v = fminf(fmaxf(v, -a.vmax), a.vmax);
+    }
+    return v;
+}
+
+template <int COEF, int K, bool EDGE, bool PLAIN>
+__device__ __forceinline__ void skew_strip(const DevParams &p, const TbArgs &a, int i_s, int i_e, int gj0, int lane)
+{
+    constexpr int QD = 3;  // prefetch depth (rows); equal to the unroll factor
+    constexpr int H = (K + 3) & ~3;
+    constexpr bool NEED_ACT = !(PLAIN && COEF == WG_COEF_TABLE);  // the plain table update ignores the mask
+    constexpr bool NEED_TCE = EDGE && COEF == WG_COEF_TABLE;       // tc of this lane's boundary column
+    const int m0 = i_s - K - 1, m1 = i_e + K;                      // input rows [m0, m1)
+    const bool lane_core = 4 * lane >= H && 4 * lane < 128 - H;
+    const bool grp_ok = gj0 >= 0 && gj0 < p.ny;  // the group holds at least one domain column
+    // EDGE: the lane's boundary column (0..3), or -1; the domain has ny >= 8 columns
+    const int cr = p.ny - 1 - gj0;  // column ny-1 within the lane's group when 0..3
+    const int ce = !EDGE ? -1 : (gj0 == 0 ? 0 : (cr >= 0 && cr <= 3 ? cr : -1));
+    const bool src_lane = EDGE && p.src_on && p.src_j >= gj0 && p.src_j < gj0 + 4;
+
+    float W[K + 1][3][4];  // W[s][k][c] = level s at row m-s-2+k, column gj0+c
+    float Yp[4];           // psi(t-1) at row m-1
+    float T[K + 1][4];     // tcc at rows m, m-1, ..., m-K
+    float TE[K + 1];       // tc of the lane's boundary column at the same rows (EDGE, table)
+    uint32_t aq = 0;       // bits 4d..4d+3 = active bits of row m-d
+#pragma unroll
+    for (int q = 0; q <= K; q++) {
+#pragma unroll
+        for (int c = 0; c < 4; c++) { W[q][0][c] = W[q][1][c] = W[q][2][c] = 0.f; T[q][c] = 0.f; }
+        TE[q] = 0.f;
+    }
+#pragma unroll
+    for (int c = 0; c < 4; c++) Yp[c] = 0.f;
+
+    float4 qx[QD], qy[QD], qc[QD];
+    float qe[QD];
+    uint32_t qa[QD];
+    auto fetch = [&](int m, float4 &x, float4 &y, float4 &c, float &te, uint32_t &ab) {
+        x = y = c = make_float4(0.f, 0.f, 0.f, 0.f);
+        te = 0.f;
+        ab = 0u;
+        if ((!EDGE || grp_ok) && m >= 0 && m < p.nx) {
+            const size_t o = (size_t)m * p.pitch + gj0;
+            x = *reinterpret_cast<const float4 *>(a.phi + o);
+            y = *reinterpret_cast<const float4 *>(a.psi + o);
+            if (COEF == WG_COEF_TABLE) c = *reinterpret_cast<const float4 *>(a.tcc + o);
+            if (NEED_TCE && ce >= 0 && a.tc) te = a.tc[o + (unsigned)ce];  // the table exists with an absorbing boundary
+            if (NEED_ACT) ab = a.act[(size_t)m * p.wpitch + (gj0 >> 5)];  // raw word: bits are taken when the row is used
+        }
+    };
+#pragma unroll
+    for (int q = 0; q < QD; q++) fetch(m0 + q, qx[q], qy[q], qc[q], qe[q], qa[q]);
+
+    for (int mb = m0; mb < m1; mb += QD) {
+#pragma unroll
+        for (int u = 0; u < QD; u++) {
+            const int m = mb + u;
+            if (m >= m1) break;  // warp-uniform
+            const float xin[4] = {qx[u].x, qx[u].y, qx[u].z, qx[u].w};
+            const float yin[4] = {qy[u].x, qy[u].y, qy[u].z, qy[u].w};
+            const float cin[4] = {qc[u].x, qc[u].y, qc[u].z, qc[u].w};
+            const float tein = qe[u];
+            if (NEED_ACT) aq = (aq << 4) | ((qa[u] >> (gj0 & 31)) & 0xFu);
+            fetch(m + QD, qx[u], qy[u], qc[u], qe[u], qa[u]);
+            float ylev1[4];
+#pragma unroll
+            for (int c = 0; c < 4; c++) {
+                W[0][0][c] = W[0][1][c];
+                W[0][1][c] = W[0][2][c];
+                W[0][2][c] = xin[c];
+                ylev1[c] = Yp[c];
+                Yp[c] = yin[c];
+#pragma unroll
+                for (int q = K; q > 0; q--) T[q][c] = T[q - 1][c];
+                T[0][c] = cin[c];
+            }
+#pragma unroll
+            for (int q = K; q > 0; q--) TE[q] = TE[q - 1];
+            TE[0] = tein;
+#pragma unroll
+            for (int lv = 1; lv <= K; lv++) {
+                const int r = m - lv;  // row of this level's new value
+                const float *Wc = W[lv - 1][1];
+                const float *Yl = (lv == 1) ? ylev1 : W[lv - 2 >= 0 ? lv - 2 : 0][0];
+                const float e3 = __shfl_down_sync(0xffffffffu, Wc[0], 1);
+                const float w0 = __shfl_up_sync(0xffffffffu, Wc[3], 1);
+                float v[4];
+#pragma unroll
+                for (int c = 0; c < 4; c++) {
+                    const float e = (c < 3) ? Wc[c + 1 < 4 ? c + 1 : 3] : e3;
+                    const float w = (c > 0) ? Wc[c > 0 ? c - 1 : 0] : w0;
+                    const bool act = NEED_ACT ? ((aq >> (4 * lv + c)) & 1u) : true;
+                    v[c] = skew_cell<COEF, false, PLAIN>(p, a, r, gj0 + c, lv, Wc[c], Yl[c], W[lv - 1][2][c],
+                                                         W[lv - 1][0][c], e, w, T[lv][c], 0.f, act);
+                }
+                if (EDGE) {
+                    const bool row_edge = r == 0 || r == p.nx - 1;  // warp-uniform
+                    if (ce >= 0 && r > 0 && r < p.nx - 1) {         // the lane holding column 0 or ny-1
+                        const float x = pick4(Wc[0], Wc[1], Wc[2], Wc[3], ce);
+                        const float res = col_edge_cell<COEF>(
+                            p, a, r, x, pick4(Yl[0], Yl[1], Yl[2], Yl[3], ce),
+                            pick4(W[lv - 1][2][0], W[lv - 1][2][1], W[lv - 1][2][2], W[lv - 1][2][3], ce),
+                            pick4(W[lv - 1][0][0], W[lv - 1][0][1], W[lv - 1][0][2], W[lv - 1][0][3], ce),
+                            pick4(Wc[1], Wc[2], Wc[3], e3, ce), pick4(w0, Wc[0], Wc[1], Wc[2], ce),
+                            pick4(T[lv][0], T[lv][1], T[lv][2], T[lv][3], ce), TE[lv],
+                            NEED_ACT ? ((aq >> (4 * lv + ce)) & 1u) : true, gj0 != 0);
+                        v[0] = (ce == 0) ? res : v[0];
+                        v[1] = (ce == 1) ? res : v[1];
+                        v[2] = (ce == 2) ? res : v[2];
+                        v[3] = (ce == 3) ? res : v[3];
+                    }
+                    if (row_edge) {  // rows 0 and nx-1 by the general rule, one cell at a time
+#pragma unroll 1
+                        for (int c = 0; c < 4; c++) {
+                            const int gj = gj0 + c;
+                            if (gj < 0 || gj >= p.ny) continue;
+                            const float tcv = (COEF == WG_COEF_TABLE && a.tc) ? a.tc[(size_t)r * p.pitch + gj] : 0.f;
+                            const float res = skew_cell<COEF, true, false>(
+                                p, a, r, gj, lv, pick4(Wc[0], Wc[1], Wc[2], Wc[3], c), pick4(Yl[0], Yl[1], Yl[2], Yl[3], c),
+                                pick4(W[lv - 1][2][0], W[lv - 1][2][1], W[lv - 1][2][2], W[lv - 1][2][3], c),
+                                pick4(W[lv - 1][0][0], W[lv - 1][0][1], W[lv - 1][0][2], W[lv - 1][0][3], c),
+                                pick4(Wc[1], Wc[2], Wc[3], e3, c), pick4(w0, Wc[0], Wc[1], Wc[2], c),
+                                pick4(T[lv][0], T[lv][1], T[lv][2], T[lv][3], c), tcv,
+                                NEED_ACT ? ((aq >> (4 * lv + c)) & 1u) : true);
+                            v[0] = (c == 0) ? res : v[0];
+                            v[1] = (c == 1) ? res : v[1];
+                            v[2] = (c == 2) ? res : v[2];
+                            v[3] = (c == 3) ? res : v[3];
+                        }
+                    } else if (src_lane && r == p.src_i) {  // the general rule adds it on rows 0 and nx-1
+                        const float add = a.src[lv - 1];
+                        const int cs = p.src_j - gj0;
+#pragma unroll
+                        for (int c = 0; c < 4; c++) v[c] += (cs == c) ? add : 0.f;
+                    }
+                }
+#pragma unroll
+                for (int c = 0; c < 4; c++) {
+                    W[lv][0][c] = W[lv][1][c];
+                    W[lv][1][c] = W[lv][2][c];
+                    W[lv][2][c] = v[c];
+                }
+            }
+            const int r = m - K;
+            if (lane_core && r >= i_s && r < i_e) {
+                const size_t o = (size_t)r * p.pitch + gj0;
+                if (!EDGE || gj0 + 3 < p.ny) {
+                    if (!EDGE || grp_ok) {
+                        *reinterpret_cast<float4 *>(a.phi_out + o) = make_float4(W[K][2][0], W[K][2][1], W[K][2][2], W[K][2][3]);
+                        *reinterpret_cast<float4 *>(a.psi_out + o) =
+                            make_float4(W[K - 1][1][0], W[K - 1][1][1], W[K - 1][1][2], W[K - 1][1][3]);
+                    }
+                } else if (grp_ok) {
+#pragma unroll
+                    for (int c = 0; c < 4; c++)
+                        if (gj0 + c < p.ny) {
+                            a.phi_out[o + c] = W[K][2][c];
+                            a.psi_out[o + c] = W[K - 1][1][c];
+                        }
+                }
+            }
+        }
+    }
+}
+
+// Tile (strip ts, column tile tj) stays off the edge rows and columns and away from
+// the point source: rows [i_s-K+1, i_e+K-1) and columns [t0+1, t0+127) carry the values
+// that reach its stored cells.
+template <int K>
+__device__ __forceinline__ bool skew_lean(const DevParams &p, int S, int ts, int tj)
+{
+    constexpr int H = (K + 3) & ~3, STEP = 128 - 2 * H;
+    const int t0 = tj * STEP - H, i_s = ts * S, i_e = min(i_s + S, p.nx);
+    return i_s - K >= 0 && i_e + K <= p.nx - 1 && t0 >= 1 && t0 + 128 <= p.ny - 1 &&
+           !(p.src_on && p.src_i >= i_s - K && p.src_i < i_e + K && p.src_j >= t0 && p.src_j < t0 + 128);
+}
+
+struct SkewGrid {
+    int S, tiles_j, ntiles;  // strip rows, column tiles, all tiles
+    int *ctr;                // [0] next tile, [1] warps finished (self-resetting)
+    int nwarps;              // warps of the launch
+};
+
+// Persistent: every warp takes tiles from a counter until none are left; the last warp
+// to finish resets the counter for the next launch.
+template <int COEF, int K, bool PLAIN>
+__global__ void __launch_bounds__(128, COEF == WG_COEF_TABLE ? 3 : 4) k_step_skew(const __grid_constant__ DevParams p, const __grid_constant__ TbArgs a,
+                                                      const SkewGrid g)
+{
+    constexpr int H = (K + 3) & ~3, STEP = 128 - 2 * H;
+    const int lane = threadIdx.x & 31;
+    for (;;) {
+        int t = 0;
+        if (lane == 0) t = atomicAdd(&g.ctr[0], 1);
+        t = __shfl_sync(0xffffffffu, t, 0);
+        if (t >= g.ntiles) break;
+        const int ts = t / g.tiles_j, tj = t % g.tiles_j;
+        const int i_s = ts * g.S, i_e = min(i_s + g.S, p.nx), gj0 = tj * STEP - H + 4 * lane;
+        if (skew_lean<K>(p, g.S, ts, tj)) skew_strip<COEF, K, false, PLAIN>(p, a, i_s, i_e, gj0, lane);
+        else skew_strip<COEF, K, true, PLAIN>(p, a, i_s, i_e, gj0, lane);
+    }
+    if (lane == 0) {
+        __threadfence();
+        if (atomicAdd(&g.ctr[1], 1) == g.nwarps - 1) {
+            g.ctr[0] = 0;
+            g.ctr[1] = 0;
+            __threadfence();
+        }
+    }
+}
+
+static bool skew_shape_ok(const DevParams &p, int K, int S)
+{
+    return K >= 2 && K <= 4 && S >= 8 && S <= 4096 && p.ny >= 8 && p.nx >= 2;
+}
+
+static int sm_count()
+{
+    static int n = 0;
+    if (!n) {
+        int dev = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev);
+        if (n <= 0) n = 1;
+    }
+    return n;
+}
+
+template <int COEF, int K, bool PLAIN>
+static void launch_skew_k(const DevParams &p, const TbArgs &a, SkewGrid g, cudaStream_t st)
+{
+    static int per_sm = 0;
+    if (!per_sm) {
+        int nb = 0;
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_step_skew<COEF, K, PLAIN>, 128, 0);
+        per_sm = nb > 0 ? nb : 1;
+    }
+    g.nwarps = std::min(per_sm * sm_count() * 4, (g.ntiles + 3) & ~3);
+    k_step_skew<COEF, K, PLAIN><<<g.nwarps / 4, 128, 0, st>>>(p, a, g);
+}
+
+template <int COEF, bool PLAIN>
+static void launch_skew_c(const DevParams &p, const TbArgs &a, int K, const SkewGrid &g, cudaStream_t st)
+{
+    switch (K) {
+    case 2: launch_skew_k<COEF, 2, PLAIN>(p, a, g, st); break;
+    case 3: launch_skew_k<COEF, 3, PLAIN>(p, a, g, st); break;
+    default: launch_skew_k<COEF, 4, PLAIN>(p, a, g, st); break;
+    }
+}
+
+static void launch_skew(const DevParams &p, const TbArgs &a, int coef, int K, int S, int *ctr, cudaStream_t st)
+{
+    const int H = (K + 3) & ~3, step = 128 - 2 * H;
+    SkewGrid g{};
+    g.S = S;
+    g.tiles_j = (p.ny + H + step - 1) / step;
+    g.ntiles = g.tiles_j * ((p.nx + S - 1) / S);
+    g.ctr = ctr;
+    const bool plain = p.twospeeds && !p.floor_clamp;
+    if (coef == WG_COEF_TABLE) {
+        if (plain) launch_skew_c<WG_COEF_TABLE, true>(p, a, K, g, st);
+        else launch_skew_c<WG_COEF_TABLE, false>(p, a, K, g, st);
+    } else {
+        if (plain) launch_skew_c<WG_COEF_MASK, true>(p, a, K, g, st);
+        else launch_skew_c<WG_COEF_MASK, false>(p, a, K, g, st);
+    }
+}
+
 static int tb_halo(int K) { return (K + 3) & ~3; }
 
 static bool tb_shape_ok(int K, int L, int W)
@@ -404,6 +785,10 @@ static wg_status ensure_tb_buffers(wg_scene *s)
             WG_CUDA(cudaMalloc(&s->g[k], fb));
             WG_CUDA(cudaMemsetAsync(s->g[k], 0, fb, s->st));
         }
+    if (!s->tb_ctr) {
+        WG_CUDA(cudaMalloc(&s->tb_ctr, 2 * sizeof(int)));
+        WG_CUDA(cudaMemsetAsync(s->tb_ctr, 0, 2 * sizeof(int), s->st));
+    }
     return WG_OK;
 }
 
@@ -466,7 +851,13 @@ wg_status tb_pass<float>(wg_scene *s, int k)
     if (!tb_depth_ok(k)) { set_error("temporal block depth %d outside 2..8", k); return WG_ERR_INVALID; }
     const int W = s->tile_j > 0 ? s->tile_j : 256, L = s->tile_i > 0 ? s->tile_i : 32;
     TbArgs a = tb_args(s);
-    if (!launch_tb(s, a, k, L, W)) {
+    if (W == 1) {  // time-skewed streaming strips of L rows
+        if (!skew_shape_ok(s->dp, k, L)) {
+            set_error("unsupported skewed strip (depth %d of 2..4, %d rows of 8..4096, ny >= 8)", k, L);
+            return WG_ERR_INVALID;
+        }
+        launch_skew(s->dp, a, s->coef, k, L, s->tb_ctr, s->st);
+    } else if (clear_error(), !launch_tb(s, a, k, L, W)) {
         if (wg_last_error()[0] == 0) set_error("unsupported temporal block (depth %d, tile %d x %d)", k, L, W);
         return WG_ERR_INVALID;
     }
@@ -539,7 +930,8 @@ void autotune_scene(wg_scene *s)
         float best = 1e30f;
         struct Cand { int k, l, w; };
         const Cand cands[] = {{1, 0, 0},    {2, 16, 256}, {3, 16, 256}, {4, 16, 256}, {4, 24, 256},
-                              {6, 24, 256}, {4, 32, 256}, {6, 32, 256}, {4, 32, 128}, {6, 32, 128}};
+                              {6, 32, 256}, {4, 32, 128}, {2, 16, 1},   {3, 16, 1},   {2, 24, 1},
+                              {3, 24, 1},   {4, 24, 1},   {3, 32, 1}};
         for (const Cand &c : cands) {
             s->tb_k = c.k;
             s->tile_i = c.l;
@@ -547,8 +939,14 @@ void autotune_scene(wg_scene *s)
             float ms_best = 1e30f;
             for (int rep = 0; rep < 3; rep++) {
                 cudaEventRecord(e0, s->st);
-                scene_step_impl<float>(s, updates);
+                const wg_status st = scene_step_impl<float>(s, updates);
                 cudaEventRecord(e1, s->st);
+                if (st != WG_OK) {  // a shape this scene does not take
+                    cudaEventSynchronize(e1);
+                    clear_error();
+                    ms_best = 1e30f;
+                    break;
+                }
                 cudaEventSynchronize(e1);
                 float ms = 0.f;
                 cudaEventElapsedTime(&ms, e0, e1);
