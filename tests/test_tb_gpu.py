@@ -16,8 +16,14 @@ from youtube_simulations_gb300 import wavegpu as W
 pytestmark = pytest.mark.gpu
 
 
-def case(name, nx=301, ny=517, seed=0):
+# Widths put column ny-1 at each of the four positions of a four-column group
+# (517: first, 518: second, 611: third, 520: last).
+WIDTH = {"dir_kappa_floor": 517, "abs_twospeeds_src": 517, "abs_stadium": 520, "topbot": 518}
+
+
+def case(name, nx=301, ny=None, seed=0):
     rng = np.random.default_rng(seed)
+    ny = ny or WIDTH.get(name, 517)
     over = dict(nx=nx, ny=ny)
     if name == "dir_kappa_floor":
         p = params_of("s_dir", **over)

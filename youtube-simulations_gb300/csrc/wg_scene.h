@@ -5,6 +5,11 @@
 
 #define WG_TB_MAX_K 16
 
+struct SkewPlanCache {
+    int4 *dev = nullptr;  // (column tile, first row, end row, edge) per warp
+    int n = 0, min_rows = 0;
+};
+
 struct wg_scene {
     wg_params prm;
     wg::DevParams dp;
@@ -35,7 +40,7 @@ struct wg_scene {
     uint8_t *rgb = nullptr, *lut = nullptr;
     size_t rgb_bytes = 0;
     int tb_k = 0, tile_i = 0, tile_j = 0;
-    int *tb_ctr = nullptr;  // tile counter of the persistent skewed kernel
+    SkewPlanCache skew[5];  // task lists of the skewed kernel, by depth
     float *bv_osc = nullptr, *bv_src = nullptr;  // boundary values of the current step() call
     size_t bv_cap = 0;
     long long bv_t0 = 0;

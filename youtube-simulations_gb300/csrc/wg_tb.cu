@@ -16,6 +16,7 @@
 // Periodic and VPER_HABS boundaries (which read the opposite side of the grid) and
 // Neumann gathers use the single-step kernel.
 #include <algorithm>
+#include <cmath>
 #include <map>
 #include <mutex>
 #include <tuple>
@@ -383,7 +384,7 @@ __device__ __forceinline__ float skew_cell(const DevParams &p, const TbArgs &a, 
 // of the row windows, so that rotating them is register renaming.  Core columns
 // [H, 128-H) store level K (new phi) and level K-1 (new psi) of the rows in the strip.
 //
-// Tiles that reach an edge row or column or hold the point source (EDGE) take three
+// Tiles that reach an edge row or column or hold the point source (edge tiles) take three
 // extra steps after the common update: the lane holding column 0 or ny-1 redoes that
 // cell by the column rule; rows 0 and nx-1 (warp-uniform) are redone by the general
 // rule; the source cell gets its increment.  Cells outside the domain keep whatever
@@ -423,25 +424,54 @@ __device__ __forceinline__ float col_edge_cell(const DevParams &p, const TbArgs 
     return v;
 }
 
-template <int COEF, int K, bool EDGE, bool PLAIN>
-__device__ __forceinline__ void skew_strip(const DevParams &p, const TbArgs &a, int i_s, int i_e, int gj0, int lane)
+// Asynchronous global->shared copies of one lane's 16 (or 4) bytes; with src_bytes 0
+// nothing is read and the destination is zero-filled.
+__device__ __forceinline__ void cp_async16(void *dst, const void *src, int src_bytes)
 {
-    constexpr int QD = 3;  // prefetch depth (rows); equal to the unroll factor
+    const unsigned d = (unsigned)__cvta_generic_to_shared(dst);
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16, %2;\n" ::"r"(d), "l"(src), "r"(src_bytes) : "memory");
+}
+__device__ __forceinline__ void cp_async4(void *dst, const void *src, int src_bytes)
+{
+    const unsigned d = (unsigned)__cvta_generic_to_shared(dst);
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 4, %2;\n" ::"r"(d), "l"(src), "r"(src_bytes) : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
+template <int N>
+__device__ __forceinline__ void cp_async_wait() { asm volatile("cp.async.wait_group %0;\n" ::"n"(N) : "memory"); }
+
+// Row slot of a warp's shared-memory ring (floats): phi[128], psi[128], tcc[128] (table
+// scenes), then one active word and one edge-column tc per lane.
+template <int COEF> struct SkewSlot {
+    static constexpr int PSI = 128, TCC = 256, ACT = (COEF == WG_COEF_TABLE) ? 384 : 256, TCE = ACT + 32, SIZE = TCE + 32;
+    static constexpr int DEPTH = (COEF == WG_COEF_TABLE) ? 6 : 8;  // ring slots
+};
+
+// GEN = false: inner tiles (fix = false) and tiles of column 0, of column ny-1 when ny is
+// a multiple of 4, or of the point source (fix = true), all away from rows 0 and nx-1.
+// GEN = true (fix = true): the others, with the general rule on rows 0 and nx-1.
+template <int COEF, int K, bool PLAIN, bool GEN>
+__device__ __forceinline__ void skew_strip(const DevParams &p, const TbArgs &a, int i_s, int i_e, int gj0, int lane,
+                                           float *ring, bool edge)
+{
+    using SL = SkewSlot<COEF>;
+    constexpr int D = SL::DEPTH;
+    constexpr int QD = D - 1;                    // rows in flight ahead of the one in use
     constexpr int H = (K + 3) & ~3;
     constexpr bool NEED_ACT = !(PLAIN && COEF == WG_COEF_TABLE);  // the plain table update ignores the mask
-    constexpr bool NEED_TCE = EDGE && COEF == WG_COEF_TABLE;       // tc of this lane's boundary column
+    const bool need_tce = edge && COEF == WG_COEF_TABLE;           // tc of this lane's boundary column
     const int m0 = i_s - K - 1, m1 = i_e + K;                      // input rows [m0, m1)
     const bool lane_core = 4 * lane >= H && 4 * lane < 128 - H;
     const bool grp_ok = gj0 >= 0 && gj0 < p.ny;  // the group holds at least one domain column
-    // EDGE: the lane's boundary column (0..3), or -1; the domain has ny >= 8 columns
+    // edge tiles: the lane's boundary column (0..3), or -1; the domain has ny >= 8 columns
     const int cr = p.ny - 1 - gj0;  // column ny-1 within the lane's group when 0..3
-    const int ce = !EDGE ? -1 : (gj0 == 0 ? 0 : (cr >= 0 && cr <= 3 ? cr : -1));
-    const bool src_lane = EDGE && p.src_on && p.src_j >= gj0 && p.src_j < gj0 + 4;
+    const int ce = !edge ? -1 : (gj0 == 0 ? 0 : (cr >= 0 && cr <= 3 ? cr : -1));
+    const bool src_lane = edge && p.src_on && p.src_j >= gj0 && p.src_j < gj0 + 4;
 
     float W[K + 1][3][4];  // W[s][k][c] = level s at row m-s-2+k, column gj0+c
     float Yp[4];           // psi(t-1) at row m-1
     float T[K + 1][4];     // tcc at rows m, m-1, ..., m-K
-    float TE[K + 1];       // tc of the lane's boundary column at the same rows (EDGE, table)
+    float TE[K + 1];       // tc of the lane's boundary column at the same rows (edge tiles, table)
     uint32_t aq = 0;       // bits 4d..4d+3 = active bits of row m-d
 #pragma unroll
     for (int q = 0; q <= K; q++) {
@@ -452,36 +482,46 @@ __device__ __forceinline__ void skew_strip(const DevParams &p, const TbArgs &a, 
 #pragma unroll
     for (int c = 0; c < 4; c++) Yp[c] = 0.f;
 
-    float4 qx[QD], qy[QD], qc[QD];
-    float qe[QD];
-    uint32_t qa[QD];
-    auto fetch = [&](int m, float4 &x, float4 &y, float4 &c, float &te, uint32_t &ab) {
-        x = y = c = make_float4(0.f, 0.f, 0.f, 0.f);
-        te = 0.f;
-        ab = 0u;
-        if ((!EDGE || grp_ok) && m >= 0 && m < p.nx) {
-            const size_t o = (size_t)m * p.pitch + gj0;
-            x = *reinterpret_cast<const float4 *>(a.phi + o);
-            y = *reinterpret_cast<const float4 *>(a.psi + o);
-            if (COEF == WG_COEF_TABLE) c = *reinterpret_cast<const float4 *>(a.tcc + o);
-            if (NEED_TCE && ce >= 0 && a.tc) te = a.tc[o + (unsigned)ce];  // the table exists with an absorbing boundary
-            if (NEED_ACT) ab = a.act[(size_t)m * p.wpitch + (gj0 >> 5)];  // raw word: bits are taken when the row is used
+    // row m goes to slot (m - m0) % D; each lane copies, and later reads, only its own bytes
+    auto issue = [&](int m, int slot) {
+        float *b = ring + slot * SL::SIZE;
+        const bool ok = grp_ok && m >= 0 && m < p.nx;
+        const size_t o = ok ? (size_t)m * p.pitch + gj0 : 0;
+        const int n16 = ok ? 16 : 0;
+        cp_async16(b + 4 * lane, a.phi + o, n16);
+        cp_async16(b + SL::PSI + 4 * lane, a.psi + o, n16);
+        if (COEF == WG_COEF_TABLE) cp_async16(b + SL::TCC + 4 * lane, a.tcc + o, n16);
+        if (NEED_ACT) cp_async4(b + SL::ACT + lane, a.act + (ok ? (size_t)m * p.wpitch + (gj0 >> 5) : 0), ok ? 4 : 0);
+        if (need_tce) {
+            const bool te = ok && ce >= 0 && a.tc;  // the table exists with an absorbing boundary
+            cp_async4(b + SL::TCE + lane, te ? a.tc + o + (unsigned)ce : a.phi, te ? 4 : 0);
         }
+        cp_async_commit();
     };
 #pragma unroll
-    for (int q = 0; q < QD; q++) fetch(m0 + q, qx[q], qy[q], qc[q], qe[q], qa[q]);
+    for (int q = 0; q < QD; q++) issue(m0 + q, q);
+    int slot = 0;  // slot of row m
 
-    for (int mb = m0; mb < m1; mb += QD) {
+    for (int mb = m0; mb < m1; mb += 3) {
 #pragma unroll
-        for (int u = 0; u < QD; u++) {
+        for (int u = 0; u < 3; u++) {
             const int m = mb + u;
             if (m >= m1) break;  // warp-uniform
-            const float xin[4] = {qx[u].x, qx[u].y, qx[u].z, qx[u].w};
-            const float yin[4] = {qy[u].x, qy[u].y, qy[u].z, qy[u].w};
-            const float cin[4] = {qc[u].x, qc[u].y, qc[u].z, qc[u].w};
-            const float tein = qe[u];
-            if (NEED_ACT) aq = (aq << 4) | ((qa[u] >> (gj0 & 31)) & 0xFu);
-            fetch(m + QD, qx[u], qy[u], qc[u], qe[u], qa[u]);
+            cp_async_wait<QD - 1>();  // row m has landed
+            const float *b = ring + slot * SL::SIZE;
+            const float4 xq = *reinterpret_cast<const float4 *>(b + 4 * lane);
+            const float4 yq = *reinterpret_cast<const float4 *>(b + SL::PSI + 4 * lane);
+            const float4 cq = (COEF == WG_COEF_TABLE) ? *reinterpret_cast<const float4 *>(b + SL::TCC + 4 * lane)
+                                                      : make_float4(0.f, 0.f, 0.f, 0.f);
+            const uint32_t aw = NEED_ACT ? reinterpret_cast<const uint32_t *>(b)[SL::ACT + lane] : 0u;
+            const float tein = need_tce ? b[SL::TCE + lane] : 0.f;
+            const float xin[4] = {xq.x, xq.y, xq.z, xq.w};
+            const float yin[4] = {yq.x, yq.y, yq.z, yq.w};
+            const float cin[4] = {cq.x, cq.y, cq.z, cq.w};
+            if (NEED_ACT) aq = (aq << 4) | ((aw >> (gj0 & 31)) & 0xFu);
+            // the slot of row m-1 (read in the previous row) takes row m+QD
+            issue(m + QD, slot == 0 ? D - 1 : slot - 1);
+            slot = (slot == D - 1) ? 0 : slot + 1;
             float ylev1[4];
 #pragma unroll
             for (int c = 0; c < 4; c++) {
@@ -513,12 +553,28 @@ __device__ __forceinline__ void skew_strip(const DevParams &p, const TbArgs &a, 
                     v[c] = skew_cell<COEF, false, PLAIN>(p, a, r, gj0 + c, lv, Wc[c], Yl[c], W[lv - 1][2][c],
                                                          W[lv - 1][0][c], e, w, T[lv][c], 0.f, act);
                 }
-                if (EDGE) {
-                    const bool row_edge = r == 0 || r == p.nx - 1;  // warp-uniform
-                    if (ce >= 0 && r > 0 && r < p.nx - 1) {         // the lane holding column 0 or ny-1
-                        const float x = pick4(Wc[0], Wc[1], Wc[2], Wc[3], ce);
+                if (!GEN && edge) {  // warp-uniform
+                    if (ce >= 0 && r > 0 && r < p.nx - 1) {  // the lane holding column 0 (c = 0) or ny-1 (c = 3)
+                        const bool lf = ce == 0;
                         const float res = col_edge_cell<COEF>(
-                            p, a, r, x, pick4(Yl[0], Yl[1], Yl[2], Yl[3], ce),
+                            p, a, r, lf ? Wc[0] : Wc[3], lf ? Yl[0] : Yl[3], lf ? W[lv - 1][2][0] : W[lv - 1][2][3],
+                            lf ? W[lv - 1][0][0] : W[lv - 1][0][3], lf ? Wc[1] : e3, lf ? w0 : Wc[2],
+                            lf ? T[lv][0] : T[lv][3], TE[lv], NEED_ACT ? ((aq >> (4 * lv + ce)) & 1u) : true, !lf);
+                        v[0] = lf ? res : v[0];
+                        v[3] = lf ? v[3] : res;
+                    }
+                    if (src_lane && r == p.src_i) {
+                        const float add = a.src[lv - 1];
+                        const int cs = p.src_j - gj0;
+#pragma unroll
+                        for (int c = 0; c < 4; c++) v[c] += (cs == c) ? add : 0.f;
+                    }
+                }
+                if (GEN) {
+                    const bool row_edge = r == 0 || r == p.nx - 1;  // warp-uniform
+                    if (ce >= 0 && r > 0 && r < p.nx - 1) {  // the lane holding column 0 or ny-1: picked by index
+                        const float res = col_edge_cell<COEF>(
+                            p, a, r, pick4(Wc[0], Wc[1], Wc[2], Wc[3], ce), pick4(Yl[0], Yl[1], Yl[2], Yl[3], ce),
                             pick4(W[lv - 1][2][0], W[lv - 1][2][1], W[lv - 1][2][2], W[lv - 1][2][3], ce),
                             pick4(W[lv - 1][0][0], W[lv - 1][0][1], W[lv - 1][0][2], W[lv - 1][0][3], ce),
                             pick4(Wc[1], Wc[2], Wc[3], e3, ce), pick4(w0, Wc[0], Wc[1], Wc[2], ce),
@@ -564,8 +620,8 @@ __device__ __forceinline__ void skew_strip(const DevParams &p, const TbArgs &a, 
             const int r = m - K;
             if (lane_core && r >= i_s && r < i_e) {
                 const size_t o = (size_t)r * p.pitch + gj0;
-                if (!EDGE || gj0 + 3 < p.ny) {
-                    if (!EDGE || grp_ok) {
+                if (gj0 + 3 < p.ny) {
+                    if (grp_ok) {
                         *reinterpret_cast<float4 *>(a.phi_out + o) = make_float4(W[K][2][0], W[K][2][1], W[K][2][2], W[K][2][3]);
                         *reinterpret_cast<float4 *>(a.psi_out + o) =
                             make_float4(W[K - 1][1][0], W[K - 1][1][1], W[K - 1][1][2], W[K - 1][1][3]);
@@ -581,52 +637,26 @@ __device__ __forceinline__ void skew_strip(const DevParams &p, const TbArgs &a, 
             }
         }
     }
+    cp_async_wait<0>();  // rows prefetched past the strip land before the ring is reused
 }
 
-// Tile (strip ts, column tile tj) stays off the edge rows and columns and away from
-// the point source: rows [i_s-K+1, i_e+K-1) and columns [t0+1, t0+127) carry the values
-// that reach its stored cells.
-template <int K>
-__device__ __forceinline__ bool skew_lean(const DevParams &p, int S, int ts, int tj)
-{
-    constexpr int H = (K + 3) & ~3, STEP = 128 - 2 * H;
-    const int t0 = tj * STEP - H, i_s = ts * S, i_e = min(i_s + S, p.nx);
-    return i_s - K >= 0 && i_e + K <= p.nx - 1 && t0 >= 1 && t0 + 128 <= p.ny - 1 &&
-           !(p.src_on && p.src_i >= i_s - K && p.src_i < i_e + K && p.src_j >= t0 && p.src_j < t0 + 128);
-}
-
-struct SkewGrid {
-    int S, tiles_j, ntiles;  // strip rows, column tiles, all tiles
-    int *ctr;                // [0] next tile, [1] warps finished (self-resetting)
-    int nwarps;              // warps of the launch
-};
-
-// Persistent: every warp takes tiles from a counter until none are left; the last warp
-// to finish resets the counter for the next launch.
+// One warp per task: column tile tj (x), rows [i_s, i_e) (y, z), and its kind (w): 0 inner,
+// 1 column 0 / column ny-1 / point source, 2 rows 0 and nx-1 or a column ny-1 that is not
+// a group's last.  The task list fills one wave of resident warps.
 template <int COEF, int K, bool PLAIN>
-__global__ void __launch_bounds__(128, COEF == WG_COEF_TABLE ? 3 : 4) k_step_skew(const __grid_constant__ DevParams p, const __grid_constant__ TbArgs a,
-                                                      const SkewGrid g)
+__global__ void __launch_bounds__(128, 4) k_step_skew(const __grid_constant__ DevParams p, const __grid_constant__ TbArgs a,
+                                                      const int4 *__restrict__ tasks, int ntasks)
 {
     constexpr int H = (K + 3) & ~3, STEP = 128 - 2 * H;
+    extern __shared__ float4 skew_smem[];
     const int lane = threadIdx.x & 31;
-    for (;;) {
-        int t = 0;
-        if (lane == 0) t = atomicAdd(&g.ctr[0], 1);
-        t = __shfl_sync(0xffffffffu, t, 0);
-        if (t >= g.ntiles) break;
-        const int ts = t / g.tiles_j, tj = t % g.tiles_j;
-        const int i_s = ts * g.S, i_e = min(i_s + g.S, p.nx), gj0 = tj * STEP - H + 4 * lane;
-        if (skew_lean<K>(p, g.S, ts, tj)) skew_strip<COEF, K, false, PLAIN>(p, a, i_s, i_e, gj0, lane);
-        else skew_strip<COEF, K, true, PLAIN>(p, a, i_s, i_e, gj0, lane);
-    }
-    if (lane == 0) {
-        __threadfence();
-        if (atomicAdd(&g.ctr[1], 1) == g.nwarps - 1) {
-            g.ctr[0] = 0;
-            g.ctr[1] = 0;
-            __threadfence();
-        }
-    }
+    const int warp = blockIdx.x * 4 + (threadIdx.x >> 5);
+    if (warp >= ntasks) return;  // warp-uniform
+    float *ring = reinterpret_cast<float *>(skew_smem) + (threadIdx.x >> 5) * SkewSlot<COEF>::DEPTH * SkewSlot<COEF>::SIZE;
+    const int4 t = tasks[warp];
+    const int gj0 = t.x * STEP - H + 4 * lane;
+    if (t.w == 2) skew_strip<COEF, K, PLAIN, true>(p, a, t.y, t.z, gj0, lane, ring, true);
+    else skew_strip<COEF, K, PLAIN, false>(p, a, t.y, t.z, gj0, lane, ring, t.w == 1);
 }
 
 static bool skew_shape_ok(const DevParams &p, int K, int S)
@@ -647,44 +677,129 @@ static int sm_count()
 }
 
 template <int COEF, int K, bool PLAIN>
-static void launch_skew_k(const DevParams &p, const TbArgs &a, SkewGrid g, cudaStream_t st)
+static int skew_capacity()
 {
+    constexpr size_t smem = 4 * SkewSlot<COEF>::DEPTH * SkewSlot<COEF>::SIZE * sizeof(float);  // 4 warps
     static int per_sm = 0;
     if (!per_sm) {
+        cudaFuncSetAttribute(k_step_skew<COEF, K, PLAIN>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
         int nb = 0;
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_step_skew<COEF, K, PLAIN>, 128, 0);
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_step_skew<COEF, K, PLAIN>, 128, smem);
         per_sm = nb > 0 ? nb : 1;
     }
-    g.nwarps = std::min(per_sm * sm_count() * 4, (g.ntiles + 3) & ~3);
-    k_step_skew<COEF, K, PLAIN><<<g.nwarps / 4, 128, 0, st>>>(p, a, g);
+    return per_sm * sm_count() * 4;
+}
+
+template <int COEF, int K, bool PLAIN>
+static void launch_skew_k(const DevParams &p, const TbArgs &a, const int4 *tasks, int ntasks, cudaStream_t st)
+{
+    constexpr size_t smem = 4 * SkewSlot<COEF>::DEPTH * SkewSlot<COEF>::SIZE * sizeof(float);
+    skew_capacity<COEF, K, PLAIN>();  // sets the shared-memory attribute once
+    k_step_skew<COEF, K, PLAIN><<<(ntasks + 3) / 4, 128, smem, st>>>(p, a, tasks, ntasks);
 }
 
 template <int COEF, bool PLAIN>
-static void launch_skew_c(const DevParams &p, const TbArgs &a, int K, const SkewGrid &g, cudaStream_t st)
+static int skew_dispatch(const DevParams &p, const TbArgs *a, int K, const int4 *tasks, int ntasks, cudaStream_t st)
 {
+    // a == nullptr: return the number of resident warps instead of launching
     switch (K) {
-    case 2: launch_skew_k<COEF, 2, PLAIN>(p, a, g, st); break;
-    case 3: launch_skew_k<COEF, 3, PLAIN>(p, a, g, st); break;
-    default: launch_skew_k<COEF, 4, PLAIN>(p, a, g, st); break;
+    case 2: if (!a) return skew_capacity<COEF, 2, PLAIN>(); launch_skew_k<COEF, 2, PLAIN>(p, *a, tasks, ntasks, st); break;
+    case 3: if (!a) return skew_capacity<COEF, 3, PLAIN>(); launch_skew_k<COEF, 3, PLAIN>(p, *a, tasks, ntasks, st); break;
+    default: if (!a) return skew_capacity<COEF, 4, PLAIN>(); launch_skew_k<COEF, 4, PLAIN>(p, *a, tasks, ntasks, st); break;
     }
+    return 0;
 }
 
-static void launch_skew(const DevParams &p, const TbArgs &a, int coef, int K, int S, int *ctr, cudaStream_t st)
+static int skew_call(const DevParams &p, const TbArgs *a, int coef, int K, const int4 *tasks, int ntasks, cudaStream_t st)
 {
-    const int H = (K + 3) & ~3, step = 128 - 2 * H;
-    SkewGrid g{};
-    g.S = S;
-    g.tiles_j = (p.ny + H + step - 1) / step;
-    g.ntiles = g.tiles_j * ((p.nx + S - 1) / S);
-    g.ctr = ctr;
     const bool plain = p.twospeeds && !p.floor_clamp;
-    if (coef == WG_COEF_TABLE) {
-        if (plain) launch_skew_c<WG_COEF_TABLE, true>(p, a, K, g, st);
-        else launch_skew_c<WG_COEF_TABLE, false>(p, a, K, g, st);
-    } else {
-        if (plain) launch_skew_c<WG_COEF_MASK, true>(p, a, K, g, st);
-        else launch_skew_c<WG_COEF_MASK, false>(p, a, K, g, st);
+    if (coef == WG_COEF_TABLE)
+        return plain ? skew_dispatch<WG_COEF_TABLE, true>(p, a, K, tasks, ntasks, st)
+                     : skew_dispatch<WG_COEF_TABLE, false>(p, a, K, tasks, ntasks, st);
+    return plain ? skew_dispatch<WG_COEF_MASK, true>(p, a, K, tasks, ntasks, st)
+                 : skew_dispatch<WG_COEF_MASK, false>(p, a, K, tasks, ntasks, st);
+}
+
+// Task list of a skewed pass.  Every column tile is cut into a top and a bottom segment
+// of R rows (kind 2) and row chunks in between; a chunk costs its rows plus 2K+1 rows of
+// pipeline fill, and a row of a boundary column tile about SKEW_EDGE_COST rows of an
+// inner one.  Chunks are sized so that all warps carry about the same cost and the list
+// fills the resident warps once (inner chunks of at least min_rows rows).  Tasks are
+// ordered by row band so that the boundary chunks spread over the SMs.
+#define SKEW_EDGE_COST 1.25
+static std::vector<int4> skew_plan(const DevParams &p, int K, int min_rows, int cap)
+{
+    const int H = (K + 3) & ~3, step = 128 - 2 * H, F = 2 * K + 1;
+    const int nx = p.nx, tiles_j = (p.ny + H + step - 1) / step;
+    const int R = std::max(K + 1, 8);
+    const bool segs = nx >= 2 * R + 1;  // else every task is of kind 2
+    const int mid0 = segs ? R : 0, mid1 = segs ? nx - R : nx, nmid = mid1 - mid0;
+    std::vector<int> col_kind(tiles_j);  // 0 inner, 1 column 0 or ny-1 (last of a group), 2 ny-1 elsewhere
+    int n_edge = 0;
+    for (int tj = 0; tj < tiles_j; tj++) {
+        const int t0 = tj * step - H;
+        const bool left = t0 < 1, right = t0 + 128 > p.ny - 1;
+        col_kind[tj] = (right && (p.ny & 3) != 0) ? 2 : ((left || right) ? 1 : 0);
+        n_edge += col_kind[tj] != 0;
     }
+    const int n_inner = tiles_j - n_edge;
+    const int nseg = segs ? 2 * tiles_j : 0;
+    const int capm = std::max(cap - nseg, tiles_j);
+    auto edge_chunks = [&](int nl) {
+        const double rows_l = std::ceil((double)nmid / nl) + F;
+        const double re = rows_l / SKEW_EDGE_COST - F;
+        return re >= 1.0 ? std::min(nmid, (int)std::ceil(nmid / re)) : nmid;
+    };
+    int nl = 1;
+    const int nl_max = std::max(1, nmid / std::max(min_rows, 1));
+    for (int c = 1; c <= nl_max; c++) {
+        const int need = n_inner * c + n_edge * (n_inner ? edge_chunks(c) : c);
+        if (need > capm && c > 1) break;
+        nl = c;
+    }
+    const int ne = n_inner ? edge_chunks(nl) : nl;
+    struct T { double key; int4 t; };
+    std::vector<T> ts;
+    auto add = [&](int tj, int i_s, int i_e, int kind) {
+        const int t0 = tj * step - H;
+        const bool src = p.src_on && p.src_i >= i_s - K && p.src_i < i_e + K && p.src_j >= t0 && p.src_j < t0 + 128;
+        if (kind == 0 && src) kind = 1;
+        ts.push_back({(i_s + i_e) * 0.5 / nx + tj * 1e-9, make_int4(tj, i_s, i_e, kind)});
+    };
+    for (int tj = 0; tj < tiles_j; tj++) {
+        if (segs) {
+            add(tj, 0, R, 2);
+            add(tj, nx - R, nx, 2);
+        }
+        const int n = col_kind[tj] ? ne : nl;
+        for (int q = 0; q < n; q++) {
+            const int i_s = mid0 + (int)((long long)q * nmid / n), i_e = mid0 + (int)((long long)(q + 1) * nmid / n);
+            if (i_s < i_e) add(tj, i_s, i_e, segs ? col_kind[tj] : 2);
+        }
+    }
+    std::sort(ts.begin(), ts.end(), [](const T &x, const T &y) { return x.key < y.key; });
+    std::vector<int4> out(ts.size());
+    for (size_t i = 0; i < ts.size(); i++) out[i] = ts[i].t;
+    return out;
+}
+
+// Task list of (depth K, minimum rows L) for this scene, built once and kept on the device.
+static wg_status skew_tasks(wg_scene *s, int K, int L, const int4 **tasks, int *ntasks)
+{
+    SkewPlanCache &c = s->skew[K];
+    if (!c.dev || c.min_rows != L) {
+        const int cap = skew_call(s->dp, nullptr, s->coef, K, nullptr, 0, s->st);
+        const std::vector<int4> v = skew_plan(s->dp, K, L, cap);
+        if (c.dev) cudaFree(c.dev);
+        c.dev = nullptr;
+        WG_CUDA(cudaMalloc(&c.dev, v.size() * sizeof(int4)));
+        WG_CUDA(cudaMemcpy(c.dev, v.data(), v.size() * sizeof(int4), cudaMemcpyHostToDevice));
+        c.n = (int)v.size();
+        c.min_rows = L;
+    }
+    *tasks = c.dev;
+    *ntasks = c.n;
+    return WG_OK;
 }
 
 static int tb_halo(int K) { return (K + 3) & ~3; }
@@ -785,10 +900,6 @@ static wg_status ensure_tb_buffers(wg_scene *s)
             WG_CUDA(cudaMalloc(&s->g[k], fb));
             WG_CUDA(cudaMemsetAsync(s->g[k], 0, fb, s->st));
         }
-    if (!s->tb_ctr) {
-        WG_CUDA(cudaMalloc(&s->tb_ctr, 2 * sizeof(int)));
-        WG_CUDA(cudaMemsetAsync(s->tb_ctr, 0, 2 * sizeof(int), s->st));
-    }
     return WG_OK;
 }
 
@@ -856,7 +967,10 @@ wg_status tb_pass<float>(wg_scene *s, int k)
             set_error("unsupported skewed strip (depth %d of 2..4, %d rows of 8..4096, ny >= 8)", k, L);
             return WG_ERR_INVALID;
         }
-        launch_skew(s->dp, a, s->coef, k, L, s->tb_ctr, s->st);
+        const int4 *tasks = nullptr;
+        int ntasks = 0;
+        if ((st = skew_tasks(s, k, L, &tasks, &ntasks))) return st;
+        skew_call(s->dp, &a, s->coef, k, tasks, ntasks, s->st);
     } else if (clear_error(), !launch_tb(s, a, k, L, W)) {
         if (wg_last_error()[0] == 0) set_error("unsupported temporal block (depth %d, tile %d x %d)", k, L, W);
         return WG_ERR_INVALID;
