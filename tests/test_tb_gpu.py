@@ -58,7 +58,7 @@ def case(name, nx=301, ny=None, seed=0):
 
 CASES = ["dir_kappa_floor", "abs_twospeeds_src", "abs_stadium", "topbot", "osc_left_tall"]
 SHAPES = [(2, 32, 256), (4, 32, 128), (5, 48, 256), (8, 64, 128), (3, 16, 256),
-          (2, 64, 1), (3, 37, 1), (4, 24, 1), (4, 128, 1), (2, 8, 1)]
+          (2, 64, 1), (3, 37, 1), (4, 24, 1), (4, 128, 1), (2, 8, 1), (5, 16, 1), (6, 40, 1)]
 
 
 @pytest.mark.parametrize("name", CASES)

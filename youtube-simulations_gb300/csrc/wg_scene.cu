@@ -433,7 +433,7 @@ wg_status wg_scene_set_blocking(wg_scene *s, int32_t k, int32_t tile_i, int32_t 
         set_error("tile width must be 1 (skewed strips), 128 or 256");
         return WG_ERR_INVALID;
     }
-    if (tile_j == 1 && (tile_i < 8 || tile_i > 4096 || k > 4)) { set_error("skewed strips: 8..4096 rows, depth <= 4"); return WG_ERR_INVALID; }
+    if (tile_j == 1 && (tile_i < 8 || tile_i > 4096 || k > 6)) { set_error("skewed strips: 8..4096 rows, depth <= 6"); return WG_ERR_INVALID; }
     if (tile_j > 1 && tile_i != 0 && (tile_i < 16 || tile_i > 64 || tile_i - 2 * k < 8)) {
         set_error("tile height must be 16..64 with at least 8 core rows");
         return WG_ERR_INVALID;

@@ -4,6 +4,7 @@
 #include "wg_internal.h"
 
 #define WG_TB_MAX_K 16
+#define WG_SKEW_MAX_K 6  // deepest skewed pass
 
 struct SkewPlanCache {
     int4 *dev = nullptr;  // (column tile, first row, end row, edge) per warp
@@ -40,7 +41,7 @@ struct wg_scene {
     uint8_t *rgb = nullptr, *lut = nullptr;
     size_t rgb_bytes = 0;
     int tb_k = 0, tile_i = 0, tile_j = 0;
-    SkewPlanCache skew[5];  // task lists of the skewed kernel, by depth
+    SkewPlanCache skew[WG_SKEW_MAX_K + 1];  // task lists of the skewed kernel, by depth
     float *bv_osc = nullptr, *bv_src = nullptr;  // boundary values of the current step() call
     size_t bv_cap = 0;
     long long bv_t0 = 0;

@@ -442,6 +442,9 @@ __device__ __forceinline__ void cp_async_wait() { asm volatile("cp.async.wait_gr
 
 // Row slot of a warp's shared-memory ring (floats): phi[128], psi[128], tcc[128] (table
 // scenes), then one active word and one edge-column tc per lane.
+#ifndef SKEW_UNROLL
+#define SKEW_UNROLL 1  // rows per loop trip: 3 turns the row windows by renaming registers
+#endif
 template <int COEF> struct SkewSlot {
     static constexpr int PSI = 128, TCC = 256, ACT = (COEF == WG_COEF_TABLE) ? 384 : 256, TCE = ACT + 32, SIZE = TCE + 32;
     static constexpr int DEPTH = (COEF == WG_COEF_TABLE) ? 6 : 8;  // ring slots
@@ -502,9 +505,9 @@ __device__ __forceinline__ void skew_strip(const DevParams &p, const TbArgs &a, 
     for (int q = 0; q < QD; q++) issue(m0 + q, q);
     int slot = 0;  // slot of row m
 
-    for (int mb = m0; mb < m1; mb += 3) {
+    for (int mb = m0; mb < m1; mb += SKEW_UNROLL) {
 #pragma unroll
-        for (int u = 0; u < 3; u++) {
+        for (int u = 0; u < SKEW_UNROLL; u++) {
             const int m = mb + u;
             if (m >= m1) break;  // warp-uniform
             cp_async_wait<QD - 1>();  // row m has landed
@@ -661,7 +664,7 @@ __global__ void __launch_bounds__(128, 4) k_step_skew(const __grid_constant__ De
 
 static bool skew_shape_ok(const DevParams &p, int K, int S)
 {
-    return K >= 2 && K <= 4 && S >= 8 && S <= 4096 && p.ny >= 8 && p.nx >= 2;
+    return K >= 2 && K <= WG_SKEW_MAX_K && S >= 8 && S <= 4096 && p.ny >= 8 && p.nx >= 2;
 }
 
 static int sm_count()
@@ -705,7 +708,9 @@ static int skew_dispatch(const DevParams &p, const TbArgs *a, int K, const int4 
     switch (K) {
     case 2: if (!a) return skew_capacity<COEF, 2, PLAIN>(); launch_skew_k<COEF, 2, PLAIN>(p, *a, tasks, ntasks, st); break;
     case 3: if (!a) return skew_capacity<COEF, 3, PLAIN>(); launch_skew_k<COEF, 3, PLAIN>(p, *a, tasks, ntasks, st); break;
-    default: if (!a) return skew_capacity<COEF, 4, PLAIN>(); launch_skew_k<COEF, 4, PLAIN>(p, *a, tasks, ntasks, st); break;
+    case 4: if (!a) return skew_capacity<COEF, 4, PLAIN>(); launch_skew_k<COEF, 4, PLAIN>(p, *a, tasks, ntasks, st); break;
+    case 5: if (!a) return skew_capacity<COEF, 5, PLAIN>(); launch_skew_k<COEF, 5, PLAIN>(p, *a, tasks, ntasks, st); break;
+    default: if (!a) return skew_capacity<COEF, 6, PLAIN>(); launch_skew_k<COEF, 6, PLAIN>(p, *a, tasks, ntasks, st); break;
     }
     return 0;
 }
@@ -786,6 +791,7 @@ static std::vector<int4> skew_plan(const DevParams &p, int K, int min_rows, int 
 // Task list of (depth K, minimum rows L) for this scene, built once and kept on the device.
 static wg_status skew_tasks(wg_scene *s, int K, int L, const int4 **tasks, int *ntasks)
 {
+    if (K < 0 || K > WG_SKEW_MAX_K) { set_error("skewed depth %d outside 0..%d", K, WG_SKEW_MAX_K); return WG_ERR_INVALID; }
     SkewPlanCache &c = s->skew[K];
     if (!c.dev || c.min_rows != L) {
         const int cap = skew_call(s->dp, nullptr, s->coef, K, nullptr, 0, s->st);
@@ -964,7 +970,7 @@ wg_status tb_pass<float>(wg_scene *s, int k)
     TbArgs a = tb_args(s);
     if (W == 1) {  // time-skewed streaming strips of L rows
         if (!skew_shape_ok(s->dp, k, L)) {
-            set_error("unsupported skewed strip (depth %d of 2..4, %d rows of 8..4096, ny >= 8)", k, L);
+            set_error("unsupported skewed strip (depth %d of 2..6, %d rows of 8..4096, ny >= 8)", k, L);
             return WG_ERR_INVALID;
         }
         const int4 *tasks = nullptr;
@@ -1044,8 +1050,8 @@ void autotune_scene(wg_scene *s)
         float best = 1e30f;
         struct Cand { int k, l, w; };
         const Cand cands[] = {{1, 0, 0},    {2, 16, 256}, {3, 16, 256}, {4, 16, 256}, {4, 24, 256},
-                              {6, 32, 256}, {4, 32, 128}, {2, 16, 1},   {3, 16, 1},   {2, 24, 1},
-                              {3, 24, 1},   {4, 24, 1},   {3, 32, 1}};
+                              {6, 32, 256}, {4, 32, 128}, {2, 16, 1},   {3, 16, 1},   {4, 16, 1},
+                              {5, 16, 1},   {6, 16, 1},   {4, 48, 1}};
         for (const Cand &c : cands) {
             s->tb_k = c.k;
             s->tile_i = c.l;
