@@ -9,8 +9,8 @@
 //  k_step_edge    native form, the four boundary lines and the point source.
 //  k_neumann      Neumann gather of wave_billiard.c:379-389 for the active records.
 //  k_energy_cols  compute_energy (wave_common.c:453-472) per cell, one warp per
-//                 column, FP64 Neumaier sums of j < ny/2 and j >= ny/2.
-//  k_energy_final total and the six compute_energy_tblr boxes from the columns.
+//                 column: sums of j < ny/2 and j >= ny/2, box partials per block.
+//  k_energy_final total and the six compute_energy_tblr boxes from the partials.
 #include "wg_internal.h"
 #include "wg_cells.cuh"
 
@@ -290,16 +290,12 @@ __global__ void k_neumann_fast(DevParams p, const T *__restrict__ phi, T *__rest
 // ---------------------------------------------------------------------------
 // Energy
 // ---------------------------------------------------------------------------
-template <class T>
-__device__ __forceinline__ void warp_merge(Neu &a)
+// Kahan step: s + c carries the running sum (c is minus the part lost so far).
+__device__ __forceinline__ void kahan_add(float &s, float &c, float x)
 {
-#pragma unroll
-    for (int off = 16; off > 0; off >>= 1) {
-        Neu o;
-        o.s = __shfl_down_sync(0xffffffffu, a.s, off);
-        o.c = __shfl_down_sync(0xffffffffu, a.c, off);
-        a.merge(o);
-    }
+    const float y = x - c, t = s + y;
+    c = (t - s) - y;
+    s = t;
 }
 
 // compute_energy in FP32 for FP32 fields (same formula and order as cell_energy).
@@ -314,86 +310,104 @@ __device__ __forceinline__ float cell_energy32(float es2, float hc2, float hc2b,
     return 0.0f;
 }
 
-// One warp per column i.  MASK: 0 = int16 (xy != 0), 1 = "nonzero" bit plane.
-// Per cell compute_energy (wave_common.c:453-472): FP64 for FP64 fields, FP32 for
-// FP32 fields.  Each lane sums its cells in FP64; lanes and columns are combined
-// with Neumaier-compensated FP64 sums.  Outputs the j < ny/2 and j >= ny/2 sums.
+// One warp per column i, eight columns per block.  MASK: 0 = int16 (xy != 0), 1 =
+// "nonzero" bit plane.  Per cell compute_energy (wave_common.c:453-472): FP64 for FP64
+// fields, FP32 for FP32 fields.  Every cell energy is a sum of squares (>= 0), so plain
+// FP64 sums in a tree lose no more than a few ulps: each lane sums its cells (FP32
+// fields: a Kahan sum in FP32, turned into FP64 once), the warp sums its lanes, and
+// the block sums the six boxes of compute_energy_tblr (sub_wave_comp.c:1752-1800)
+// over its columns.  cols[i] = (sum over j < ny/2, sum over j >= ny/2);
+// part[6 b + k] = box k of block b (0..2 top left/mid/right, 3..5 bottom).
+#define ENERGY_COLS_PER_BLOCK 8
 template <class T, int MASK>
-__global__ void __launch_bounds__(256) k_energy_cols(const __grid_constant__ DevParams p, const T *__restrict__ phi,
-                                                     const T *__restrict__ psi, const int16_t *__restrict__ xy,
-                                                     const uint32_t *__restrict__ nz, double2 *__restrict__ bot,
-                                                     double2 *__restrict__ top)
+__global__ void __launch_bounds__(32 * ENERGY_COLS_PER_BLOCK)
+    k_energy_cols(const __grid_constant__ DevParams p, const T *__restrict__ phi, const T *__restrict__ psi,
+                  const int16_t *__restrict__ xy, const uint32_t *__restrict__ nz, int ileft, int iright,
+                  double2 *__restrict__ cols, double *__restrict__ part)
 {
-    const int i = blockIdx.x * (blockDim.x / 32) + threadIdx.x / 32;
-    const int lane = threadIdx.x & 31;
-    if (i >= p.nx) return;
-    const int NX = p.nx, NY = p.ny, jmid = NY / 2;
-    const size_t row = (size_t)i * p.pitch;
-    const int ip = (i + 1 == NX) ? NX - 1 : i + 1, im = (i == 0) ? 0 : i - 1;
-    const T *re = phi + (size_t)ip * p.pitch, *rw = phi + (size_t)im * p.pitch, *rc = phi + row, *ry = psi + row;
-    const float es2 = (float)p.e_scale2, hc2 = (float)p.ehalf_c2, hc2b = (float)p.ehalf_c2b;
+    __shared__ double sh[ENERGY_COLS_PER_BLOCK][2];
+    __shared__ int sbox[ENERGY_COLS_PER_BLOCK];
+    const int wid = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int i = blockIdx.x * ENERGY_COLS_PER_BLOCK + wid;
     double pb = 0.0, pt = 0.0;
-    for (int j = lane; j < NY; j += 32) {
-        const int jp = (j + 1 == NY) ? NY - 1 : j + 1, jm = (j == 0) ? 0 : j - 1;
-        int m;
-        if (MASK == 0) m = xy[row + j] != 0;
-        else m = (nz[(size_t)i * p.wpitch + (j >> 5)] >> (j & 31)) & 1u;
-        double en;
-        if (sizeof(T) == 8)
-            en = cell_energy(p, (double)rc[j], (double)ry[j], (double)re[j], (double)rw[j], (double)rc[jp],
-                             (double)rc[jm], m);
-        else
-            en = (double)cell_energy32(es2, hc2, hc2b, p.twospeeds, (float)rc[j], (float)ry[j], (float)re[j],
-                                       (float)rw[j], (float)rc[jp], (float)rc[jm], m);
-        if (j < jmid) pb += en; else pt += en;
+    if (i < p.nx) {
+        const int NX = p.nx, NY = p.ny, jmid = NY / 2;
+        const size_t row = (size_t)i * p.pitch;
+        const int ip = (i + 1 == NX) ? NX - 1 : i + 1, im = (i == 0) ? 0 : i - 1;
+        const T *re = phi + (size_t)ip * p.pitch, *rw = phi + (size_t)im * p.pitch, *rc = phi + row, *ry = psi + row;
+        const float es2 = (float)p.e_scale2, hc2 = (float)p.ehalf_c2, hc2b = (float)p.ehalf_c2b;
+        float kb = 0.f, kbc = 0.f, kt = 0.f, ktc = 0.f;  // FP32 Kahan sums (FP32 fields)
+#pragma unroll 4
+        for (int j = lane; j < NY; j += 32) {
+            const int jp = (j + 1 == NY) ? NY - 1 : j + 1, jm = (j == 0) ? 0 : j - 1;
+            int m;
+            if (MASK == 0) m = xy[row + j] != 0;
+            else m = (nz[(size_t)i * p.wpitch + (j >> 5)] >> (j & 31)) & 1u;
+            if (sizeof(T) == 8) {
+                const double en = cell_energy(p, (double)rc[j], (double)ry[j], (double)re[j], (double)rw[j],
+                                              (double)rc[jp], (double)rc[jm], m);
+                if (j < jmid) pb += en; else pt += en;
+            } else {
+                const float en = cell_energy32(es2, hc2, hc2b, p.twospeeds, (float)rc[j], (float)ry[j], (float)re[j],
+                                               (float)rw[j], (float)rc[jp], (float)rc[jm], m);
+                if (j < jmid) kahan_add(kb, kbc, en);
+                else kahan_add(kt, ktc, en);
+            }
+        }
+        if (sizeof(T) == 4) {
+            pb = (double)kb - (double)kbc;
+            pt = (double)kt - (double)ktc;
+        }
     }
-    Neu sb, st;
-    sb.add(pb);
-    st.add(pt);
-    warp_merge<T>(sb);
-    warp_merge<T>(st);
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1) {
+        pb += __shfl_down_sync(0xffffffffu, pb, off);
+        pt += __shfl_down_sync(0xffffffffu, pt, off);
+    }
     if (lane == 0) {
-        bot[i] = make_double2(sb.s, sb.c);
-        top[i] = make_double2(st.s, st.c);
+        if (i < p.nx) cols[i] = make_double2(pb, pt);
+        sh[wid][0] = pb;
+        sh[wid][1] = pt;
+        sbox[wid] = (i < ileft) ? 0 : (i < iright ? 1 : 2);
+    }
+    __syncthreads();
+    if (threadIdx.x < 6) {
+        const int k = threadIdx.x, box = k % 3, half = k < 3 ? 1 : 0;  // top boxes sum j >= ny/2
+        double acc = 0.0;
+#pragma unroll
+        for (int w = 0; w < ENERGY_COLS_PER_BLOCK; w++)
+            if (sbox[w] == box) acc += sh[w][half];
+        part[(size_t)blockIdx.x * 6 + k] = acc;
     }
 }
 
 // out[0] = total, out[1..6] = boxes (top left/mid/right, bottom left/mid/right),
-// out[7..7+nx) = column sums over j < ny/2.  One block of 1024 threads.
-__global__ void __launch_bounds__(1024) k_energy_final(int nx, int ileft, int iright, const double2 *__restrict__ bot,
-                                                       const double2 *__restrict__ top, double *__restrict__ out)
+// out[7..7+nx) = column sums over j < ny/2.  One block of 256 threads.
+__global__ void __launch_bounds__(256) k_energy_final(int nx, int nblocks, const double2 *__restrict__ cols,
+                                                      const double *__restrict__ part, double *__restrict__ out)
 {
-    __shared__ double sh_s[7][32], sh_c[7][32];
-    Neu acc[7];  // 0 total, 1..3 top boxes, 4..6 bottom boxes
-    for (int i = threadIdx.x; i < nx; i += blockDim.x) {
-        const double2 b = bot[i], t = top[i];
-        Neu nb, nt;
-        nb.s = b.x; nb.c = b.y;
-        nt.s = t.x; nt.c = t.y;
-        out[7 + i] = nb.value();
-        const int box = (i < ileft) ? 0 : (i < iright ? 1 : 2);
-        acc[0].merge(nb);
-        acc[0].merge(nt);
-        acc[1 + box].merge(nt);
-        acc[4 + box].merge(nb);
-    }
+    __shared__ double sh[6][8];
+    for (int i = threadIdx.x; i < nx; i += blockDim.x) out[7 + i] = cols[i].x;
+    double acc[6] = {0.0, 0.0, 0.0, 0.0, 0.0, 0.0};
+    for (int b = threadIdx.x; b < nblocks; b += blockDim.x)
+#pragma unroll
+        for (int k = 0; k < 6; k++) acc[k] += part[(size_t)b * 6 + k];
     const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
 #pragma unroll
-    for (int k = 0; k < 7; k++) {
-        warp_merge<double>(acc[k]);
-        if (lane == 0) { sh_s[k][wid] = acc[k].s; sh_c[k][wid] = acc[k].c; }
+    for (int k = 0; k < 6; k++) {
+#pragma unroll
+        for (int off = 16; off > 0; off >>= 1) acc[k] += __shfl_down_sync(0xffffffffu, acc[k], off);
+        if (lane == 0) sh[k][wid] = acc[k];
     }
     __syncthreads();
-    if (wid == 0) {
-        const int nw = blockDim.x >> 5;
-#pragma unroll
-        for (int k = 0; k < 7; k++) {
-            Neu a;
-            if (lane < nw) { a.s = sh_s[k][lane]; a.c = sh_c[k][lane]; }
-            warp_merge<double>(a);
-            if (lane == 0) out[k] = a.value();
-        }
+    if (threadIdx.x < 6) {
+        double a = 0.0;
+        for (int w = 0; w < (int)(blockDim.x >> 5); w++) a += sh[threadIdx.x][w];
+        out[1 + threadIdx.x] = a;
+        sh[threadIdx.x][0] = a;
     }
+    __syncthreads();
+    if (threadIdx.x == 0) out[0] = ((sh[0][0] + sh[1][0]) + sh[2][0]) + ((sh[3][0] + sh[4][0]) + sh[5][0]);
 }
 
 // ---------------------------------------------------------------------------
@@ -520,11 +534,12 @@ template <class T>
 void launch_energy(const DevParams &p, const T *phi, const T *psi, const int16_t *xy, const uint32_t *nz,
                    double2 *bot, double2 *top, int ileft, int iright, double *out, cudaStream_t st)
 {
-    const int warps = 8;
-    dim3 grd((p.nx + warps - 1) / warps);
-    if (xy) k_energy_cols<T, 0><<<grd, warps * 32, 0, st>>>(p, phi, psi, xy, nz, bot, top);
-    else k_energy_cols<T, 1><<<grd, warps * 32, 0, st>>>(p, phi, psi, xy, nz, bot, top);
-    k_energy_final<<<1, 1024, 0, st>>>(p.nx, ileft, iright, bot, top, out);
+    // bot: per-column sums; top (2 nx doubles): six box partials per block of 8 columns
+    const int nblocks = (p.nx + ENERGY_COLS_PER_BLOCK - 1) / ENERGY_COLS_PER_BLOCK;
+    double *part = reinterpret_cast<double *>(top);
+    if (xy) k_energy_cols<T, 0><<<nblocks, 32 * ENERGY_COLS_PER_BLOCK, 0, st>>>(p, phi, psi, xy, nz, ileft, iright, bot, part);
+    else k_energy_cols<T, 1><<<nblocks, 32 * ENERGY_COLS_PER_BLOCK, 0, st>>>(p, phi, psi, xy, nz, ileft, iright, bot, part);
+    k_energy_final<<<1, 256, 0, st>>>(p.nx, nblocks, bot, part, out);
 }
 template void launch_energy<float>(const DevParams &, const float *, const float *, const int16_t *, const uint32_t *, double2 *, double2 *, int, int, double *, cudaStream_t);
 template void launch_energy<double>(const DevParams &, const double *, const double *, const int16_t *, const uint32_t *, double2 *, double2 *, int, int, double *, cudaStream_t);

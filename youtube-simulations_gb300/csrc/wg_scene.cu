@@ -397,8 +397,15 @@ wg_status wg_scene_energy(wg_scene *s, double *total, double *columns, int32_t i
     WG_CUDA(cudaGetLastError());
     const size_t nout = columns ? (size_t)s->prm.nx + 7 : 7;
     WG_CUDA(cudaMemcpyAsync(s->hout, s->eout, nout * sizeof(double), cudaMemcpyDeviceToHost, s->st));
+    // the bounded-wait flag rides in the last slot of the same pinned buffer: one sync
+    int *hflag = reinterpret_cast<int *>(s->hout + s->prm.nx + 7);
+    WG_CUDA(cudaMemcpyAsync(hflag, s->dflag, sizeof(int), cudaMemcpyDeviceToHost, s->st));
     WG_CUDA(cudaStreamSynchronize(s->st));
-    if (wg_status fs = scene_check_flag(s)) return fs;
+    if (*hflag) {
+        WG_CUDA(cudaMemsetAsync(s->dflag, 0, sizeof(int), s->st));
+        set_error("a tile load did not complete within its bounded wait; the last step is invalid");
+        return WG_ERR_TIMEOUT;
+    }
     if (total) *total = s->hout[0];
     if (boxes) memcpy(boxes, s->hout + 1, 6 * sizeof(double));
     if (columns) memcpy(columns, s->hout + 7, s->prm.nx * sizeof(double));

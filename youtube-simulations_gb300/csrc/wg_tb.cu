@@ -1046,7 +1046,7 @@ void autotune_scene(wg_scene *s)
         cudaEvent_t e0, e1;
         cudaEventCreate(&e0);
         cudaEventCreate(&e1);
-        const int updates = 24;
+        const int updates = 60;  // a multiple of every depth 2..6
         float best = 1e30f;
         struct Cand { int k, l, w; };
         const Cand cands[] = {{1, 0, 0},    {2, 16, 256}, {3, 16, 256}, {4, 16, 256}, {4, 24, 256},
