@@ -55,6 +55,7 @@ template <class T> void launch_count_nonfinite(int nx, int ny, int pitch, const 
 void launch_pack_mask(int nx, int ny, int wpitch, const int16_t *xy, uint32_t *act, uint32_t *nz, cudaStream_t st);
 template <class T> void launch_convert_in(int nx, int ny, int pitch, const double *src, T *dst, cudaStream_t st);
 template <class T> void launch_convert_out(int nx, int ny, int pitch, const T *src, double *dst, cudaStream_t st);
+template <class T> void launch_repack_in(int nx, int ny, int pitch, const T *src, T *dst, cudaStream_t st);
 void launch_cell_energy(const DevParams &p, const double *phi, const double *psi, const int16_t *xy, int i, int j,
                         double *out, cudaStream_t st);
 

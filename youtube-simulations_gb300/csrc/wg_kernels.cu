@@ -455,6 +455,15 @@ __global__ void k_convert_in(int nx, int ny, int pitch, const double *__restrict
     if (j >= pitch || i >= nx) return;
     dst[(size_t)i * pitch + j] = (j < ny) ? (T)src[(size_t)i * ny + j] : (T)0;
 }
+// Dense [nx][ny] rows of the field precision into the pitched layout (padding zeroed).
+template <class T>
+__global__ void k_repack_in(int nx, int ny, int pitch, const T *__restrict__ src, T *__restrict__ dst)
+{
+    const int j = blockIdx.x * blockDim.x + threadIdx.x;
+    const int i = blockIdx.y;
+    if (j >= pitch || i >= nx) return;
+    dst[(size_t)i * pitch + j] = (j < ny) ? src[(size_t)i * ny + j] : (T)0;
+}
 template <class T>
 __global__ void k_convert_out(int nx, int ny, int pitch, const T *__restrict__ src, double *__restrict__ dst)
 {
@@ -570,6 +579,14 @@ void launch_convert_out(int nx, int ny, int pitch, const T *src, double *dst, cu
     dim3 grd((ny + 255) / 256, nx);
     k_convert_out<T><<<grd, 256, 0, st>>>(nx, ny, pitch, src, dst);
 }
+template <class T>
+void launch_repack_in(int nx, int ny, int pitch, const T *src, T *dst, cudaStream_t st)
+{
+    dim3 grd((pitch + 255) / 256, nx);
+    k_repack_in<T><<<grd, 256, 0, st>>>(nx, ny, pitch, src, dst);
+}
+template void launch_repack_in<float>(int, int, int, const float *, float *, cudaStream_t);
+template void launch_repack_in<double>(int, int, int, const double *, double *, cudaStream_t);
 template void launch_convert_in<float>(int, int, int, const double *, float *, cudaStream_t);
 template void launch_convert_in<double>(int, int, int, const double *, double *, cudaStream_t);
 template void launch_convert_out<float>(int, int, int, const float *, double *, cudaStream_t);

@@ -300,9 +300,20 @@ wg_status wg_scene_upload_state(wg_scene *s, const void *phi, const void *psi, i
     void *dst[2] = {s->f[s->cur], s->f[1 - s->cur]};
     const void *src[2] = {phi, psi};
     if (host_precision == s->prec) {
-        for (int k = 0; k < 2; k++)
-            WG_CUDA(cudaMemcpy2DAsync(dst[k], s->pitch * s->esz, src[k], ny * s->esz, ny * s->esz, nx,
-                                      cudaMemcpyHostToDevice, s->st));
+        // contiguous copies (faster over the host link than row-pitched ones) into the dense
+        // stage, then a repack into the pitched fields on the device
+        const size_t bytes = (size_t)nx * ny * s->esz;
+        if (wg_status st = scene_alloc_dense_stage(s, 2 * bytes)) return st;
+        char *stage = (char *)s->dstage;
+        for (int k = 0; k < 2; k++) {
+            WG_CUDA(cudaMemcpyAsync(stage + k * bytes, src[k], bytes, cudaMemcpyHostToDevice, s->st));
+            if (s->prec == WG_FP32)
+                launch_repack_in<float>(nx, ny, s->pitch, (const float *)(stage + k * bytes), (float *)dst[k], s->st);
+            else
+                launch_repack_in<double>(nx, ny, s->pitch, (const double *)(stage + k * bytes), (double *)dst[k], s->st);
+            s->launches++;
+        }
+        WG_CUDA(cudaGetLastError());
         return WG_OK;  // stream-ordered; the host buffers must stay valid until the next sync
     }
     if (host_precision == WG_FP64) {
