@@ -543,11 +543,15 @@ __device__ __forceinline__ void skew_strip(const DevParams &p, const TbArgs &a, 
 #pragma unroll
             for (int lv = 1; lv <= K; lv++) {
                 const int r = m - lv;  // row of this level's new value
+                float v[4] = {0.f, 0.f, 0.f, 0.f};
+                // Level lv at row r reaches the stored rows only from r >= i_s - K + lv on, i.e.
+                // from input row m0 + 2 lv + 1: in the pipeline fill the earlier levels are skipped
+                // (warp-uniform), and their window slots hold zeros that nothing reads.
+                if (m - m0 >= 2 * lv + 1) {
                 const float *Wc = W[lv - 1][1];
                 const float *Yl = (lv == 1) ? ylev1 : W[lv - 2 >= 0 ? lv - 2 : 0][0];
                 const float e3 = __shfl_down_sync(0xffffffffu, Wc[0], 1);
                 const float w0 = __shfl_up_sync(0xffffffffu, Wc[3], 1);
-                float v[4];
 #pragma unroll
                 for (int c = 0; c < 4; c++) {
                     const float e = (c < 3) ? Wc[c + 1 < 4 ? c + 1 : 3] : e3;
@@ -613,6 +617,7 @@ __device__ __forceinline__ void skew_strip(const DevParams &p, const TbArgs &a, 
                         for (int c = 0; c < 4; c++) v[c] += (cs == c) ? add : 0.f;
                     }
                 }
+                }  // levels in use
 #pragma unroll
                 for (int c = 0; c < 4; c++) {
                     W[lv][0][c] = W[lv][1][c];
@@ -731,11 +736,11 @@ static int skew_call(const DevParams &p, const TbArgs *a, int coef, int K, const
 // inner one.  Chunks are sized so that all warps carry about the same cost and the list
 // fills the resident warps once (inner chunks of at least min_rows rows).  Tasks are
 // ordered by row band so that the boundary chunks spread over the SMs.
-#define SKEW_EDGE_COST 1.25
+#define SKEW_EDGE_COST 1.9  // per-warp timing of the 3840x2160 passes: 1.87 (K 4), 1.90 (K 5)
 static std::vector<int4> skew_plan(const DevParams &p, int K, int min_rows, int cap)
 {
     const int H = (K + 3) & ~3, step = 128 - 2 * H, F = 2 * K + 1;
-    const int nx = p.nx, tiles_j = (p.ny + H + step - 1) / step;
+    const int nx = p.nx, tiles_j = (p.ny + step - 1) / step;  // tile tj stores columns [tj*step, (tj+1)*step)
     const int R = std::max(K + 1, 8);
     const bool segs = nx >= 2 * R + 1;  // else every task is of kind 2
     const int mid0 = segs ? R : 0, mid1 = segs ? nx - R : nx, nmid = mid1 - mid0;
