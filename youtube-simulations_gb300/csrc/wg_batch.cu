@@ -104,41 +104,32 @@ __device__ __forceinline__ void batch_tile(const DevParams &p, const T *__restri
     }
 }
 
+// Persistent blocks take work items (BT_ROWS rows x one column tile of one scene) from
+// a device counter.  Each item's scene entry, first row, column tile and slot come from
+// one int4 of the item table built with the scene table.  The ticket of the following
+// item is taken while this one runs, and read after it, so its latency is hidden.
 template <class T>
-__global__ void __launch_bounds__(256) k_batch_step(const BatchHdr *__restrict__ hdr, const SlotDev *__restrict__ tab,
-                                                    SlotDyn *__restrict__ dyn, int *__restrict__ counter, int u)
+__global__ void __launch_bounds__(256, 4) k_batch_step(const BatchHdr *__restrict__ hdr, const SlotDev *__restrict__ tab,
+                                                    const int4 *__restrict__ items, SlotDyn *__restrict__ dyn,
+                                                    int *__restrict__ counter, int u)
 {
-    __shared__ int item, entry;
-    __shared__ SlotDev sd;
-    const int total = hdr->total_tiles, nact = hdr->nactive;
+    __shared__ int s_next[2];
+    const int total = hdr->total_tiles;
     const int tid = threadIdx.y * blockDim.x + threadIdx.x;
-    while (true) {
-        if (tid == 0) item = atomicAdd(counter + u, 1);
-        __syncthreads();
-        const int it = item;
+    if (tid == 0) s_next[0] = atomicAdd(counter + u, 1);
+    __syncthreads();
+    for (int buf = 0;; buf ^= 1) {
+        const int it = s_next[buf];
         if (it >= total) break;
-        if (tid == 0) {
-            int lo = 0, hi = nact - 1;  // last entry with tile_base <= it
-            while (lo < hi) {
-                const int mid = (lo + hi + 1) >> 1;
-                if (tab[mid].tile_base <= it) lo = mid; else hi = mid - 1;
-            }
-            entry = lo;
-        }
-        __syncthreads();
-        {   // cooperative copy of the scene's table entry into shared memory
-            const int *src = reinterpret_cast<const int *>(tab + entry);
-            int *dst = reinterpret_cast<int *>(&sd);
-            for (int w = tid; w < (int)(sizeof(SlotDev) / sizeof(int)); w += blockDim.x * blockDim.y) dst[w] = src[w];
-        }
-        __syncthreads();
-        const int local = it - sd.tile_base;
-        const int ti = local / sd.tiles_j, tj = local % sd.tiles_j;
-        const SlotDyn d = dyn[sd.slot];
+        int next = 0;
+        if (tid == 0) next = atomicAdd(counter + u, 1);
+        const int4 w = items[it];
+        const SlotDev &sd = tab[w.x];
+        const SlotDyn d = dyn[w.w];
         const int phase = (d.cur + u) & 1;
-        batch_tile<T>(sd.p, (const T *)sd.f[phase], (T *)sd.f[1 - phase], sd.act, sd.nz, ti * BT_ROWS, tj,
-                      d.time + u + 1);
-        __syncthreads();  // sd and item are rewritten for the next work item
+        batch_tile<T>(sd.p, (const T *)sd.f[phase], (T *)sd.f[1 - phase], sd.act, sd.nz, w.y, w.z, d.time + u + 1);
+        if (tid == 0) s_next[buf ^ 1] = next;
+        __syncthreads();  // the next ticket is visible; s_next[buf] is free again
     }
 }
 
@@ -158,11 +149,14 @@ using namespace wg;
 
 namespace wg {
 
+static void batch_drop_graphs(wg_batch *b);
+
 wg_status batch_refresh_table(wg_batch *b)
 {
     constexpr int Vf = 4, Vd = 2;
     const int V = (b->prec == WG_FP32) ? Vf : Vd;
     std::vector<SlotDev> tab;
+    std::vector<int4> items;
     int base = 0;
     long long cells = 0;
     for (int k = 0; k < (int)b->slots.size(); k++) {
@@ -181,6 +175,8 @@ wg_status batch_refresh_table(wg_batch *b)
         d.ntiles = tiles_i * d.tiles_j;
         d.tile_base = base;
         base += d.ntiles;
+        for (int ti = 0; ti < tiles_i; ti++)
+            for (int tj = 0; tj < d.tiles_j; tj++) items.push_back(make_int4((int)tab.size(), ti * BT_ROWS, tj, k));
         cells += (long long)h.prm.nx * h.prm.ny;
         tab.push_back(d);
     }
@@ -191,9 +187,19 @@ wg_status batch_refresh_table(wg_batch *b)
         WG_CUDA(cudaMalloc(&b->d_tab, sizeof(SlotDev) * cap));
         b->tab_cap = cap;
     }
+    if ((int)items.size() > b->items_cap) {
+        if (b->d_items) cudaFree(b->d_items);
+        b->d_items = nullptr;
+        const int cap = std::max(1024, (int)items.size() * 2);
+        WG_CUDA(cudaMalloc(&b->d_items, sizeof(int4) * cap));
+        b->items_cap = cap;
+        batch_drop_graphs(b);  // the graphs hold the item-table pointer
+    }
     // the graphs hold the table pointer: a reallocation invalidates them
-    if (!tab.empty())
+    if (!tab.empty()) {
         WG_CUDA(cudaMemcpyAsync(b->d_tab, tab.data(), sizeof(SlotDev) * tab.size(), cudaMemcpyHostToDevice, b->st));
+        WG_CUDA(cudaMemcpyAsync(b->d_items, items.data(), sizeof(int4) * items.size(), cudaMemcpyHostToDevice, b->st));
+    }
     BatchHdr h{(int)tab.size(), base};
     WG_CUDA(cudaMemcpyAsync(b->d_hdr, &h, sizeof h, cudaMemcpyHostToDevice, b->st));
     WG_CUDA(cudaStreamSynchronize(b->st));
@@ -213,7 +219,8 @@ static void batch_enqueue_frame(wg_batch *b, int n)
 {
     cudaMemsetAsync(b->d_counter, 0, sizeof(int) * n, b->st);
     dim3 blk(BT_THREADS, 4);
-    for (int u = 0; u < n; u++) k_batch_step<T><<<b->persistent_blocks, blk, 0, b->st>>>(b->d_hdr, b->d_tab, b->d_dyn, b->d_counter, u);
+    for (int u = 0; u < n; u++)
+        k_batch_step<T><<<b->persistent_blocks, blk, 0, b->st>>>(b->d_hdr, b->d_tab, b->d_items, b->d_dyn, b->d_counter, u);
     const int cap = std::max(b->tab_cap, 1);
     k_batch_advance<<<(cap + 255) / 256, 256, 0, b->st>>>(b->d_hdr, b->d_tab, b->d_dyn, n);
 }
@@ -265,7 +272,7 @@ wg_status wg_batch_destroy(wg_batch *b)
         void *ptrs[] = {h.f[0], h.f[1], h.act, h.nz, h.ebot, h.etop, h.eout};
         for (void *p : ptrs) if (p) cudaFree(p);
     }
-    void *ptrs[] = {b->d_tab, b->d_dyn, b->d_hdr, b->d_counter};
+    void *ptrs[] = {b->d_tab, b->d_dyn, b->d_hdr, b->d_counter, b->d_items};
     for (void *p : ptrs) if (p) cudaFree(p);
     if (b->h_out) cudaFreeHost(b->h_out);
     if (b->own_stream && b->st) cudaStreamDestroy(b->st);

@@ -6,7 +6,7 @@
 
 namespace wg {
 
-constexpr int BT_ROWS = 8;       // tile rows
+constexpr int BT_ROWS = 32;      // rows of one work item
 constexpr int BT_THREADS = 64;   // threads along j per tile row (x V cells)
 
 struct __align__(16) SlotDev {   // one entry of the compact table of active scenes
@@ -51,6 +51,8 @@ struct wg_batch {
     wg::SlotDyn *d_dyn = nullptr;
     int dyn_cap = 0;
     wg::BatchHdr *d_hdr = nullptr;
+    int4 *d_items = nullptr;                // (table entry, first row, column tile, slot) per work item
+    int items_cap = 0;
     int *d_counter = nullptr;
     int counter_cap = 0;
     int nactive = 0;
