@@ -164,6 +164,15 @@ wg_status wg_compute_energy_x_all(double **phi, double **psi, int16_t **xy_in, d
 wg_status wg_compute_energy_tblr(double **phi, double **psi, int16_t **xy_in,
                                  int32_t ileft, int32_t iright, double energies[6]);
 
+/* add_circular_wave (wave_common.c:337-351): phi += init_amp*factor*exp(-r^2/variance)
+ * *cos(-r/wavelength) on the cells with xy_in != 0 (every cell with TWOSPEEDS), r the
+ * distance of the cell centre (ij_to_xy, sub_wave.c:469-476) from (x, y); psi is not
+ * touched.  init_amp, variance, wavelength are the reference's INITIAL_AMP,
+ * INITIAL_VARIANCE, INITIAL_WAVELENGTH.  Strict mode: the caller's phi rows are
+ * updated; resident mode: the device copy of phi (wg_dropin_sync before reading it). */
+wg_status wg_dropin_add_circular_wave(double init_amp, double factor, double x, double y, double variance,
+                                      double wavelength, double **phi, double **psi, int16_t **xy_in);
+
 /* Energy diagnostics over device fields the caller owns, without any allocation.
  * No counterpart in the reference: it is for callers that cannot allocate device
  * memory at the time they need the diagnostics, e.g. a host program that carves all
@@ -246,6 +255,11 @@ typedef struct wg_frame_params {
 } wg_frame_params;
 wg_status wg_scene_frame_rgb8(wg_scene *s, const wg_frame_params *fp, const uint8_t *lut,
                               uint8_t *rgb_host, void *rgb_device);
+/* add_circular_wave (wave_common.c:337-351) on the scene's phi (level t): the pulse of
+ * wg_dropin_add_circular_wave, with the scene's mask and TWOSPEEDS.  Only the cells where
+ * exp(-r^2/variance) is nonzero in double precision are visited. */
+wg_status wg_scene_add_circular_wave(wg_scene *s, double init_amp, double factor, double x, double y,
+                                     double variance, double wavelength);
 
 /* ------------------------------------------------------------------------- */
 /* 3. Batches of uneven scenes: one persistent launch over a tile work queue   */

@@ -14,7 +14,8 @@
  * current after each call, as the reference's are).  Define WAVEGPU_RESIDENT before
  * including this header to keep the fields in HBM between calls; then call
  * wavegpu_sync() before the host reads phi/psi (draw, energy) and wavegpu_invalidate()
- * after the host writes them (e.g. add_circular_wave).
+ * after the host writes them (e.g. the reference's own add_circular_wave; its device
+ * counterpart wavegpu_add_circular_wave below needs neither).
  */
 #ifndef WAVEGPU_DROPIN_H
 #define WAVEGPU_DROPIN_H
@@ -116,5 +117,21 @@ static void evolve_wave(double *phi[NX], double *psi[NX], double *tmp[NX], short
                                   (const wg_neumann_bc *)neumann_bc, BC_NEUMANN ? n_neumann_points : 0),
                    "evolve_wave");
 }
+
+/* add_circular_wave (wave_common.c:337-351) on the GPU, with the program's INITIAL_AMP,
+ * INITIAL_VARIANCE and INITIAL_WAVELENGTH.  With WAVEGPU_RESIDENT it adds the pulse to the
+ * device copy of phi, so the periodic re-injection of animation() (wave_billiard.c:916-934)
+ * needs no wavegpu_invalidate(); without it the host rows are updated as the reference's
+ * function would update them. */
+#if defined(INITIAL_AMP) && defined(INITIAL_VARIANCE) && defined(INITIAL_WAVELENGTH)
+static void wavegpu_add_circular_wave(double factor, double x, double y, double *phi[NX], double *psi[NX],
+                                      short int *xy_in[NX])
+{
+    wavegpu_ensure_();
+    wavegpu_check_(wg_dropin_add_circular_wave(INITIAL_AMP, factor, x, y, INITIAL_VARIANCE, INITIAL_WAVELENGTH, phi,
+                                               psi, (int16_t **)xy_in),
+                   "add_circular_wave");
+}
+#endif
 
 #endif /* WAVEGPU_DROPIN_H */

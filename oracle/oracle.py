@@ -45,6 +45,8 @@ def _setup(L):
     L.wo_compute_energy.argtypes = [_V, _V, _V, _V, ctypes.c_int, ctypes.c_int]
     L.wo_energy_x.argtypes = [_V, _V, _V, _V, _V]
     L.wo_energy_tblr.argtypes = [_V, _V, _V, _V, ctypes.c_int, ctypes.c_int, _V]
+    _D = ctypes.c_double
+    L.wo_add_circular_wave.argtypes = [_V, _D, _D, _D, _D, _D, _D, _V, _V]
     L.wo_energy_total_naive.restype = ctypes.c_double
     L.wo_energy_total_naive.argtypes = [_V, _V, _V, _V]
     L.wo_energy_total_comp.restype = ctypes.c_double
@@ -125,6 +127,15 @@ def energy_tblr(params, phi, psi, xy, ileft, iright):
     out = np.zeros(6)
     lib().wo_energy_tblr(_pp(params), _p(_f64(phi, n)), _p(_f64(psi, n)),
                          _p(np.ascontiguousarray(xy, np.int16)), ileft, iright, _p(out))
+    return out
+
+
+def add_circular_wave(params, init_amp, factor, x, y, variance, wavelength, phi, xy):
+    """add_circular_wave (wave_common.c:337-351) on a copy of phi; returns the new phi."""
+    n = params.nx * params.ny
+    out = np.array(_f64(phi, n), dtype=np.float64, copy=True)
+    lib().wo_add_circular_wave(_pp(params), init_amp, factor, x, y, variance, wavelength, _p(out),
+                               _p(np.ascontiguousarray(xy, np.int16)))
     return out
 
 

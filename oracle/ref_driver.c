@@ -9,7 +9,8 @@
  *
  * Usage: ref_<variant> <in.bin> <out.bin>.  The input holds a header of 16 int64,
  * 4 doubles, circles, then the fields; see oracle/refio.py for the exact layout.
- * Modes: 0 STEP, 1 SETUP (full builds), 2 TIME, 3 OSC.
+ * Modes: 0 STEP, 1 SETUP (full builds), 2 TIME, 3 OSC, 4 PULSE (full builds:
+ * add_circular_wave(hd[0], hd[2], hd[3], phi, psi, xy_in) on the given fields).
  */
 #define main ref_main
 #include REF_TU
@@ -20,7 +21,7 @@
 #include <string.h>
 #include <omp.h>
 
-enum { M_STEP = 0, M_SETUP = 1, M_TIME = 2, M_OSC = 3 };
+enum { M_STEP = 0, M_SETUP = 1, M_TIME = 2, M_OSC = 3, M_PULSE = 4 };
 
 static void rd(FILE *f, void *p, size_t n)
 {
@@ -146,7 +147,14 @@ int main(int argc, char **argv)
         return 3;
 #endif
     }
-    if (mode == M_SETUP) {
+    if (mode == M_PULSE) {
+#if defined(REF_FULL) && defined(REF_KIND_WB)
+        add_circular_wave(hd[0], hd[2], hd[3], phi, psi, xyrows);
+#else
+        fprintf(stderr, "PULSE needs a full build\n");
+        return 3;
+#endif
+    } else if (mode == M_SETUP) {
 #if defined(REF_FULL) && defined(REF_KIND_WB)
         ncircles = (int)ncirc;
         for (int c = 0; c < ncirc; c++) {

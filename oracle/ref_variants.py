@@ -26,6 +26,7 @@ SMALL_BASE = dict(
     OMEGA=0.05, OMEGA_B=0.03, AMPLITUDE=1.0, DAMPING=0.0, ACHIRP=0.25,
     OSCIL_LEFT_YSHIFT=0.0, OSCIL_YMAX=0.6, OSCIL_YMID=0.1,
     INITIAL_VARIANCE=0.0003, INITIAL_SHIFT=20.0, WAVE_PACKET_SHIFT=200.0,
+    INITIAL_AMP=1.0, INITIAL_WAVELENGTH=0.01,
     B_DOMAIN=1, LAMBDA=1.8, NPOLY=6, APOLY=0.0, VARIABLE_IOR=0,
 )
 

@@ -3,7 +3,7 @@
 File layout read by oracle/ref_driver.c:
   int64[16]  magic 0x57415645, nx, ny, mode, nsteps, n_nbc, ncircles, ileft, iright,
              src_on, src_i, src_j, n_times, 0, 0, 0
-  double[4]  src_amp, src_period, 0, 0
+  double[4]  src_amp, src_period, 0, 0 (PULSE: factor, 0, x, y)
   double[3*ncircles] circles (xc, yc, r)
   mode OSC : int32[n_times]
   else     : double phi, psi, tmp, tcc, tc, tgamma [nx*ny each]; int16 xy [nx*ny];
@@ -20,7 +20,7 @@ import numpy as np
 
 HERE = Path(__file__).resolve().parent
 BIN = HERE / "_ref" / "bin"
-STEP, SETUP, TIME, OSC = 0, 1, 2, 3
+STEP, SETUP, TIME, OSC, PULSE = 0, 1, 2, 3, 4
 
 
 def available(variant):
@@ -33,7 +33,7 @@ def _neumann_dtype():
 
 
 def run(variant, nx, ny, mode=STEP, nsteps=0, fields=None, xy=None, nbc=None, circles=None,
-        src=None, times=None, threads=None, timeout=600):
+        src=None, times=None, threads=None, timeout=600, pulse=None):
     circles = np.zeros((0, 3)) if circles is None else np.asarray(circles, np.float64)[:, :3]
     n_nbc = 0 if nbc is None else len(nbc)
     hdr = np.zeros(16, np.int64)
@@ -44,6 +44,8 @@ def run(variant, nx, ny, mode=STEP, nsteps=0, fields=None, xy=None, nbc=None, ci
         hd[0], hd[1] = src[2], src[3]
     if times is not None:
         hdr[12] = len(times)
+    if pulse is not None:  # PULSE: (factor, x, y) of add_circular_wave
+        hd[0], hd[2], hd[3] = pulse
     with tempfile.TemporaryDirectory() as td:
         fin, fout = Path(td) / "in.bin", Path(td) / "out.bin"
         with open(fin, "wb") as f:

@@ -681,3 +681,20 @@ int wo_init_neumann(const wg_params *p, int domain, double lambda, int npoly, do
     }
     return n;
 }
+
+/* add_circular_wave (wave_common.c:337-351): adds INITIAL_AMP*factor*exp(-r^2/VARIANCE)
+ * *cos(-r/WAVELENGTH) to phi on the cells with xy_in != 0 (all cells with TWOSPEEDS);
+ * psi is not touched.  Same expression order as the reference. */
+void wo_add_circular_wave(const wg_params *p, double init_amp, double factor, double x, double y,
+                          double variance, double wavelength, double *phi, const int16_t *xy_in)
+{
+    for (int i = 0; i < p->nx; i++)
+        for (int j = 0; j < p->ny; j++) {
+            double xy[2], dist2;
+            wo_ij_to_xy(p, i, j, xy);
+            dist2 = (xy[0] - x) * (xy[0] - x) + (xy[1] - y) * (xy[1] - y);
+            const size_t c = (size_t)i * p->ny + j;
+            if ((xy_in[c]) || (p->twospeeds))
+                phi[c] += init_amp * factor * exp(-dist2 / variance) * cos(-sqrt(dist2) / wavelength);
+        }
+}

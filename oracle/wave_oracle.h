@@ -75,6 +75,9 @@ void wo_mask(const wg_params *p, int domain, double lambda, int npoly, double ap
 
 /* init_ior_2d constant/two-speed branch (sub_wave.c:12983-13002). */
 void wo_init_ior(const wg_params *p, const int16_t *xy_in, double *tcc, double *tc, double *tgamma);
+/* add_circular_wave (wave_common.c:337-351) on flat [nx][ny] arrays. */
+void wo_add_circular_wave(const wg_params *p, double init_amp, double factor, double x, double y,
+                          double variance, double wavelength, double *phi, const int16_t *xy_in);
 
 /* init_neumann_bc for D_ELLIPSE (domain 1) / D_POLYGON (domain 8); marks ghost cells
  * -1 in xy_in and returns the record count (or -1 on overflow). */

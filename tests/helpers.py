@@ -1,6 +1,7 @@
 """Shared test inputs: deterministic seeded scenes for every compiled-reference variant."""
 import numpy as np
 
+import oracle
 import ref_variants
 from youtube_simulations_gb300 import params as P
 from youtube_simulations_gb300 import scenes
@@ -48,6 +49,22 @@ def variant_inputs(variant, seed=1, noisy_tmp=True, smooth=False):
     tmp = 0.3 * rng.standard_normal(n) if noisy_tmp else np.zeros(n)
     fields = dict(phi=phi, psi=psi, tmp=tmp, tcc=tcc, tc=tc, tgamma=tg)
     return p, fields, xy, nbc
+
+
+# add_circular_wave cases: (variant, factor, x, y); full builds of the reference carry it
+PULSE_CASES = [("full_stadium", -0.7, 0.31, -0.12), ("full_neu_ellipse", 1.3, -0.52, 0.21), ("c1", 0.9, 0.4, -0.3)]
+
+
+def pulse_inputs(variant, seed=7):
+    """(params, macros, phi, psi, xy) for an add_circular_wave case: the variant's mask
+    (the oracle's restatement of the reference's, pinned elsewhere), seeded phi/psi."""
+    m = ref_variants.VARIANTS[variant]["macros"]
+    p = params_of(variant)
+    xy = oracle.mask(p, m["B_DOMAIN"], m["LAMBDA"], m.get("NPOLY", 6), m.get("APOLY", 0.0))
+    rng = np.random.default_rng(seed)
+    phi = rng.standard_normal(p.nx * p.ny) * 0.01
+    psi = rng.standard_normal(p.nx * p.ny) * 0.01
+    return p, m, phi, psi, xy
 
 
 def rel_err(a, b):

@@ -12,9 +12,10 @@ import numpy as np
 import pytest
 
 import oracle
-from helpers import variant_inputs
+from helpers import pulse_inputs, variant_inputs
 
 GOLDEN = json.loads((Path(__file__).resolve().parent / "golden" / "reference_outputs.json").read_text())
+PULSES = json.loads((Path(__file__).resolve().parent / "golden" / "reference_pulses.json").read_text())
 
 
 def digest(*arrays):
@@ -53,3 +54,17 @@ def test_oracle_matches_recorded_reference(key):
             assert abs(float(np.sum(got[k] ** 2)) - rec["sumsq"][k]) <= 1e-12 * max(rec["sumsq"][k], 1e-300)
         else:
             assert digest(got[k]) == rec["output_sha256"][k], k
+
+
+@pytest.mark.parametrize("name", sorted(PULSES))
+def test_add_circular_wave_matches_recorded_reference(name):
+    """add_circular_wave (wave_common.c:337-351): the oracle against the reference's
+    recorded output; exact hash, or (another libm's exp/cos) sums within 1e-12."""
+    rec = PULSES[name]
+    p, m, phi, psi, xy = pulse_inputs(name)
+    assert digest(phi, psi, xy) == rec["input_sha256"]
+    got = oracle.add_circular_wave(p, m["INITIAL_AMP"], rec["factor"], rec["x"], rec["y"], m["INITIAL_VARIANCE"],
+                                   m["INITIAL_WAVELENGTH"], phi, xy)
+    if digest(got) != rec["output_sha256"]:
+        assert abs(float(np.sum(got)) - rec["sum"]) <= 1e-12 * rec["max_abs"] * got.size
+        assert abs(float(np.sum(got ** 2)) - rec["sumsq"]) <= 1e-12 * rec["sumsq"]

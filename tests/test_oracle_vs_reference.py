@@ -9,7 +9,7 @@ import pytest
 import oracle
 import ref_variants
 import refio
-from helpers import params_of, variant_inputs
+from helpers import PULSE_CASES, params_of, pulse_inputs, variant_inputs
 
 pytestmark = pytest.mark.skipif(not refio.available("s_dir"), reason="compiled reference absent")
 
@@ -128,3 +128,18 @@ def test_mask_setup_bitexact(variant, domain, lam):
     assert np.array_equal(scenes.mask(p, domain, lam=lam), ref["xy"])
     tcc, tc, tg = scenes.tables(p, ref["xy"])
     assert np.array_equal(tcc, ref["tcc"]) and np.array_equal(tg, ref["tgamma"])
+
+
+@pytest.mark.parametrize("variant,factor,x,y", PULSE_CASES)
+def test_add_circular_wave_bitexact(variant, factor, x, y):
+    """add_circular_wave (wave_common.c:337-351) of the reference's full build against
+    the oracle, bit for bit (psi untouched)."""
+    if not refio.available(variant):
+        pytest.skip("full build absent")
+    p, m, phi, psi, xy = pulse_inputs(variant)
+    ref = refio.run(variant, p.nx, p.ny, refio.PULSE, fields={"phi": phi, "psi": psi}, xy=xy, pulse=(factor, x, y))
+    mine = oracle.add_circular_wave(p, m["INITIAL_AMP"], factor, x, y, m["INITIAL_VARIANCE"], m["INITIAL_WAVELENGTH"],
+                                    phi, xy)
+    assert np.array_equal(mine, ref["phi"])
+    assert np.array_equal(psi, ref["psi"])
+    assert not np.array_equal(mine, phi)

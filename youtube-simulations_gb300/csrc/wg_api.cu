@@ -417,6 +417,27 @@ wg_status wg_dropin_sync(void)
     return WG_OK;
 }
 
+wg_status wg_dropin_add_circular_wave(double init_amp, double factor, double x, double y, double variance,
+                                      double wavelength, double **phi, double **psi, int16_t **xy_in)
+{
+    std::lock_guard<std::mutex> lk(g_di_mu);
+    wg_status s = di_require();
+    if (s) return s;
+    if (!phi || !psi || !xy_in) { set_error("NULL argument"); return WG_ERR_INVALID; }
+    PulseArgs pa;
+    if ((s = pulse_args(g_di.prm, g_di.pitch, g_di.dp.wpitch, init_amp, factor, x, y, variance, wavelength, &pa)))
+        return s;
+    if ((s = di_statics(xy_in, nullptr, nullptr, nullptr, false))) return s;
+    bool fresh;
+    const int k = di_slot(phi, 0, &fresh);
+    if (k < 0) { set_error("too many field arrays"); return WG_ERR_STATE; }
+    if (fresh && (s = di_upload_rows<double>(phi, g_di.buf[k]))) return s;
+    launch_add_circular_wave<double>(pa, g_di.buf[k], g_di.xy, nullptr, g_di.st);
+    WG_CUDA(cudaGetLastError());
+    if (g_di.mode == WG_DROPIN_STRICT) return di_download_rows(g_di.buf[k], phi);
+    return WG_OK;
+}
+
 wg_status wg_dropin_invalidate(void)
 {
     std::lock_guard<std::mutex> lk(g_di_mu);

@@ -56,6 +56,19 @@ void launch_pack_mask(int nx, int ny, int wpitch, const int16_t *xy, uint32_t *a
 template <class T> void launch_convert_in(int nx, int ny, int pitch, const double *src, T *dst, cudaStream_t st);
 template <class T> void launch_convert_out(int nx, int ny, int pitch, const T *src, double *dst, cudaStream_t st);
 template <class T> void launch_repack_in(int nx, int ny, int pitch, const T *src, T *dst, cudaStream_t st);
+
+// add_circular_wave (wg_pulse.cu): the grid geometry, the pulse and the box of cells to visit
+struct PulseArgs {
+    int nx, ny, pitch, wpitch, twospeeds;
+    int i0, ni, j0, nj;
+    double init_amp, factor, x, y, variance, wavelength;
+    double xmin, xspan, ymin, yspan;
+};
+wg_status pulse_args(const wg_params &p, int pitch, int wpitch, double init_amp, double factor, double x, double y,
+                     double variance, double wavelength, PulseArgs *a);
+// xy (int16 mask, nonzero test) or, when xy is NULL, nz (the "nonzero" bit plane)
+template <class T> void launch_add_circular_wave(const PulseArgs &a, T *phi, const int16_t *xy, const uint32_t *nz,
+                                                 cudaStream_t st);
 void launch_cell_energy(const DevParams &p, const double *phi, const double *psi, const int16_t *xy, int i, int j,
                         double *out, cudaStream_t st);
 

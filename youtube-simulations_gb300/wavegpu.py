@@ -60,6 +60,7 @@ SIGNATURES = {
     "wg_compute_energy_x_all": (_I32, [_PP, _PP, _PP, _V]),
     "wg_compute_energy_tblr": (_I32, [_PP, _PP, _PP, _I32, _I32, _V]),
     "wg_compute_energy_device_noalloc": (_I32, [_V, _V, _V, _V, _I32, _I32, _I32, _V, _V]),
+    "wg_dropin_add_circular_wave": (_I32, [_D, _D, _D, _D, _D, _D, _PP, _PP, _PP]),
     "wg_scene_create": (_I32, [_V, _I32, _I32, _V, ctypes.POINTER(_V)]),
     "wg_scene_destroy": (_I32, [_V]),
     "wg_scene_bytes": (_I32, [_V, _I32, _I32, ctypes.POINTER(ctypes.c_size_t)]),
@@ -77,6 +78,7 @@ SIGNATURES = {
     "wg_scene_launch_count": (_I32, [_V, ctypes.POINTER(_I64)]),
     "wg_scene_check_finite": (_I32, [_V, ctypes.POINTER(_I64)]),
     "wg_scene_frame_rgb8": (_I32, [_V, _V, _V, _V, _V]),
+    "wg_scene_add_circular_wave": (_I32, [_V, _D, _D, _D, _D, _D, _D]),
     "wg_batch_create": (_I32, [_I32, _V, ctypes.POINTER(_V)]),
     "wg_batch_destroy": (_I32, [_V]),
     "wg_batch_add": (_I32, [_V, _V, _V, _V, _V, ctypes.POINTER(_I32)]),
@@ -206,6 +208,13 @@ def compute_energy_tblr(f, ileft, iright, a="phi", b="psi"):
     return out
 
 
+def add_circular_wave(f, factor, x, y, init_amp=1.0, variance=0.0003, wavelength=0.01, a="phi", b="psi"):
+    """wg_dropin_add_circular_wave: the reference's add_circular_wave (wave_common.c:337-351)
+    on the row arrays of a RowFields (or on their resident device copy)."""
+    check(lib().wg_dropin_add_circular_wave(init_amp, factor, x, y, variance, wavelength, f.rows(a), f.rows(b),
+                                            f.rows("xy")))
+
+
 def dropin_time():
     t = ctypes.c_int64()
     check(lib().wg_dropin_get_time(ctypes.byref(t)))
@@ -286,6 +295,10 @@ class Scene:
         boxes = np.zeros(6)
         check(lib().wg_scene_energy(self.h, ctypes.byref(total), cols.ctypes.data, ileft, iright, boxes.ctypes.data))
         return total.value, cols, boxes
+
+    def add_circular_wave(self, factor, x, y, init_amp=1.0, variance=0.0003, wavelength=0.01):
+        """add_circular_wave (wave_common.c:337-351) on the scene's phi."""
+        check(lib().wg_scene_add_circular_wave(self.h, init_amp, factor, x, y, variance, wavelength))
 
     def total_energy(self):
         total = ctypes.c_double()
