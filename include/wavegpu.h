@@ -236,14 +236,30 @@ wg_status wg_scene_launch_count(wg_scene *s, int64_t *n);
 /* Blow-up detector: *bad = number of non-finite phi values (0 = healthy). */
 wg_status wg_scene_check_finite(wg_scene *s, int64_t *bad);
 
-/* Colour-mapped frame: the P_AMPLITUDE colour map of phi (wave_common.c:1053-1065,
+/* Colour-mapped frame of draw_wave_highres_palette (wave_common.c:1053-1162,
  * 1750-1848; colors_waves.c:3-16,161-218; colormaps.c:2449-2482) at every size-th
  * cell, as an RGB8 image of (ny/size) rows x (nx/size) columns, row r = j/size from
- * the bottom (GL's origin), column = i/size.  Drawn cells (TWOSPEEDS or xy != 0) take
- * palette entry min(255, (int)(256 * 0.5 * (1 + COLOR_RANGE*tanh(SLOPE*(VSHIFT +
- * VSCALE*phi)/scale)))) of the caller's 256x3 byte palette `lut` (the reference's
- * turbo_srgb_bytes), times the optional fades, rounded; other cells are black.
+ * the bottom (GL's origin), column = i/size, for the C_ONEDIM colour scheme with the
+ * caller's 256x3 byte palette `lut` (e.g. the reference's turbo_srgb_bytes).
+ * Per sampled cell, `plot` selects the value (wave_value, wave_common.c:1053-1162):
+ *   WG_P_AMPLITUDE  VSHIFT + VSCALE*phi;  WG_P_ENERGY  compute_energy;  WG_P_MIXED
+ *   phi above NY/2, energy below;  WG_P_MEAN_ENERGY  running sum of energy / (time+1);
+ *   WG_P_LOG_ENERGY / _LOG_MEAN_ENERGY  LOG_SHIFT + LOG_SCALE*log(...);  WG_P_ENERGY_FLUX
+ *   FLUX_SCALE*|phi-psi|*|grad phi|;  WG_P_TOTAL_ENERGY_FLUX  direction of the decaying
+ *   (x0.99 per frame) sum of the flux on a wrapped linear scale, dimmed by
+ *   tanh(FLUX_SCALE*|sum|);  WG_P_AVERAGE_ENERGY / _LOG_AVERAGE_ENERGY  exponential
+ *   average with AVRG_E_FACTOR.
+ * amplitude = COLOR_RANGE*tanh(SLOPE*value/scale)*exp(-time*ATTENUATION); palette entry
+ * (int)(256*h), clamped to 0..255, with h = 0.5*(1 + amplitude), or h = amplitude for
+ * the energy and flux modes (color_scheme_asym_palette).  Drawn cells (TWOSPEEDS or
+ * xy != 0) take that entry times the optional fades, rounded; other cells are black.
+ * The running sums (mean, average, total flux) live in the scene at frame resolution
+ * and are updated on every sampled cell by each call; they restart at zero on
+ * wg_scene_frame_reset or when `plot` or `size` changes.
  * rgb_host and/or rgb_device receive the image (either may be NULL). */
+enum { WG_P_AMPLITUDE = 0, WG_P_ENERGY = 1, WG_P_MIXED = 2, WG_P_MEAN_ENERGY = 3, WG_P_LOG_ENERGY = 4,
+       WG_P_LOG_MEAN_ENERGY = 5, WG_P_ENERGY_FLUX = 6, WG_P_TOTAL_ENERGY_FLUX = 7, WG_P_AVERAGE_ENERGY = 8,
+       WG_P_LOG_AVERAGE_ENERGY = 9 };  /* P_* of global_pdes.c:318-327 */
 typedef struct wg_frame_params {
     int32_t size;            /* downsampling (draw_wave_highres_palette's size=2) */
     int32_t fade;            /* apply fade_value */
@@ -251,10 +267,19 @@ typedef struct wg_frame_params {
     double slope, color_range, scale; /* SLOPE, COLOR_RANGE, scale */
     double fade_value;
     int32_t fade_in_obstacle; /* FADE_IN_OBSTACLE: times (tcc/COURANT^2)^0.1 (wave_common.c:1739-1748) */
+    int32_t plot;            /* WG_P_* */
+    double log_shift, log_scale;  /* LOG_SHIFT, LOG_SCALE */
+    double flux_scale;       /* FLUX_SCALE */
+    double avrg_e_factor;    /* AVRG_E_FACTOR */
+    double attenuation;      /* ATTENUATION */
+    int32_t time;            /* the frame counter `time` of draw_wave_highres_palette */
     int32_t reserved;
 } wg_frame_params;
 wg_status wg_scene_frame_rgb8(wg_scene *s, const wg_frame_params *fp, const uint8_t *lut,
                               uint8_t *rgb_host, void *rgb_device);
+/* Restart the frame's running sums (the reference's total_energy, average_energy and
+ * total_flux arrays) at zero. */
+wg_status wg_scene_frame_reset(wg_scene *s);
 /* add_circular_wave (wave_common.c:337-351) on the scene's phi (level t): the pulse of
  * wg_dropin_add_circular_wave, with the scene's mask and TWOSPEEDS.  Only the cells where
  * exp(-r^2/variance) is nonzero in double precision are visited. */

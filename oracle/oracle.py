@@ -47,6 +47,7 @@ def _setup(L):
     L.wo_energy_tblr.argtypes = [_V, _V, _V, _V, ctypes.c_int, ctypes.c_int, _V]
     _D = ctypes.c_double
     L.wo_add_circular_wave.argtypes = [_V, _D, _D, _D, _D, _D, _D, _V, _V]
+    L.wo_frame_cells.argtypes = [_V, _V, _V, _V, ctypes.c_int, _V, _V, _V, _V]
     L.wo_energy_total_naive.restype = ctypes.c_double
     L.wo_energy_total_naive.argtypes = [_V, _V, _V, _V]
     L.wo_energy_total_comp.restype = ctypes.c_double
@@ -181,11 +182,35 @@ def init_neumann(params, domain, lam, xy, npoly=6, apoly=0.0, max_records=80000)
     return xy, recs[:n].copy()
 
 
+def frame_cells(params, phi, psi, xy, size):
+    """compute_energy and the compute_energy_flux velocity / gradients at the sampled
+    cells, arrays [row = j/size][col = i/size] (wo_frame_cells)."""
+    n = params.nx * params.ny
+    w, h = params.nx // size, params.ny // size
+    out = [np.zeros(w * h) for _ in range(4)]
+    lib().wo_frame_cells(_pp(params), _p(_f64(phi, n)), _p(_f64(psi, n)), _p(np.ascontiguousarray(xy, np.int16)),
+                         int(size), *[_p(a) for a in out])
+    return [a.reshape(h, w) for a in out]
+
+
+_PI, _PID, _DPI = 3.141592654, 1.570796327, 6.283185307  # global_pdes.c:8-10
+
+
+def _argument(x, y):
+    """argument() of sub_wave.c:287-302, elementwise."""
+    safe = np.where(x != 0.0, x, 1.0)
+    a = np.arctan(y / safe) + np.where(x < 0.0, _PI, 0.0)
+    return np.where(x != 0.0, a, np.where(y < 0.0, _PI * 1.5, _PID))
+
+
 def frame_rgb8(params, phi, xy, lut, size=2, vshift=-0.2, vscale=1.0, slope=1.0, color_range=0.8, scale=1.0,
-               fade=False, fade_value=1.0, fade_in_obstacle=False, tcc=None):
-    """P_AMPLITUDE frame of draw_wave_highres_palette (wave_common.c:1053-1065,
-    1750-1848; colors_waves.c:3-16, 161-218; colormaps.c:2449-2482) with the palette
-    `lut` (256x3 bytes): rows j/size from the bottom, columns i/size."""
+               fade=False, fade_value=1.0, fade_in_obstacle=False, tcc=None, plot=0, psi=None, state=None,
+               log_shift=0.75, log_scale=0.75, flux_scale=250.0, avrg_e_factor=0.95, attenuation=0.0, time=0):
+    """draw_wave_highres_palette (wave_common.c:1750-1848) with wave_value (wave_common.c:
+    1053-1162) for the C_ONEDIM scheme (colors_waves.c:3-22, 161-258; colormaps.c:
+    2449-2482) and the palette `lut` (256x3 bytes): rows j/size from the bottom, columns
+    i/size.  `state` (a dict) carries the running sums of the mean, average and
+    total-flux modes from one frame to the next."""
     nx, ny = params.nx, params.ny
     phi2 = np.asarray(phi, np.float64).reshape(nx, ny)
     xy2 = np.asarray(xy).reshape(nx, ny)
@@ -193,16 +218,62 @@ def frame_rgb8(params, phi, xy, lut, size=2, vshift=-0.2, vscale=1.0, slope=1.0,
     ii = np.arange(w) * size
     jj = np.arange(h) * size
     v = phi2[np.ix_(ii, jj)].T                      # [row = j][col = i]
-    drawn = (xy2[np.ix_(ii, jj)].T != 0) | bool(params.twospeeds)
-    value = vshift + vscale * v
-    amp = color_range * np.tanh(slope * value / scale)
-    hue = (256.0 * (0.5 * (1.0 + amp))).astype(np.int64)
-    hue = np.clip(hue, 0, 255)
-    f = np.ones_like(value)
+    m = xy2[np.ix_(ii, jj)].T != 0
+    drawn = m | bool(params.twospeeds)
+    state = {} if state is None else state
+    asym, linear, dim = False, False, np.ones_like(v)
+    if plot != 0:
+        energy, vel, gx, gy = frame_cells(params, phi, psi, xy, size)
+    if plot == 0:
+        value = vshift + vscale * v
+    elif plot == 1:
+        value, asym = energy, True
+    elif plot == 2:
+        value = np.where((jj > ny // 2)[:, None], v, energy)
+    elif plot == 3:
+        acc = state.setdefault("acc", np.zeros((h, w)))
+        acc += energy
+        value, asym = acc / float(time + 1), True
+    elif plot == 4:
+        value = log_shift + log_scale * np.log(np.where(energy < 1.0e-20, 1.0e-20, energy))
+    elif plot == 5:
+        acc = state.setdefault("acc", np.zeros((h, w)))
+        acc += np.where(energy == 0.0, 1.0e-20, energy)
+        value = log_shift + log_scale * np.log(acc / float(time + 1))
+    elif plot == 6:
+        mod = np.where(drawn, vel * np.sqrt(gx * gx + gy * gy), 0.0)
+        value, asym = mod * flux_scale, True
+    elif plot == 7:
+        tx = state.setdefault("fx", np.zeros((h, w)))
+        ty = state.setdefault("fy", np.zeros((h, w)))
+        tx[...] = tx * 0.99 + np.where(drawn, vel * gx, 0.0)
+        ty[...] = ty * 0.99 + np.where(drawn, vel * gy, 0.0)
+        mod = np.sqrt(tx * tx + ty * ty)
+        arg = _argument(tx, ty)
+        arg = np.where(arg < 0.0, arg + _DPI, arg)
+        value, linear, dim = arg / _DPI, True, np.tanh(mod * flux_scale)
+    else:
+        acc = state.setdefault("acc", np.zeros((h, w)))
+        acc[...] = avrg_e_factor * acc + (1.0 - avrg_e_factor) * energy
+        if plot == 8:
+            value, asym = acc.copy(), True
+        else:
+            with np.errstate(divide="ignore"):
+                value = np.where(acc == 0.0, log_shift - 10.0 * log_scale, log_shift + log_scale * np.log(acc))
+    if linear:
+        hh = slope * value
+        hh = np.where(hh > 1.0, hh - 1.0, np.where(hh < 0.0, hh + 1.0, hh))
+    else:
+        amp = color_range * np.tanh(slope * value / scale)
+        if attenuation != 0.0:
+            amp = amp * np.exp(-(float(time) * attenuation))
+        hh = amp if asym else 0.5 * (1.0 + amp)
+    hv = 256.0 * hh
+    hue = np.trunc(np.clip(hv, 0.0, 255.0)).astype(np.int64)
+    f = dim.copy()
     if fade_in_obstacle:
         c2 = params.courant * params.courant
         if tcc is None:
-            m = xy2[np.ix_(ii, jj)].T != 0
             cc = np.where(m, c2, params.courantb * params.courantb)
         else:
             cc = np.asarray(tcc, np.float64).reshape(nx, ny)[np.ix_(ii, jj)].T

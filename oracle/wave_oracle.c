@@ -698,3 +698,27 @@ void wo_add_circular_wave(const wg_params *p, double init_amp, double factor, do
                 phi[c] += init_amp * factor * exp(-dist2 / variance) * cos(-sqrt(dist2) / wavelength);
         }
 }
+
+/* Per sampled cell (i = col*size, j = row*size; arrays [row][col]) of
+ * draw_wave_highres_palette (wave_common.c:1750-1848): compute_energy
+ * (wave_common.c:453-472), and the velocity |phi - psi| and gradients of
+ * compute_energy_flux (wave_common.c:475-511). */
+void wo_frame_cells(const wg_params *p, const double *phi, const double *psi, const int16_t *xy_in, int size,
+                    double *energy, double *vel, double *gx, double *gy)
+{
+    const int NX = p->nx, NY = p->ny, w = NX / size, h = NY / size;
+    for (int row = 0; row < h; row++)
+        for (int col = 0; col < w; col++) {
+            const int i = col * size, j = row * size;
+            const size_t k = (size_t)row * w + col;
+            int iplus = i + 1, iminus = i - 1, jplus = j + 1, jminus = j - 1;
+            if (iplus == NX) iplus = NX - 1;
+            if (iminus == -1) iminus = 0;
+            if (jplus == NY) jplus = NY - 1;
+            if (jminus == -1) jminus = 0;
+            energy[k] = wo_compute_energy(p, phi, psi, xy_in, i, j);
+            vel[k] = fabs(phi[(size_t)i * NY + j] - psi[(size_t)i * NY + j]);
+            gx[k] = phi[(size_t)iplus * NY + j] - phi[(size_t)iminus * NY + j];
+            gy[k] = phi[(size_t)i * NY + jplus] - phi[(size_t)i * NY + jminus];
+        }
+}

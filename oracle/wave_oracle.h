@@ -75,6 +75,10 @@ void wo_mask(const wg_params *p, int domain, double lambda, int npoly, double ap
 
 /* init_ior_2d constant/two-speed branch (sub_wave.c:12983-13002). */
 void wo_init_ior(const wg_params *p, const int16_t *xy_in, double *tcc, double *tc, double *tgamma);
+/* compute_energy and the compute_energy_flux velocity/gradients at the sampled cells
+ * of draw_wave_highres_palette (arrays [row][col], row = j/size, col = i/size). */
+void wo_frame_cells(const wg_params *p, const double *phi, const double *psi, const int16_t *xy_in, int size,
+                    double *energy, double *vel, double *gx, double *gy);
 /* add_circular_wave (wave_common.c:337-351) on flat [nx][ny] arrays. */
 void wo_add_circular_wave(const wg_params *p, double init_amp, double factor, double x, double y,
                           double variance, double wavelength, double *phi, const int16_t *xy_in);

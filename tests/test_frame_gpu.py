@@ -1,8 +1,10 @@
 """RGB8 frames of a scene (wg_scene_frame_rgb8) against the oracle's restatement of
-draw_wave_highres_palette's P_AMPLITUDE colour map.  The palette is a seeded
-synthetic 256x3 byte table (the caller supplies the reference's own palette).
-tanh on the GPU and in numpy may differ in the last bit, which can move a value across
-a palette boundary: at most 0.1% of pixels may differ, by one palette step."""
+draw_wave_highres_palette / wave_value for every plot mode (amplitude, energy, mixed,
+mean, log, flux, total flux, average), with the running sums carried over frames.
+The palette is a seeded synthetic 256x3 byte table (the caller supplies the
+reference's own palette).  tanh, log and atan on the GPU and in numpy may differ in the
+last bit, which can move a value across a palette boundary: a few pixels (0.1-0.2%)
+may differ."""
 import numpy as np
 import pytest
 
@@ -37,3 +39,44 @@ def test_frame_matches_oracle(prec, coef, opts):
     assert img.shape == ref.shape
     diff = np.any(img != ref, axis=-1)
     assert diff.mean() <= 1e-3
+
+
+# chosen so that every mode gives a varied image on this scene (20 to 130 distinct colours)
+PLOT_KW = dict(slope=1.5, scale=40.0, log_shift=0.75, log_scale=0.25, flux_scale=3.0e4, avrg_e_factor=0.9)
+
+
+@pytest.mark.parametrize("plot", list(range(10)))
+@pytest.mark.parametrize("prec", [P.FP64, P.FP32])
+def test_frame_plot_modes_match_oracle(plot, prec):
+    """Every P_* mode of wave_value (wave_common.c:1053-1162) over four frames, so that
+    the running sums of the mean, average and total-flux modes accumulate."""
+    p, f, xy, _ = variant_inputs("s_abs", seed=5, smooth=True)
+    L = lut(2)
+    state = {}
+    with W.Scene(p, prec, P.COEF_TABLE) as s:
+        s.upload(f["phi"], f["psi"], xy, f["tcc"], f["tc"], f["tgamma"])
+        for t in range(4):
+            s.step(3)
+            img = s.frame_rgb8(L, size=1, plot=plot, time=t, **PLOT_KW)
+            phi, psi = s.download()
+            ref = oracle.frame_rgb8(p, phi, xy, L, size=1, plot=plot, psi=psi, state=state, time=t, **PLOT_KW)
+            diff = np.any(img != ref, axis=-1)
+            assert diff.sum() <= max(2, 2e-3 * diff.size), (plot, t, int(diff.sum()))
+
+
+def test_frame_reset_restarts_running_sums():
+    p, f, xy, _ = variant_inputs("s_abs", seed=5, smooth=True)
+    L = lut(3)
+    with W.Scene(p, P.FP64, P.COEF_TABLE) as s:
+        s.upload(f["phi"], f["psi"], xy, f["tcc"], f["tc"], f["tgamma"])
+        first = s.frame_rgb8(L, plot=P.P_MEAN_ENERGY, time=0, **PLOT_KW)
+        s.frame_rgb8(L, plot=P.P_MEAN_ENERGY, time=0, **PLOT_KW)  # the sum is now twice the energy
+        s.frame_reset()
+        again = s.frame_rgb8(L, plot=P.P_MEAN_ENERGY, time=0, **PLOT_KW)
+    assert np.array_equal(first, again)
+
+
+def test_server_refuses_non_amplitude_frames():
+    lut_ = lut(4)
+    with pytest.raises(W.WaveGpuError):
+        W.Server(lut_, precision=P.FP32, plot=P.P_ENERGY).close()

@@ -225,7 +225,7 @@ wg_status wg_scene_destroy(wg_scene *s)
     for (auto &f : s->f) if (f) cudaFree(f);
     for (auto &g : s->g) if (g) cudaFree(g);
     void *dev[] = {s->act, s->nz, s->tcc, s->tc, s->tg, s->nidx, s->nw, s->ebot, s->etop, s->eout, s->dcount,
-                   s->dstage, s->rgb, s->lut, s->bv_osc, s->bv_src, s->dflag};
+                   s->dstage, s->rgb, s->lut, s->bv_osc, s->bv_src, s->dflag, s->facc};
     for (void *d : dev) if (d) cudaFree(d);
     for (auto &c : s->skew) if (c.dev) cudaFree(c.dev);
     if (s->hout) cudaFreeHost(s->hout);

@@ -39,6 +39,9 @@ struct wg_scene {
     void *hstage = nullptr;
     size_t hstage_bytes = 0;
     uint8_t *rgb = nullptr, *lut = nullptr;
+    double *facc = nullptr;                  // frame running sums (mean, average, total flux)
+    size_t facc_n = 0;
+    int facc_plot = -1, facc_size = 0;
     size_t rgb_bytes = 0;
     int tb_k = 0, tile_i = 0, tile_j = 0;
     SkewPlanCache skew[WG_SKEW_MAX_K + 1];  // task lists of the skewed kernel, by depth

@@ -177,6 +177,7 @@ extern "C" {
 wg_status wg_server_create(const wg_server_config *cfg, void *stream, wg_server **out)
 {
     if (!cfg || !out) { set_error("NULL argument"); return WG_ERR_INVALID; }
+    if (cfg->frame.plot != WG_P_AMPLITUDE) { set_error("server frames are P_AMPLITUDE frames"); return WG_ERR_INVALID; }
     if (cfg->steps_per_frame < 1 || cfg->max_scenes < 1 || cfg->frame.size < 1 || !(cfg->frame.scale != 0.0)) {
         set_error("bad server configuration");
         return WG_ERR_INVALID;

@@ -86,13 +86,21 @@ NEUMANN_DTYPE = np.dtype([
 assert NEUMANN_DTYPE.itemsize == 64
 
 
+# plot modes of draw_wave_highres_palette (global_pdes.c:318-327; wg_frame_params.plot)
+(P_AMPLITUDE, P_ENERGY, P_MIXED, P_MEAN_ENERGY, P_LOG_ENERGY, P_LOG_MEAN_ENERGY, P_ENERGY_FLUX,
+ P_TOTAL_ENERGY_FLUX, P_AVERAGE_ENERGY, P_LOG_AVERAGE_ENERGY) = range(10)
+
+
 class WgFrameParams(ctypes.Structure):
     _fields_ = [
         ("size", ctypes.c_int32), ("fade", ctypes.c_int32),
         ("vshift", ctypes.c_double), ("vscale", ctypes.c_double),
         ("slope", ctypes.c_double), ("color_range", ctypes.c_double),
         ("scale", ctypes.c_double), ("fade_value", ctypes.c_double),
-        ("fade_in_obstacle", ctypes.c_int32), ("reserved", ctypes.c_int32),
+        ("fade_in_obstacle", ctypes.c_int32), ("plot", ctypes.c_int32),
+        ("log_shift", ctypes.c_double), ("log_scale", ctypes.c_double),
+        ("flux_scale", ctypes.c_double), ("avrg_e_factor", ctypes.c_double),
+        ("attenuation", ctypes.c_double), ("time", ctypes.c_int32), ("reserved", ctypes.c_int32),
     ]
 
 

@@ -78,6 +78,7 @@ SIGNATURES = {
     "wg_scene_launch_count": (_I32, [_V, ctypes.POINTER(_I64)]),
     "wg_scene_check_finite": (_I32, [_V, ctypes.POINTER(_I64)]),
     "wg_scene_frame_rgb8": (_I32, [_V, _V, _V, _V, _V]),
+    "wg_scene_frame_reset": (_I32, [_V]),
     "wg_scene_add_circular_wave": (_I32, [_V, _D, _D, _D, _D, _D, _D]),
     "wg_batch_create": (_I32, [_I32, _V, ctypes.POINTER(_V)]),
     "wg_batch_destroy": (_I32, [_V]),
@@ -328,15 +329,21 @@ class Scene:
         check(lib().wg_scene_launch_count(self.h, ctypes.byref(n)))
         return n.value
 
+    def frame_reset(self):
+        check(lib().wg_scene_frame_reset(self.h))
+
     def nonfinite(self):
         n = _I64()
         check(lib().wg_scene_check_finite(self.h, ctypes.byref(n)))
         return n.value
 
     def frame_rgb8(self, lut, size=2, vshift=-0.2, vscale=1.0, slope=1.0, color_range=0.8, scale=1.0,
-                   fade=False, fade_value=1.0, fade_in_obstacle=False):
+                   fade=False, fade_value=1.0, fade_in_obstacle=False, plot=P.P_AMPLITUDE, log_shift=0.75,
+                   log_scale=0.75, flux_scale=250.0, avrg_e_factor=0.95, attenuation=0.0, time=0):
+        """wg_scene_frame_rgb8; the keyword defaults are wave_billiard.c's macros."""
         fp = P.WgFrameParams(size, int(fade), vshift, vscale, slope, color_range, scale, fade_value,
-                             int(fade_in_obstacle), 0)
+                             int(fade_in_obstacle), int(plot), log_shift, log_scale, flux_scale, avrg_e_factor,
+                             attenuation, int(time), 0)
         lut = np.ascontiguousarray(lut, np.uint8).reshape(256, 3)
         out = np.zeros((self.params.ny // size, self.params.nx // size, 3), np.uint8)
         check(lib().wg_scene_frame_rgb8(self.h, ctypes.byref(fp), lut.ctypes.data, out.ctypes.data, None))
@@ -421,10 +428,11 @@ class Server:
     batch, one frame per tick for every resident scene, RGB8 frames to host memory."""
 
     def __init__(self, lut, precision=P.FP32, steps_per_frame=10, max_scenes=512, hbm_budget=150 << 30,
-                 size=2, vshift=-0.2, vscale=1.0, slope=1.0, color_range=0.8, scale=1.0, stream=None):
+                 size=2, vshift=-0.2, vscale=1.0, slope=1.0, color_range=0.8, scale=1.0, stream=None,
+                 plot=P.P_AMPLITUDE):
         cfg = P.WgServerConfig()
         cfg.precision, cfg.steps_per_frame, cfg.max_scenes, cfg.hbm_budget = precision, steps_per_frame, max_scenes, hbm_budget
-        cfg.frame = P.WgFrameParams(size, 0, vshift, vscale, slope, color_range, scale, 1.0, 0, 0)
+        cfg.frame = P.WgFrameParams(size, 0, vshift, vscale, slope, color_range, scale, 1.0, 0, int(plot))
         lut = np.ascontiguousarray(lut, np.uint8).reshape(-1)
         ctypes.memmove(cfg.lut, lut.ctypes.data, 768)
         h = ctypes.c_void_p()
