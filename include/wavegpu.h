@@ -173,6 +173,11 @@ wg_status wg_compute_energy_tblr(double **phi, double **psi, int16_t **xy_in,
 wg_status wg_dropin_add_circular_wave(double init_amp, double factor, double x, double y, double variance,
                                       double wavelength, double **phi, double **psi, int16_t **xy_in);
 
+/* phi[i][j] as the drop-in holds it: the resident device copy when `phi` is one of the
+ * resident arrays (one 8-byte read, no full sync; SAVE_TIME_SERIES sampling in
+ * animation(), wave_billiard.c:900-908), else the caller's own row. */
+wg_status wg_dropin_cell(double **phi, int32_t i, int32_t j, double *out);
+
 /* Energy diagnostics over device fields the caller owns, without any allocation.
  * No counterpart in the reference: it is for callers that cannot allocate device
  * memory at the time they need the diagnostics, e.g. a host program that carves all
@@ -280,6 +285,21 @@ wg_status wg_scene_frame_rgb8(wg_scene *s, const wg_frame_params *fp, const uint
 /* Restart the frame's running sums (the reference's total_energy, average_energy and
  * total_flux arrays) at zero. */
 wg_status wg_scene_frame_reset(wg_scene *s);
+/* RGB8 frame (row 0 at the bottom, width x height pixels) to a file: the uncompressed
+ * baseline TIFF of writetiff (sub_wave.c:62-122: 8-bit RGB, one row per strip,
+ * ORIENTATION_BOTLEFT, `description` as ImageDescription, scanline s = row
+ * height-1-s), or a binary PPM (P6, top row first).  Host-only; no GPU needed. */
+wg_status wg_write_tiff(const char *path, const char *description, const uint8_t *rgb, int32_t width,
+                        int32_t height);
+wg_status wg_write_ppm(const char *path, const uint8_t *rgb, int32_t width, int32_t height);
+/* SAVE_TIME_SERIES (wave_billiard.c:667-672, 900-908): record phi at n cells (i[k], j[k])
+ * after every update, room for `capacity` updates (n = 0 removes the probes).  While
+ * probes are set the scene takes single updates (no temporal blocking).  A step that
+ * would overflow the buffer is refused (WG_ERR_STATE) until the samples are read.
+ * wg_scene_read_probes copies the oldest min(count, max_updates) updates x n values
+ * (update-major) to `out` and drops them from the buffer. */
+wg_status wg_scene_set_probes(wg_scene *s, int32_t n, const int32_t *i, const int32_t *j, int32_t capacity);
+wg_status wg_scene_read_probes(wg_scene *s, double *out, int32_t max_updates, int32_t *count);
 /* add_circular_wave (wave_common.c:337-351) on the scene's phi (level t): the pulse of
  * wg_dropin_add_circular_wave, with the scene's mask and TWOSPEEDS.  Only the cells where
  * exp(-r^2/variance) is nonzero in double precision are visited. */

@@ -118,6 +118,16 @@ static void evolve_wave(double *phi[NX], double *psi[NX], double *tmp[NX], short
                    "evolve_wave");
 }
 
+/* phi[i][j] for SAVE_TIME_SERIES sampling (wave_billiard.c:900-908): with
+ * WAVEGPU_RESIDENT one cell of the device copy is read, without a full wavegpu_sync(). */
+static double wavegpu_cell(double *phi[NX], int i, int j)
+{
+    double v = 0.0;
+    wavegpu_ensure_();
+    wavegpu_check_(wg_dropin_cell(phi, i, j, &v), "wg_dropin_cell");
+    return v;
+}
+
 /* add_circular_wave (wave_common.c:337-351) on the GPU, with the program's INITIAL_AMP,
  * INITIAL_VARIANCE and INITIAL_WAVELENGTH.  With WAVEGPU_RESIDENT it adds the pulse to the
  * device copy of phi, so the periodic re-injection of animation() (wave_billiard.c:916-934)

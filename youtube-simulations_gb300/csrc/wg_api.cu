@@ -438,6 +438,26 @@ wg_status wg_dropin_add_circular_wave(double init_amp, double factor, double x, 
     return WG_OK;
 }
 
+wg_status wg_dropin_cell(double **phi, int32_t i, int32_t j, double *out)
+{
+    std::lock_guard<std::mutex> lk(g_di_mu);
+    wg_status s = di_require();
+    if (s) return s;
+    if (!phi || !out || i < 0 || j < 0 || i >= g_di.prm.nx || j >= g_di.prm.ny) { set_error("bad arguments"); return WG_ERR_INVALID; }
+    if (g_di.mode == WG_DROPIN_RESIDENT)
+        for (int k = 0; k < 3; k++)
+            if (g_di.host_rows[k] == phi) {
+                WG_CUDA(cudaMemcpyAsync(g_di.hout, g_di.buf[k] + (size_t)i * g_di.pitch + j, sizeof(double),
+                                        cudaMemcpyDeviceToHost, g_di.st));
+                WG_CUDA(cudaStreamSynchronize(g_di.st));
+                *out = g_di.hout[0];
+                return WG_OK;
+            }
+    if (!phi[i]) { set_error("row %d is NULL", i); return WG_ERR_INVALID; }
+    *out = phi[i][j];
+    return WG_OK;
+}
+
 wg_status wg_dropin_invalidate(void)
 {
     std::lock_guard<std::mutex> lk(g_di_mu);

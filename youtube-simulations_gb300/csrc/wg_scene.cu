@@ -112,8 +112,12 @@ static wg_status single_update(wg_scene *s)
 template <class T>
 wg_status scene_step_impl(wg_scene *s, int nsteps)
 {
+    if (s->probe_n && s->probe_count + nsteps > s->probe_cap) {
+        set_error("probe buffer full: %d of %d updates recorded; read them first", s->probe_count, s->probe_cap);
+        return WG_ERR_STATE;
+    }
     const int k = s->tb_k;
-    const bool tb = k > 1 && tb_supported(s);
+    const bool tb = k > 1 && tb_supported(s) && !s->probe_n;  // probes sample every update
     if (tb) {
         wg_status st = tb_prepare(s, nsteps);
         if (st) return st;
@@ -127,6 +131,7 @@ wg_status scene_step_impl(wg_scene *s, int nsteps)
         } else {
             wg_status st = single_update<T>(s);
             if (st) return st;
+            probe_record(s);
             nsteps--;
         }
     }
@@ -225,7 +230,7 @@ wg_status wg_scene_destroy(wg_scene *s)
     for (auto &f : s->f) if (f) cudaFree(f);
     for (auto &g : s->g) if (g) cudaFree(g);
     void *dev[] = {s->act, s->nz, s->tcc, s->tc, s->tg, s->nidx, s->nw, s->ebot, s->etop, s->eout, s->dcount,
-                   s->dstage, s->rgb, s->lut, s->bv_osc, s->bv_src, s->dflag, s->facc};
+                   s->dstage, s->rgb, s->lut, s->bv_osc, s->bv_src, s->dflag, s->facc, s->probe_cells, s->probe_buf};
     for (void *d : dev) if (d) cudaFree(d);
     for (auto &c : s->skew) if (c.dev) cudaFree(c.dev);
     if (s->hout) cudaFreeHost(s->hout);

@@ -39,6 +39,9 @@ struct wg_scene {
     void *hstage = nullptr;
     size_t hstage_bytes = 0;
     uint8_t *rgb = nullptr, *lut = nullptr;
+    int2 *probe_cells = nullptr;             // SAVE_TIME_SERIES probes: cells, samples [update][probe]
+    double *probe_buf = nullptr;
+    int probe_n = 0, probe_cap = 0, probe_count = 0;
     double *facc = nullptr;                  // frame running sums (mean, average, total flux)
     size_t facc_n = 0;
     int facc_plot = -1, facc_size = 0;
@@ -62,4 +65,5 @@ int tb_pass_depth(int k, int remaining);
 wg_status tb_prepare(wg_scene *s, int n);
 wg_status scene_check_flag(wg_scene *s);
 void autotune_scene(wg_scene *s);
+void probe_record(wg_scene *s);  // wg_io.cu: phi at the probes after an update
 }  // namespace wg

@@ -61,6 +61,7 @@ SIGNATURES = {
     "wg_compute_energy_tblr": (_I32, [_PP, _PP, _PP, _I32, _I32, _V]),
     "wg_compute_energy_device_noalloc": (_I32, [_V, _V, _V, _V, _I32, _I32, _I32, _V, _V]),
     "wg_dropin_add_circular_wave": (_I32, [_D, _D, _D, _D, _D, _D, _PP, _PP, _PP]),
+    "wg_dropin_cell": (_I32, [_PP, _I32, _I32, ctypes.POINTER(_D)]),
     "wg_scene_create": (_I32, [_V, _I32, _I32, _V, ctypes.POINTER(_V)]),
     "wg_scene_destroy": (_I32, [_V]),
     "wg_scene_bytes": (_I32, [_V, _I32, _I32, ctypes.POINTER(ctypes.c_size_t)]),
@@ -79,6 +80,10 @@ SIGNATURES = {
     "wg_scene_check_finite": (_I32, [_V, ctypes.POINTER(_I64)]),
     "wg_scene_frame_rgb8": (_I32, [_V, _V, _V, _V, _V]),
     "wg_scene_frame_reset": (_I32, [_V]),
+    "wg_write_tiff": (_I32, [ctypes.c_char_p, ctypes.c_char_p, _V, _I32, _I32]),
+    "wg_write_ppm": (_I32, [ctypes.c_char_p, _V, _I32, _I32]),
+    "wg_scene_set_probes": (_I32, [_V, _I32, _V, _V, _I32]),
+    "wg_scene_read_probes": (_I32, [_V, _V, _I32, ctypes.POINTER(_I32)]),
     "wg_scene_add_circular_wave": (_I32, [_V, _D, _D, _D, _D, _D, _D]),
     "wg_batch_create": (_I32, [_I32, _V, ctypes.POINTER(_V)]),
     "wg_batch_destroy": (_I32, [_V]),
@@ -216,6 +221,31 @@ def add_circular_wave(f, factor, x, y, init_amp=1.0, variance=0.0003, wavelength
                                             f.rows("xy")))
 
 
+def dropin_cell(f, i, j, a="phi"):
+    """wg_dropin_cell: phi[i][j] of a RowFields, from the resident device copy if there is one."""
+    v = _D()
+    check(lib().wg_dropin_cell(f.rows(a), int(i), int(j), ctypes.byref(v)))
+    return v.value
+
+
+def write_tiff(path, rgb, description=""):
+    """wg_write_tiff: an RGB8 frame [rows][cols][3] (row 0 at the bottom) as writetiff's TIFF."""
+    rgb = np.ascontiguousarray(rgb, np.uint8)
+    check(lib().wg_write_tiff(str(path).encode(), description.encode(), rgb.ctypes.data, rgb.shape[1], rgb.shape[0]))
+
+
+def write_ppm(path, rgb):
+    rgb = np.ascontiguousarray(rgb, np.uint8)
+    check(lib().wg_write_ppm(str(path).encode(), rgb.ctypes.data, rgb.shape[1], rgb.shape[0]))
+
+
+def write_time_series(path, values):
+    """Lines of SAVE_TIME_SERIES (wave_billiard.c:900-908): (long int)(v*1e16) as %019ld."""
+    with open(path, "w") as f:
+        for v in np.asarray(values, np.float64).reshape(-1):
+            f.write("%019d\n" % int(v * 1.0e16))
+
+
 def dropin_time():
     t = ctypes.c_int64()
     check(lib().wg_dropin_get_time(ctypes.byref(t)))
@@ -328,6 +358,23 @@ class Scene:
         n = _I64()
         check(lib().wg_scene_launch_count(self.h, ctypes.byref(n)))
         return n.value
+
+    def set_probes(self, cells, capacity):
+        """wg_scene_set_probes: record phi at cells [(i, j), ...] after every update."""
+        cells = np.asarray(cells, np.int32).reshape(-1, 2)
+        ii, jj = np.ascontiguousarray(cells[:, 0]), np.ascontiguousarray(cells[:, 1])
+        check(lib().wg_scene_set_probes(self.h, len(cells), ii.ctypes.data, jj.ctypes.data, int(capacity)))
+        self._nprobes, self._probe_cap = len(cells), int(capacity)
+
+    def read_probes(self, max_updates=None):
+        """The recorded samples [update][probe], oldest first (at most max_updates)."""
+        n = getattr(self, "_nprobes", 0)
+        if n == 0:
+            return np.zeros((0, 0))
+        c = _I32()
+        out = np.zeros((self._probe_cap if max_updates is None else min(max_updates, self._probe_cap), n))
+        check(lib().wg_scene_read_probes(self.h, out.ctypes.data, out.shape[0], ctypes.byref(c)))
+        return out[:c.value].copy()
 
     def frame_reset(self):
         check(lib().wg_scene_frame_reset(self.h))
