@@ -33,8 +33,9 @@ def case(name, nx=301, ny=None, seed=0):
         discs = scenes.seeded_discs(rng, 12, 0.05, 0.2)
         xy = scenes.mask(p, scenes.D_CIRCLES, circles=discs)
         inside = np.argwhere(xy.reshape(nx, ny) > 0)
-        si, sj = inside[len(inside) // 3]
-        p.src_on, p.src_i, p.src_j, p.src_amp, p.src_period = 1, int(si), int(sj), 0.05, 31.0
+        if len(inside):  # tiny grids may hold no disc cell: no source then
+            si, sj = inside[len(inside) // 3]
+            p.src_on, p.src_i, p.src_j, p.src_amp, p.src_period = 1, int(si), int(sj), 0.05, 31.0
     elif name == "abs_stadium":
         p = params_of("s_abs_mask", **over)
         xy = scenes.mask(p, scenes.D_STADIUM, lam=3.0)
@@ -101,3 +102,30 @@ def test_autotuned_blocking_and_launch_count():
         assert s.time == 41
     new, _, _, _ = oracle.run(p, f["phi"], f["psi"], f["tmp"], xy, f["tcc"], f["tc"], f["tgamma"], 41)
     assert rel_err(phi, new) <= 1e-5
+
+
+@pytest.mark.parametrize("nx,ny", [(3, 8), (5, 9), (9, 8), (17, 12), (20, 131), (64, 124)])
+@pytest.mark.parametrize("name", ["dir_kappa_floor", "abs_twospeeds_src"])
+def test_skewed_blocking_on_small_and_odd_grids(nx, ny, name):
+    """Grids where every task of the skewed pass takes the general rule (fewer than
+    2*8+1 rows), where one column tile holds both boundary columns, and odd widths."""
+    p, f, xy = case(name, nx=nx, ny=ny, seed=1)
+    n = 13
+    new, prev, _, _ = oracle.run(p, f["phi"], f["psi"], f["tmp"], xy, f["tcc"], f["tc"], f["tgamma"], n)
+    for k, L in [(2, 8), (3, 16), (6, 16)]:
+        with W.Scene(p, P.FP32, P.COEF_TABLE) as s:
+            s.upload(f["phi"], f["psi"], xy, f["tcc"], f["tc"], f["tgamma"])
+            s.set_blocking(k, L, 1)
+            s.step(n)
+            phi, psi = s.download()
+        assert rel_err(phi, new) <= 1e-5, (k, L)
+        assert rel_err(psi, prev) <= 1e-5, (k, L)
+
+
+def test_skewed_blocking_refuses_narrow_grids():
+    p, f, xy = case("dir_kappa_floor", nx=20, ny=7, seed=1)
+    with W.Scene(p, P.FP32, P.COEF_TABLE) as s:
+        s.upload(f["phi"], f["psi"], xy, f["tcc"], f["tc"], f["tgamma"])
+        s.set_blocking(3, 16, 1)
+        with pytest.raises(W.WaveGpuError):
+            s.step(6)
