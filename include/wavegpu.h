@@ -285,6 +285,18 @@ wg_status wg_scene_frame_rgb8(wg_scene *s, const wg_frame_params *fp, const uint
 /* Restart the frame's running sums (the reference's total_energy, average_energy and
  * total_flux arrays) at zero. */
 wg_status wg_scene_frame_reset(wg_scene *s);
+/* Mask and tables built on the device instead of wg_scene_upload's host arrays:
+ * xy_in_billiard_single_domain (sub_wave.c:5712-6252) at every cell centre for domain
+ * 0 rectangle, 1 ellipse, 2 stadium, 8 polygon (npoly, apoly), 20 discs, 201 discs in a
+ * rectangle (circles: ncircles x (xc, yc, radius), the reference's circles[]), and for
+ * WG_COEF_TABLE scenes the tables of init_ior_2d (sub_wave.c:12983-13002).  Then
+ * wg_scene_upload_state sets phi and psi.  Masks are 0/1; Neumann scenes are refused
+ * (their ghost cells and records come from the host).  The polygon's cos/sin are
+ * CUDA's: a cell within rounding of an edge may fall on the other side. */
+wg_status wg_scene_build_domain(wg_scene *s, int32_t domain, double lambda, int32_t npoly, double apoly,
+                                const double *circles, int32_t ncircles);
+/* The scene's mask as 0/1 (1 where xy != 0), [nx][ny]. */
+wg_status wg_scene_download_mask(wg_scene *s, int16_t *xy);
 /* RGB8 frame (row 0 at the bottom, width x height pixels) to a file: the uncompressed
  * baseline TIFF of writetiff (sub_wave.c:62-122: 8-bit RGB, one row per strip,
  * ORIENTATION_BOTLEFT, `description` as ImageDescription, scanline s = row

@@ -295,6 +295,7 @@ wg_status wg_scene_upload(wg_scene *s, const double *phi, const double *psi, con
     s->cur = 0;
     s->time = 0;
     s->uploaded = true;
+    s->has_mask = true;
     return WG_OK;
 }
 
@@ -304,6 +305,8 @@ wg_status wg_scene_upload_state(wg_scene *s, const void *phi, const void *psi, i
     const int nx = s->prm.nx, ny = s->prm.ny;
     void *dst[2] = {s->f[s->cur], s->f[1 - s->cur]};
     const void *src[2] = {phi, psi};
+    if (!s->has_mask) { set_error("upload or build the mask first"); return WG_ERR_STATE; }
+    s->uploaded = true;
     if (host_precision == s->prec) {
         // contiguous copies (faster over the host link than row-pitched ones) into the dense
         // stage, then a repack into the pitched fields on the device

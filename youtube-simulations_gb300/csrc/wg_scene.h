@@ -52,6 +52,7 @@ struct wg_scene {
     size_t bv_cap = 0;
     long long bv_t0 = 0;
     bool uploaded = false;
+    bool has_mask = false;  // by wg_scene_upload or wg_scene_build_domain
 };
 
 namespace wg {

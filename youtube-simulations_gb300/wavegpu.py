@@ -80,6 +80,8 @@ SIGNATURES = {
     "wg_scene_check_finite": (_I32, [_V, ctypes.POINTER(_I64)]),
     "wg_scene_frame_rgb8": (_I32, [_V, _V, _V, _V, _V]),
     "wg_scene_frame_reset": (_I32, [_V]),
+    "wg_scene_build_domain": (_I32, [_V, _I32, _D, _I32, _D, _V, _I32]),
+    "wg_scene_download_mask": (_I32, [_V, _V]),
     "wg_write_tiff": (_I32, [ctypes.c_char_p, ctypes.c_char_p, _V, _I32, _I32]),
     "wg_write_ppm": (_I32, [ctypes.c_char_p, _V, _I32, _I32]),
     "wg_scene_set_probes": (_I32, [_V, _I32, _V, _V, _I32]),
@@ -358,6 +360,17 @@ class Scene:
         n = _I64()
         check(lib().wg_scene_launch_count(self.h, ctypes.byref(n)))
         return n.value
+
+    def build_domain(self, domain, lam=1.8, npoly=6, apoly=0.0, circles=None):
+        """wg_scene_build_domain: the mask (and tables) on the device; then upload_state."""
+        c = np.zeros((0, 3)) if circles is None else np.ascontiguousarray(np.asarray(circles, np.float64)[:, :3])
+        check(lib().wg_scene_build_domain(self.h, int(domain), float(lam), int(npoly), float(apoly),
+                                          c.ctypes.data if len(c) else None, len(c)))
+
+    def download_mask(self):
+        xy = np.zeros(self.params.nx * self.params.ny, np.int16)
+        check(lib().wg_scene_download_mask(self.h, xy.ctypes.data))
+        return xy
 
     def set_probes(self, cells, capacity):
         """wg_scene_set_probes: record phi at cells [(i, j), ...] after every update."""
