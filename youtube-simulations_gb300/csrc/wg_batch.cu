@@ -10,7 +10,15 @@
 //
 // The per-cell arithmetic is the single-scene kernels' (k_step_bulk / fast_edge), so a
 // scene advanced in a batch is bit-identical to the same scene advanced alone.
+//
+// FP32 scenes with mirror ("Dirichlet") or absorbing boundaries take skewed passes
+// instead (k_batch_skew, wg_tb.cu): a frame of n updates is a few passes of 2..6 updates
+// each, at the depth class tuned for the scene's size class, writing between two buffer
+// pairs.  Each depth class runs as its own branch of the frame's graph, beside the chain
+// of single updates of the other scenes.  The skewed cells are the single-update cells
+// bit for bit, so a batch gives the same fields with and without skewed passes.
 #include <algorithm>
+#include <cmath>
 #include <cstring>
 #include <map>
 #include <vector>
@@ -108,13 +116,14 @@ __device__ __forceinline__ void batch_tile(const DevParams &p, const T *__restri
 // a device counter.  Each item's scene entry, first row, column tile and slot come from
 // one int4 of the item table built with the scene table.  The ticket of the following
 // item is taken while this one runs, and read after it, so its latency is hidden.
+// all = 0: only the items of scenes without skewed passes (the first plain_tiles).
 template <class T>
 __global__ void __launch_bounds__(256, 4) k_batch_step(const BatchHdr *__restrict__ hdr, const SlotDev *__restrict__ tab,
                                                     const int4 *__restrict__ items, SlotDyn *__restrict__ dyn,
-                                                    int *__restrict__ counter, int u)
+                                                    int *__restrict__ counter, int u, int all)
 {
     __shared__ int s_next[2];
-    const int total = hdr->total_tiles;
+    const int total = all ? hdr->total_tiles : hdr->plain_tiles;
     const int tid = threadIdx.y * blockDim.x + threadIdx.x;
     if (tid == 0) s_next[0] = atomicAdd(counter + u, 1);
     __syncthreads();
@@ -126,21 +135,29 @@ __global__ void __launch_bounds__(256, 4) k_batch_step(const BatchHdr *__restric
         const int4 w = items[it];
         const SlotDev &sd = tab[w.x];
         const SlotDyn d = dyn[w.w];
-        const int phase = (d.cur + u) & 1;
-        batch_tile<T>(sd.p, (const T *)sd.f[phase], (T *)sd.f[1 - phase], sd.act, sd.nz, w.y, w.z, d.time + u + 1);
+        const int phase = (d.cur + u) & 1, base = 2 * d.pair;
+        batch_tile<T>(sd.p, (const T *)sd.f[base + phase], (T *)sd.f[base + 1 - phase], sd.act, sd.nz, w.y, w.z,
+                      d.time + u + 1);
         if (tid == 0) s_next[buf ^ 1] = next;
         __syncthreads();  // the next ticket is visible; s_next[buf] is free again
     }
 }
 
+// skewed: the frame ran the skewed passes of the scenes with a depth class
 __global__ void k_batch_advance(const BatchHdr *__restrict__ hdr, const SlotDev *__restrict__ tab,
-                                SlotDyn *__restrict__ dyn, int n)
+                                SlotDyn *__restrict__ dyn, int n, int skewed)
 {
     const int k = blockIdx.x * blockDim.x + threadIdx.x;
     if (k >= hdr->nactive) return;
     SlotDyn &d = dyn[tab[k].slot];
     d.time += n;
-    d.cur = (d.cur + n) & 1;
+    const int P = skewed ? batch_passes(n, tab[k].skew_k) : 0;
+    if (P > 0) {
+        d.pair ^= P & 1;
+        d.cur = 0;
+    } else {
+        d.cur = (d.cur + n) & 1;
+    }
 }
 
 }  // namespace wg
@@ -151,41 +168,122 @@ namespace wg {
 
 static void batch_drop_graphs(wg_batch *b);
 
+static int entry_skew_k(const wg_batch *b, const BatchSlotHost &h)
+{
+    if (!h.skew || b->skew_mode == 0) return 0;
+    return b->skew_mode > 0 ? b->skew_mode : b->class_k[h.cls];
+}
+
+// Tasks of the pass depth d for the scenes of depth class K (table entries), largest first
+// so that the ticket order balances the warps; each scene gets a share of one wave of
+// resident warps in proportion to its cells.
+static void build_skew_tasks(const std::vector<const BatchSlotHost *> &hs, const std::vector<int> &entries, int d,
+                             std::vector<int4> &out)
+{
+    long long cells = 0;
+    for (const BatchSlotHost *h : hs) cells += (long long)h->prm.nx * h->prm.ny;
+    const int cap = batch_skew_capacity(d);
+    std::vector<int4> t;
+    std::vector<float> cost;
+    for (size_t k = 0; k < hs.size(); k++) {
+        const double share = cells > 0 ? (double)hs[k]->prm.nx * hs[k]->prm.ny / (double)cells : 1.0;
+        batch_skew_plan(hs[k]->dp, entries[k], d, std::max(1, (int)(cap * share + 0.5)), t, cost);
+    }
+    std::vector<int> ord(t.size());
+    for (size_t k = 0; k < ord.size(); k++) ord[k] = (int)k;
+    std::stable_sort(ord.begin(), ord.end(), [&](int x, int y) { return cost[x] > cost[y]; });
+    out.resize(t.size());
+    for (size_t k = 0; k < ord.size(); k++) out[k] = t[ord[k]];
+}
+
+// (re)build the task list of (depth class K, pass depth d) from the current table
+static wg_status build_list(wg_batch *b, int K, int d, const std::vector<int> &tab_slot)
+{
+    auto it = b->lists.find({K, d});
+    if (it == b->lists.end()) {
+        if ((int)b->lists.size() >= b->skew_n_cap - 1) { set_error("too many skewed task lists"); return WG_ERR_STATE; }
+        BatchSkewList L;
+        L.index = (int)b->lists.size();
+        it = b->lists.emplace(std::make_pair(K, d), L).first;
+    }
+    BatchSkewList &L = it->second;
+    std::vector<const BatchSlotHost *> hs;
+    std::vector<int> entries;
+    for (size_t e = 0; e < tab_slot.size(); e++) {
+        const BatchSlotHost &h = b->slots[tab_slot[e]];
+        if (entry_skew_k(b, h) == K) {
+            hs.push_back(&h);
+            entries.push_back((int)e);
+        }
+    }
+    std::vector<int4> tasks;
+    build_skew_tasks(hs, entries, d, tasks);
+    if ((int)tasks.size() > L.cap) {
+        if (L.dev) cudaFree(L.dev);
+        L.dev = nullptr;
+        const int cap = std::max(1024, (int)tasks.size() * 2);
+        WG_CUDA(cudaMalloc(&L.dev, sizeof(int4) * cap));
+        L.cap = cap;
+        batch_drop_graphs(b);  // the graphs hold the list pointer
+    }
+    L.n = (int)tasks.size();
+    if (L.n) WG_CUDA(cudaMemcpyAsync(L.dev, tasks.data(), sizeof(int4) * L.n, cudaMemcpyHostToDevice, b->st));
+    WG_CUDA(cudaMemcpyAsync(b->d_skew_n + L.index, &L.n, sizeof(int), cudaMemcpyHostToDevice, b->st));
+    WG_CUDA(cudaStreamSynchronize(b->st));  // the host vectors above go out of scope
+    return WG_OK;
+}
+
 wg_status batch_refresh_table(wg_batch *b)
 {
     constexpr int Vf = 4, Vd = 2;
     const int V = (b->prec == WG_FP32) ? Vf : Vd;
     std::vector<SlotDev> tab;
+    std::vector<int> tab_slot;
     std::vector<int4> items;
-    int base = 0;
+    int base = 0, plain = 0, nskew = 0;
     long long cells = 0;
-    for (int k = 0; k < (int)b->slots.size(); k++) {
-        const BatchSlotHost &h = b->slots[k];
-        if (!h.used) continue;
-        SlotDev d;
-        memset(&d, 0, sizeof d);
-        d.p = h.dp;
-        d.f[0] = h.f[0];
-        d.f[1] = h.f[1];
-        d.act = h.act;
-        d.nz = h.nz;
-        d.slot = k;
-        d.tiles_j = (h.dp.pitch / V + BT_THREADS - 1) / BT_THREADS;
-        const int tiles_i = (h.prm.nx + BT_ROWS - 1) / BT_ROWS;
-        d.ntiles = tiles_i * d.tiles_j;
-        d.tile_base = base;
-        base += d.ntiles;
-        for (int ti = 0; ti < tiles_i; ti++)
-            for (int tj = 0; tj < d.tiles_j; tj++) items.push_back(make_int4((int)tab.size(), ti * BT_ROWS, tj, k));
-        cells += (long long)h.prm.nx * h.prm.ny;
-        tab.push_back(d);
+    unsigned sig = 0;
+    // scenes without skewed passes first: their items are the first plain_tiles
+    for (int pass = 0; pass < 2; pass++) {
+        for (int k = 0; k < (int)b->slots.size(); k++) {
+            const BatchSlotHost &h = b->slots[k];
+            if (!h.used) continue;
+            const int sk = entry_skew_k(b, h);
+            if ((sk > 0) != (pass == 1)) continue;
+            SlotDev d;
+            memset(&d, 0, sizeof d);
+            d.p = h.dp;
+            for (int q = 0; q < 4; q++) d.f[q] = h.f[q];
+            d.act = h.act;
+            d.nz = h.nz;
+            d.slot = k;
+            d.skew_k = sk;
+            d.tiles_j = (h.dp.pitch / V + BT_THREADS - 1) / BT_THREADS;
+            const int tiles_i = (h.prm.nx + BT_ROWS - 1) / BT_ROWS;
+            d.ntiles = tiles_i * d.tiles_j;
+            d.tile_base = base;
+            base += d.ntiles;
+            for (int ti = 0; ti < tiles_i; ti++)
+                for (int tj = 0; tj < d.tiles_j; tj++) items.push_back(make_int4((int)tab.size(), ti * BT_ROWS, tj, k));
+            cells += (long long)h.prm.nx * h.prm.ny;
+            if (sk > 0) {
+                sig |= 1u << sk;
+                nskew++;
+            } else {
+                plain = base;
+            }
+            tab.push_back(d);
+            tab_slot.push_back(k);
+        }
     }
+    if (plain > 0) sig |= 1u;
     if ((int)tab.size() > b->tab_cap) {
         if (b->d_tab) cudaFree(b->d_tab);
         b->d_tab = nullptr;
         const int cap = std::max(64, (int)tab.size() * 2);
         WG_CUDA(cudaMalloc(&b->d_tab, sizeof(SlotDev) * cap));
         b->tab_cap = cap;
+        batch_drop_graphs(b);  // the graphs hold the table pointer and size the advance launch by it
     }
     if ((int)items.size() > b->items_cap) {
         if (b->d_items) cudaFree(b->d_items);
@@ -195,16 +293,29 @@ wg_status batch_refresh_table(wg_batch *b)
         b->items_cap = cap;
         batch_drop_graphs(b);  // the graphs hold the item-table pointer
     }
-    // the graphs hold the table pointer: a reallocation invalidates them
+    if (sig != b->graph_sig) {  // another set of branches: the graphs are recorded again
+        batch_drop_graphs(b);
+        b->graph_sig = sig;
+    }
     if (!tab.empty()) {
         WG_CUDA(cudaMemcpyAsync(b->d_tab, tab.data(), sizeof(SlotDev) * tab.size(), cudaMemcpyHostToDevice, b->st));
         WG_CUDA(cudaMemcpyAsync(b->d_items, items.data(), sizeof(int4) * items.size(), cudaMemcpyHostToDevice, b->st));
     }
-    BatchHdr h{(int)tab.size(), base};
+    BatchHdr h{(int)tab.size(), base, plain, 0};
     WG_CUDA(cudaMemcpyAsync(b->d_hdr, &h, sizeof h, cudaMemcpyHostToDevice, b->st));
     WG_CUDA(cudaStreamSynchronize(b->st));
     b->nactive = (int)tab.size();
     b->total_cells = cells;
+    b->plain_tiles = plain;
+    b->skew_scenes = nskew;
+    b->tab_slot = tab_slot;
+    // the task lists in use follow the new table
+    std::vector<std::pair<int, int>> keys;
+    for (auto &kv : b->lists) keys.push_back(kv.first);
+    for (auto &key : keys) {
+        wg_status st = build_list(b, key.first, key.second, tab_slot);
+        if (st) return st;
+    }
     return WG_OK;
 }
 
@@ -214,15 +325,157 @@ static void batch_drop_graphs(wg_batch *b)
     b->graphs.clear();
 }
 
+// depth classes present in the table (bits 2..6 of graph_sig)
+static std::vector<int> batch_groups(const wg_batch *b)
+{
+    std::vector<int> g;
+    for (int K = 2; K <= WG_SKEW_MAX_K; K++)
+        if (b->graph_sig & (1u << K)) g.push_back(K);
+    return g;
+}
+
+// Everything a frame of n updates needs before it is recorded: counters, tickets, the
+// task lists of its passes, the branches' streams and events, the kernels' attributes.
+static wg_status batch_prepare_frame(wg_batch *b, int n, bool skewed)
+{
+    if (n > b->counter_cap) {
+        if (b->d_counter) cudaFree(b->d_counter);
+        b->d_counter = nullptr;
+        WG_CUDA(cudaMalloc(&b->d_counter, sizeof(int) * n));
+        b->counter_cap = n;
+        batch_drop_graphs(b);
+    }
+    if (!skewed) return WG_OK;
+    int tickets = 0;
+    for (int K : batch_groups(b)) {
+        const int P = batch_passes(n, K);
+        tickets += P;
+        for (int q = 0; q < P; q++) {
+            const int d = batch_pass_depth(n, P, q);
+            batch_skew_capacity(d);  // sets the kernel's shared-memory attribute outside the capture
+            if (!b->lists.count({K, d})) {
+                wg_status st = build_list(b, K, d, b->tab_slot);
+                if (st) return st;
+            }
+        }
+    }
+    if (tickets > b->ticket_cap) {
+        if (b->d_ticket) cudaFree(b->d_ticket);
+        b->d_ticket = nullptr;
+        const int cap = std::max(64, tickets * 2);
+        WG_CUDA(cudaMalloc(&b->d_ticket, sizeof(int) * cap));
+        b->ticket_cap = cap;
+        batch_drop_graphs(b);
+    }
+    for (int K : batch_groups(b)) {
+        if (!b->side[K]) WG_CUDA(cudaStreamCreateWithFlags(&b->side[K], cudaStreamNonBlocking));
+        if (!b->ev_join[K]) WG_CUDA(cudaEventCreateWithFlags(&b->ev_join[K], cudaEventDisableTiming));
+    }
+    if (!b->ev_fork) WG_CUDA(cudaEventCreateWithFlags(&b->ev_fork, cudaEventDisableTiming));
+    return WG_OK;
+}
+
 template <class T>
-static void batch_enqueue_frame(wg_batch *b, int n)
+static void batch_enqueue_frame(wg_batch *b, int n, bool skewed)
 {
     cudaMemsetAsync(b->d_counter, 0, sizeof(int) * n, b->st);
-    dim3 blk(BT_THREADS, 4);
-    for (int u = 0; u < n; u++)
-        k_batch_step<T><<<b->persistent_blocks, blk, 0, b->st>>>(b->d_hdr, b->d_tab, b->d_items, b->d_dyn, b->d_counter, u);
+    std::vector<int> groups;
+    if (skewed) {
+        groups = batch_groups(b);
+        int tickets = 0;
+        for (int K : groups) tickets += batch_passes(n, K);
+        cudaMemsetAsync(b->d_ticket, 0, sizeof(int) * tickets, b->st);
+        cudaEventRecord(b->ev_fork, b->st);
+        int ti = 0;
+        for (int K : groups) {  // one branch per depth class
+            cudaStream_t ss = b->side[K];
+            cudaStreamWaitEvent(ss, b->ev_fork, 0);
+            const int P = batch_passes(n, K);
+            int toff = 0;
+            for (int q = 0; q < P; q++) {
+                const int d = batch_pass_depth(n, P, q);
+                const BatchSkewList &L = b->lists.at({K, d});
+                launch_batch_skew(d, b->d_tab, b->d_dyn, L.dev, b->d_skew_n + L.index, b->d_ticket + ti++, q, toff, ss);
+                toff += d;
+            }
+            cudaEventRecord(b->ev_join[K], ss);
+        }
+    }
+    if (!skewed || (b->graph_sig & 1u)) {  // the chain of single updates
+        dim3 blk(BT_THREADS, 4);
+        for (int u = 0; u < n; u++)
+            k_batch_step<T><<<b->persistent_blocks, blk, 0, b->st>>>(b->d_hdr, b->d_tab, b->d_items, b->d_dyn,
+                                                                     b->d_counter, u, skewed ? 0 : 1);
+    }
+    for (int K : groups) cudaStreamWaitEvent(b->st, b->ev_join[K], 0);
     const int cap = std::max(b->tab_cap, 1);
-    k_batch_advance<<<(cap + 255) / 256, 256, 0, b->st>>>(b->d_hdr, b->d_tab, b->d_dyn, n);
+    k_batch_advance<<<(cap + 255) / 256, 256, 0, b->st>>>(b->d_hdr, b->d_tab, b->d_dyn, n, skewed ? 1 : 0);
+}
+
+// Depth per size class: each candidate depth times one skewed pass over the class's
+// scenes (reading their current fields, writing the other pair, so the state does not
+// change) and the fastest per update is kept.
+static wg_status batch_autotune(wg_batch *b)
+{
+    bool tuned = false;
+    for (int c = 0; c < BATCH_CLASSES; c++) {
+        if (b->class_k[c]) continue;
+        std::vector<const BatchSlotHost *> hs;
+        std::vector<int> entries;
+        for (size_t e = 0; e < b->tab_slot.size(); e++) {
+            const BatchSlotHost &h = b->slots[b->tab_slot[e]];
+            if (h.skew && h.cls == c) {
+                hs.push_back(&h);
+                entries.push_back((int)e);
+            }
+        }
+        if (hs.empty()) continue;
+        if (b->tune_ms.empty()) b->tune_ms.assign(BATCH_CLASSES * 8, 0.0);
+        cudaEvent_t e0, e1;
+        WG_CUDA(cudaEventCreate(&e0));
+        WG_CUDA(cudaEventCreate(&e1));
+        int best = 0;
+        double best_ms = 1e30;
+        int4 *dev = nullptr;
+        cudaError_t err = cudaSuccess;
+        for (int K = 2; K <= WG_SKEW_MAX_K && err == cudaSuccess; K++) {
+            std::vector<int4> tasks;
+            build_skew_tasks(hs, entries, K, tasks);
+            const int nt = (int)tasks.size();
+            err = cudaMallocAsync((void **)&dev, sizeof(int4) * std::max(nt, 1), b->st);
+            if (err == cudaSuccess && nt) err = cudaMemcpyAsync(dev, tasks.data(), sizeof(int4) * nt, cudaMemcpyHostToDevice, b->st);
+            const int idx = b->skew_n_cap - 1;  // the count slot kept for tuning
+            if (err == cudaSuccess) err = cudaMemcpyAsync(b->d_skew_n + idx, &nt, sizeof(int), cudaMemcpyHostToDevice, b->st);
+            const int reps = 2;
+            for (int r = 0; r <= reps && err == cudaSuccess; r++) {
+                if (r == 1) cudaEventRecord(e0, b->st);
+                cudaMemsetAsync(b->d_tune_ticket + r, 0, sizeof(int), b->st);
+                launch_batch_skew(K, b->d_tab, b->d_dyn, dev, b->d_skew_n + idx, b->d_tune_ticket + r, 0, 0, b->st);
+                b->launches++;
+                err = cudaGetLastError();
+            }
+            if (err == cudaSuccess) err = cudaEventRecord(e1, b->st);
+            if (err == cudaSuccess) err = cudaEventSynchronize(e1);
+            float ms = 0.f;
+            if (err == cudaSuccess) err = cudaEventElapsedTime(&ms, e0, e1);
+            if (dev) cudaFreeAsync(dev, b->st);
+            dev = nullptr;
+            if (err == cudaSuccess) err = cudaStreamSynchronize(b->st);  // tasks outlives its copy
+            const double per = ms / (reps * K);
+            b->tune_ms[c * 8 + K] = per;
+            if (per < best_ms) {
+                best_ms = per;
+                best = K;
+            }
+        }
+        cudaEventDestroy(e0);
+        cudaEventDestroy(e1);
+        if (err != cudaSuccess) return cuda_fail(err, "batch autotune");
+        b->class_k[c] = best;
+        tuned = true;
+    }
+    if (tuned) return batch_refresh_table(b);
+    return WG_OK;
 }
 
 }  // namespace wg
@@ -252,6 +505,10 @@ wg_status wg_batch_create(int32_t precision, void *stream, wg_batch **out)
                 ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_batch_step<float>, BT_THREADS * 4, 0)
                 : cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_batch_step<double>, BT_THREADS * 4, 0);
     if (e == cudaSuccess) e = cudaHostAlloc(&b->h_out, 16 * sizeof(double), cudaHostAllocDefault);
+    b->skew_n_cap = 32;
+    if (e == cudaSuccess) e = cudaMalloc(&b->d_skew_n, sizeof(int) * b->skew_n_cap);
+    if (e == cudaSuccess) e = cudaMemsetAsync(b->d_skew_n, 0, sizeof(int) * b->skew_n_cap, b->st);
+    if (e == cudaSuccess) e = cudaMalloc(&b->d_tune_ticket, sizeof(int) * 4);
     if (e != cudaSuccess) {
         wg_status r = cuda_fail(e, "wg_batch_create");
         wg_batch_destroy(b);
@@ -269,11 +526,17 @@ wg_status wg_batch_destroy(wg_batch *b)
     batch_drop_graphs(b);
     for (auto &h : b->slots) {
         if (!h.used) continue;
-        void *ptrs[] = {h.f[0], h.f[1], h.act, h.nz, h.ebot, h.etop, h.eout};
+        void *ptrs[] = {h.f[0], h.f[1], h.f[2], h.f[3], h.act, h.nz, h.ebot, h.etop, h.eout};
         for (void *p : ptrs) if (p) cudaFree(p);
     }
-    void *ptrs[] = {b->d_tab, b->d_dyn, b->d_hdr, b->d_counter, b->d_items};
+    for (auto &kv : b->lists) if (kv.second.dev) cudaFree(kv.second.dev);
+    void *ptrs[] = {b->d_tab, b->d_dyn, b->d_hdr, b->d_counter, b->d_items, b->d_skew_n, b->d_ticket, b->d_tune_ticket};
     for (void *p : ptrs) if (p) cudaFree(p);
+    for (int k = 0; k < BATCH_GROUPS; k++) {
+        if (b->side[k]) cudaStreamDestroy(b->side[k]);
+        if (b->ev_join[k]) cudaEventDestroy(b->ev_join[k]);
+    }
+    if (b->ev_fork) cudaEventDestroy(b->ev_fork);
     if (b->h_out) cudaFreeHost(b->h_out);
     if (b->own_stream && b->st) cudaStreamDestroy(b->st);
     delete b;
@@ -298,9 +561,16 @@ wg_status wg_batch_add(wg_batch *b, const wg_params *p, const double *phi, const
     h.prm = *p;
     const int pitch = pitch_for(p->ny, (int)b->esz);
     h.dp = make_dev_params(*p, pitch);
+    h.skew = batch_skew_ok(*p, b->prec);
+    {
+        const double cells = (double)p->nx * p->ny;
+        h.cls = std::min(BATCH_CLASSES - 1, std::max(0, (int)std::floor(std::log2(cells)) - 10));
+    }
     const size_t fb = (size_t)p->nx * pitch * b->esz, mb = (size_t)p->nx * h.dp.wpitch * 4;
     cudaError_t e = cudaSuccess;
-    for (int q = 0; q < 2 && e == cudaSuccess; q++) e = cudaMallocAsync(&h.f[q], fb, b->st);
+    const int nf = h.skew ? 4 : 2;  // the second pair takes the skewed passes' output
+    for (int q = 0; q < nf && e == cudaSuccess; q++) e = cudaMallocAsync(&h.f[q], fb, b->st);
+    for (int q = 2; q < nf && e == cudaSuccess; q++) e = cudaMemsetAsync(h.f[q], 0, fb, b->st);
     if (e == cudaSuccess) e = cudaMallocAsync((void **)&h.act, mb, b->st);
     if (e == cudaSuccess) e = cudaMallocAsync((void **)&h.nz, mb, b->st);
     if (e == cudaSuccess) e = cudaMallocAsync((void **)&h.ebot, p->nx * sizeof(double2), b->st);
@@ -309,12 +579,12 @@ wg_status wg_batch_add(wg_batch *b, const wg_params *p, const double *phi, const
     void *stage = nullptr;
     if (e == cudaSuccess) e = cudaMallocAsync(&stage, n * sizeof(double), b->st);
     if (e != cudaSuccess) {
-        void *ptrs[] = {h.f[0], h.f[1], h.act, h.nz, h.ebot, h.etop, h.eout, stage};
+        void *ptrs[] = {h.f[0], h.f[1], h.f[2], h.f[3], h.act, h.nz, h.ebot, h.etop, h.eout, stage};
         for (void *q : ptrs) if (q) cudaFreeAsync(q, b->st);
         h = BatchSlotHost();
         return cuda_fail(e, "wg_batch_add");
     }
-    h.bytes = 2 * fb + 2 * mb;
+    h.bytes = nf * fb + 2 * mb;
     // mask planes, then the two fields (FP64 host values rounded on the device)
     WG_CUDA(cudaMemcpyAsync(stage, xy, n * sizeof(int16_t), cudaMemcpyHostToDevice, b->st));
     launch_pack_mask(p->nx, p->ny, h.dp.wpitch, (const int16_t *)stage, h.act, h.nz, b->st);
@@ -360,7 +630,7 @@ wg_status wg_batch_remove(wg_batch *b, int32_t slot)
     BatchSlotHost &h = b->slots[slot];
     h.used = false;
     wg_status st = batch_refresh_table(b);  // the kernels stop seeing the slot first
-    void *ptrs[] = {h.f[0], h.f[1], h.act, h.nz, h.ebot, h.etop, h.eout};
+    void *ptrs[] = {h.f[0], h.f[1], h.f[2], h.f[3], h.act, h.nz, h.ebot, h.etop, h.eout};
     for (void *p : ptrs) if (p) WG_CUDA(cudaFreeAsync(p, b->st));
     h = BatchSlotHost();
     return st;
@@ -370,19 +640,16 @@ wg_status wg_batch_step(wg_batch *b, int32_t nsteps)
 {
     if (!b || nsteps < 0) { set_error("bad arguments"); return WG_ERR_INVALID; }
     if (nsteps == 0 || b->nactive == 0) return WG_OK;
-    if (nsteps > b->counter_cap) {
-        if (b->d_counter) cudaFree(b->d_counter);
-        b->d_counter = nullptr;
-        WG_CUDA(cudaMalloc(&b->d_counter, sizeof(int) * nsteps));
-        b->counter_cap = nsteps;
-        batch_drop_graphs(b);
-    }
+    wg_status st;
+    if (b->prec == WG_FP32 && b->skew_mode < 0 && nsteps >= 2 && (st = batch_autotune(b))) return st;
+    const bool skewed = b->prec == WG_FP32 && nsteps >= 2 && b->skew_scenes > 0;
+    if ((st = batch_prepare_frame(b, nsteps, skewed))) return st;
     auto it = b->graphs.find(nsteps);
     if (it == b->graphs.end()) {
         cudaGraph_t g;
         WG_CUDA(cudaStreamBeginCapture(b->st, cudaStreamCaptureModeThreadLocal));
-        if (b->prec == WG_FP32) batch_enqueue_frame<float>(b, nsteps);
-        else batch_enqueue_frame<double>(b, nsteps);
+        if (b->prec == WG_FP32) batch_enqueue_frame<float>(b, nsteps, skewed);
+        else batch_enqueue_frame<double>(b, nsteps, skewed);
         WG_CUDA(cudaStreamEndCapture(b->st, &g));
         cudaGraphExec_t ge;
         cudaError_t e = cudaGraphInstantiate(&ge, g, 0);
@@ -391,7 +658,36 @@ wg_status wg_batch_step(wg_batch *b, int32_t nsteps)
         it = b->graphs.emplace(nsteps, ge).first;
     }
     WG_CUDA(cudaGraphLaunch(it->second, b->st));
-    b->launches += nsteps + 1;
+    long long n = 1;  // the advance kernel
+    if (!skewed || (b->graph_sig & 1u)) n += nsteps;
+    if (skewed)
+        for (int K : batch_groups(b)) n += batch_passes(nsteps, K);
+    b->launches += n;
+    return WG_OK;
+}
+
+wg_status wg_batch_set_skew(wg_batch *b, int32_t mode)
+{
+    if (!b) { set_error("NULL batch"); return WG_ERR_INVALID; }
+    if (!(mode == -1 || mode == 0 || (mode >= 2 && mode <= WG_SKEW_MAX_K))) {
+        set_error("skewed depth %d: -1 (tuned per size class), 0 (off) or 2..%d", mode, WG_SKEW_MAX_K);
+        return WG_ERR_INVALID;
+    }
+    WG_CUDA(cudaStreamSynchronize(b->st));
+    b->skew_mode = mode;
+    batch_drop_graphs(b);
+    return batch_refresh_table(b);
+}
+
+wg_status wg_batch_skew_depths(wg_batch *b, int32_t *depths, double *ms_per_update)
+{
+    if (!b || !depths) { set_error("NULL argument"); return WG_ERR_INVALID; }
+    for (int c = 0; c < BATCH_CLASSES; c++) {
+        depths[c] = b->skew_mode >= 0 ? b->skew_mode : b->class_k[c];
+        if (ms_per_update)
+            for (int K = 0; K < 8; K++)
+                ms_per_update[c * 8 + K] = b->tune_ms.empty() ? 0.0 : b->tune_ms[c * 8 + K];
+    }
     return WG_OK;
 }
 
@@ -411,7 +707,7 @@ wg_status wg_batch_download(wg_batch *b, int32_t slot, double *phi, double *psi)
     double *dst[2] = {phi, psi};
     for (int q = 0; q < 2; q++) {
         if (!dst[q]) continue;
-        const void *src = h.f[q == 0 ? d.cur : 1 - d.cur];
+        const void *src = h.f[2 * d.pair + (q == 0 ? d.cur : 1 - d.cur)];
         if (b->prec == WG_FP32) launch_convert_out<float>(h.prm.nx, h.prm.ny, h.dp.pitch, (const float *)src, stage, b->st);
         else launch_convert_out<double>(h.prm.nx, h.prm.ny, h.dp.pitch, (const double *)src, stage, b->st);
         WG_CUDA(cudaMemcpyAsync(dst[q], stage, n * sizeof(double), cudaMemcpyDeviceToHost, b->st));
@@ -431,7 +727,7 @@ wg_status wg_batch_energy(wg_batch *b, int32_t slot, double *total)
     SlotDyn d;
     WG_CUDA(cudaMemcpyAsync(&d, b->d_dyn + slot, sizeof d, cudaMemcpyDeviceToHost, b->st));
     WG_CUDA(cudaStreamSynchronize(b->st));
-    const void *phi = h.f[d.cur], *psi = h.f[1 - d.cur];
+    const void *phi = h.f[2 * d.pair + d.cur], *psi = h.f[2 * d.pair + 1 - d.cur];
     if (b->prec == WG_FP32)
         launch_energy<float>(h.dp, (const float *)phi, (const float *)psi, nullptr, h.nz, h.ebot, h.etop, 0, 0, h.eout, b->st);
     else

@@ -3,6 +3,7 @@
 #include <map>
 #include <vector>
 #include "wg_internal.h"
+#include "wg_scene.h"
 
 namespace wg {
 
@@ -11,19 +12,45 @@ constexpr int BT_THREADS = 64;   // threads along j per tile row (x V cells)
 
 struct __align__(16) SlotDev {   // one entry of the compact table of active scenes
     DevParams p;
-    void *f[2];                  // the two field buffers; dyn.cur says which holds phi
+    void *f[4];                  // pair 0: f[0], f[1]; pair 1 (skewed scenes): f[2], f[3]
     uint32_t *act, *nz;
     int slot;                    // index into the per-slot dynamic state
     int tiles_j, tile_base, ntiles;
+    int skew_k;                  // depth class of the scene's skewed passes; 0: single updates only
+    int pad_[3];
 };
 struct SlotDyn {
     long long time;
-    int cur;
-    int pad;
+    int cur;                     // phi = f[2 pair + cur], psi = f[2 pair + 1 - cur]
+    int pair;
 };
 struct BatchHdr {
-    int nactive, total_tiles;
+    int nactive, total_tiles;    // all work items
+    int plain_tiles, pad_;       // items of the scenes without skewed passes (they come first)
 };
+
+constexpr int BATCH_CLASSES = 16;   // size classes: floor(log2(cells)) - 10, clamped to 0..15
+constexpr int BATCH_GROUPS = WG_SKEW_MAX_K + 1;
+
+// Skewed passes of a frame of n updates with depth class K: P passes of n/P or n/P+1
+// updates (2..6 each); 0 when n < 2.
+__host__ __device__ inline int batch_passes(int n, int K)
+{
+    if (K < 2 || n < 2) return 0;
+    int P = (n + K - 1) / K;
+    if (n < 2 * P) P = n / 2;
+    return P;
+}
+__host__ __device__ inline int batch_pass_depth(int n, int P, int q) { return n / P + (q < n % P ? 1 : 0); }
+
+// Skewed passes over many scenes (wg_tb.cu): persistent warps take tasks (table entry,
+// first column of the 128-column tile, rows i_s | i_e << 16, kind) from a ticket counter;
+// pass q of a frame reads the pair the previous pass wrote, toff updates after the frame start.
+int batch_skew_capacity(int K);
+void batch_skew_plan(const DevParams &p, int entry, int K, int cap, std::vector<int4> &tasks, std::vector<float> &cost);
+void launch_batch_skew(int K, const SlotDev *tab, const SlotDyn *dyn, const int4 *tasks, const int *ntasks, int *ticket,
+                       int q, int toff, cudaStream_t st);
+bool batch_skew_ok(const wg_params &p, int prec);
 
 wg_status batch_refresh_table(::wg_batch *b);
 
@@ -33,11 +60,18 @@ struct BatchSlotHost {
     bool used = false;
     wg_params prm;
     wg::DevParams dp;
-    void *f[2] = {nullptr, nullptr};
+    void *f[4] = {nullptr, nullptr, nullptr, nullptr};  // f[2], f[3]: second pair of skewed scenes
     uint32_t *act = nullptr, *nz = nullptr;
     double2 *ebot = nullptr, *etop = nullptr;
     double *eout = nullptr;
     size_t bytes = 0;
+    bool skew = false;      // FP32 scene whose boundaries the skewed passes cover
+    int cls = 0;            // size class
+};
+
+struct BatchSkewList {      // tasks of one pass depth for one depth class
+    int4 *dev = nullptr;
+    int cap = 0, n = 0, index = 0;  // index: its count in d_skew_n
 };
 
 struct wg_batch {
@@ -61,5 +95,17 @@ struct wg_batch {
     int persistent_blocks = 0;
     std::map<int, cudaGraphExec_t> graphs;  // one per frame length
     double *h_out = nullptr;
+    // skewed passes
+    int skew_mode = -1;                                   // -1 autotuned per size class, 0 off, 2..6 fixed
+    int class_k[wg::BATCH_CLASSES] = {0};                 // tuned depth per size class (0: not yet)
+    std::map<std::pair<int, int>, BatchSkewList> lists;   // (depth class, pass depth) -> tasks
+    int *d_skew_n = nullptr, *d_ticket = nullptr;        // task counts; tickets of a frame's passes
+    int skew_n_cap = 0, ticket_cap = 0;
+    cudaStream_t side[wg::BATCH_GROUPS] = {};             // one branch per depth class in a frame
+    cudaEvent_t ev_fork = nullptr, ev_join[wg::BATCH_GROUPS] = {};
+    unsigned graph_sig = 0;                               // depth classes present (bit K), plain chain (bit 0)
+    int plain_tiles = 0, skew_scenes = 0;
+    std::vector<int> tab_slot;                            // slot of each table entry
+    int *d_tune_ticket = nullptr;                         // tickets of the autotuner's passes
+    std::vector<double> tune_ms;                          // last autotune: ms per update, [class * 8 + K]
 };
-

@@ -67,11 +67,59 @@ __device__ __forceinline__ void vstore(T *ptr, const T (&v)[Vec<T>::n])
     *reinterpret_cast<typename Vec<T>::type *>(ptr) = t;
 }
 
+// FP32 boundary-line cell of a mirror or absorbing scene by edge32 (the rule of the
+// tiled and skewed FP32 steppers), neighbours read from the current level.
+template <int COEF>
+__device__ inline float fast_edge32(const DevParams &p, const FastArgs<float> &a, int i, int j, long long time, float y)
+{
+    const size_t o = (size_t)i * p.pitch + j;
+    const float x = a.phi[o];
+    const float n = (i + 1 < p.nx) ? a.phi[o + p.pitch] : x;
+    const float sv = (i > 0) ? a.phi[o - p.pitch] : x;
+    const float e = (j + 1 < p.ny) ? a.phi[o + 1] : x;
+    const float w = (j > 0) ? a.phi[o - 1] : x;
+    const bool act = ActBits{a.act, p.wpitch}(i, j);
+    float ccv, tcv, g;
+    if (COEF == WG_COEF_TABLE) {
+        ccv = a.tcc[o];
+        tcv = a.tc ? a.tc[o] : 0.f;
+        g = a.tg ? a.tg[o] : a.gamf;
+    } else {
+        ccv = act ? a.c2f : a.c2bf;
+        tcv = act ? (float)p.courant : (float)p.courantb;
+        g = act ? a.gamf : a.gambf;
+    }
+    const Edge32K k{a.kappaf, (float)p.kappa_sides, (float)p.kappa_topbot, (float)p.gamma_sides,
+                    (float)p.gamma_topbot, (float)p.vmax};
+    float v = edge32<false>(p, i, j, x, y, n, sv, e, w, ccv, tcv, g, act, k,
+                            [&] { return (float)osc_bc(p, (int)time, j); });
+    if (p.floor_clamp && ActBits{a.nz, p.wpitch}(i, j)) v = (float)floor_clamp(p, (double)v);
+    return v;
+}
+
+template <class T, int COEF> struct Edge32Path {
+    static __device__ __forceinline__ bool run(const DevParams &, const FastArgs<T> &, int, int, long long, T, T *)
+    {
+        return false;
+    }
+};
+template <int COEF> struct Edge32Path<float, COEF> {
+    static __device__ __forceinline__ bool run(const DevParams &p, const FastArgs<float> &a, int i, int j, long long time,
+                                               float y, float *out)
+    {
+        if (p.b_cond != WG_BC_DIRICHLET && p.b_cond != WG_BC_ABSORBING) return false;
+        *out = fast_edge32<COEF>(p, a, i, j, time, y);
+        return true;
+    }
+};
+
 // Boundary-line cell of the native form, reference rules.  Returns the value to
 // store (the old psi value y when the reference writes nothing).
 template <class T, int COEF>
 __device__ inline T fast_edge(const DevParams &p, const FastArgs<T> &a, int i, int j, long long time, T y)
 {
+    T r;  // FP32 mirror / absorbing scenes: the FP32 rule
+    if (Edge32Path<T, COEF>::run(p, a, i, j, time, y, &r)) return r;
     Field<T> PHI{a.phi, p.pitch}, PSI{a.psi, p.pitch};
     ActBits ACT{a.act, p.wpitch}, NZ{a.nz, p.wpitch};
     double v;

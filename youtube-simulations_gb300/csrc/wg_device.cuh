@@ -175,6 +175,62 @@ __device__ __forceinline__ bool left_bc(const DevParams &p, int j)
     return p.osc_left && j < p.ny - 1 && j > p.bc_jmin && j < p.bc_jmax;
 }
 
+// FP32 boundary-line cell (rows 0 and nx-1, columns 0 and ny-1) for mirror ("Dirichlet")
+// and absorbing boundaries: edge_cell's rules (below) in the FP32 increment form of
+// upd32 / absorb32, the neighbours the reference mirrors replaced by the cell itself.
+// x, y: phi and psi of the cell; n, sv, e, w: phi at i+1, i-1, j+1, j-1 (any value where
+// outside the grid); ccv, tcv, g: the cell's tcc, tc and tgamma; osc(): the oscillating
+// value.  Returns y where the reference writes nothing.  CLAMP: FLOOR on written cells
+// with act.  Every FP32 stepper (single updates, tiles, skewed passes) uses this rule.
+struct Edge32K {
+    float kappa, ks, kt, gs, gt, vmax;
+};
+template <bool CLAMP, class OscF>
+__device__ __forceinline__ float edge32(const DevParams &p, int gi, int gj, float x, float y, float n, float sv,
+                                        float e, float w, float ccv, float tcv, float g, bool act, const Edge32K &k,
+                                        const OscF &osc)
+{
+    const int NX = p.nx, NY = p.ny;
+    const bool bi0 = gi == 0, bi1 = gi == NX - 1, bj0 = gj == 0, bj1 = gj == NY - 1;
+    int mode = 0;  // 0 leapfrog with mirrored neighbours, 1 absorbing, 2 oscillating value
+    float nb = 0.f, kk = 0.f, gg = 0.f;
+    if (bj0 || bj1) {
+        if (p.osc_topbot && gi > 0 && gi < NX - 1 && ((double)gi < p.tb_shift)) {
+            e = x;
+            w = x;
+        } else if (p.b_cond == WG_BC_DIRICHLET) {
+            if (bi1) n = x;
+            if (bi0) sv = x;
+            if (bj1) e = x; else w = x;
+        } else {
+            mode = 1;
+            nb = bj1 ? w : e;
+            kk = k.kt;
+            gg = k.gt;
+        }
+    } else if (bi0 || bi1) {
+        if (bi0 && left_bc(p, gj)) {
+            mode = 2;
+        } else if (p.b_cond == WG_BC_DIRICHLET) {
+            if (bi0) sv = x; else n = x;
+        } else {
+            mode = 1;
+            nb = bi0 ? n : sv;
+            kk = k.ks;
+            gg = k.gs;
+        }
+    }
+    if (p.osc_left && !p.beam && bi0 && (bj0 || (p.corner2_on && gj == NX - 1))) mode = 2;
+    float v = y;
+    if (mode == 2 || p.twospeeds || act) {
+        if (mode == 0) v = upd32(x, y, ccv, ((n - x) + (sv - x)) + ((e - x) + (w - x)), k.kappa, g);
+        else if (mode == 1) v = absorb32(x, y, tcv, nb, kk, gg);
+        else v = osc();
+        if (CLAMP && p.floor_clamp && act) v = fminf(fmaxf(v, -k.vmax), k.vmax);
+    }
+    return v;
+}
+
 // Any boundary-line cell of the reference (left/right columns, top/bottom rows),
 // computed with the reference's rules.  Returns true when the reference writes the
 // cell; *out then holds the value (corner oscillation included, FLOOR not).

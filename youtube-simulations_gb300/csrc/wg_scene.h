@@ -48,7 +48,8 @@ struct wg_scene {
     size_t rgb_bytes = 0;
     int tb_k = 0, tile_i = 0, tile_j = 0;
     SkewPlanCache skew[WG_SKEW_MAX_K + 1];  // task lists of the skewed kernel, by depth
-    float *bv_osc = nullptr, *bv_src = nullptr;  // boundary values of the current step() call
+    float *bv_osc = nullptr;   // oscillating values of the current step() call, [n][ny]
+    double *bv_src = nullptr;  // point-source increments of the current step() call, [n]
     size_t bv_cap = 0;
     long long bv_t0 = 0;
     bool uploaded = false;

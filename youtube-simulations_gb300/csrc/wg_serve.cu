@@ -16,7 +16,7 @@ namespace wg {
 
 struct FrameDev {                // one resident scene in the frame launch
     DevParams p;
-    void *f[2];
+    void *f[4];
     uint32_t *nz;
     int slot;                    // batch slot (its dynamic state says which buffer is phi)
     int w, h, row_base;
@@ -40,7 +40,8 @@ __global__ void k_server_frames(const FrameDev *__restrict__ tab, int ntab, cons
     const FrameDev &d = tab[e];
     const int row = (int)blockIdx.x - d.row_base;
     if (row >= d.h) return;
-    const T *phi = (const T *)d.f[dyn[d.slot].cur];
+    const SlotDyn dy = dyn[d.slot];
+    const T *phi = (const T *)d.f[2 * dy.pair + dy.cur];
     const int j = row * fp.size;
     for (int col = threadIdx.x; col < d.w; col += blockDim.x) {
         const int i = col * fp.size;
@@ -120,7 +121,8 @@ static uint64_t request_bytes(const wg_server *s, const wg_params &p)
 {
     const size_t esz = s->cfg.precision == WG_FP32 ? 4 : 8;
     const size_t pitch = pitch_for(p.ny, (int)esz), wp = (pitch + 31) / 32;
-    const size_t fields = 2 * (size_t)p.nx * pitch * esz, masks = 2 * (size_t)p.nx * wp * 4;
+    const size_t pairs = batch_skew_ok(p, s->cfg.precision) ? 2 : 1;  // skewed scenes keep a second pair
+    const size_t fields = 2 * pairs * (size_t)p.nx * pitch * esz, masks = 2 * (size_t)p.nx * wp * 4;
     const size_t frame = (size_t)(p.nx / s->cfg.frame.size) * (p.ny / s->cfg.frame.size) * 3;
     return fields + masks + frame + (size_t)p.nx * 40 + 4096;
 }
@@ -137,8 +139,7 @@ static wg_status server_layout(wg_server *s)
         FrameDev d;
         memset(&d, 0, sizeof d);
         d.p = h.dp;
-        d.f[0] = h.f[0];
-        d.f[1] = h.f[1];
+        for (int q = 0; q < 4; q++) d.f[q] = h.f[q];
         d.nz = h.nz;
         d.slot = r.slot;
         d.w = r.w;

@@ -21,6 +21,7 @@
 #include <mutex>
 #include <tuple>
 #include "wg_scene.h"
+#include "wg_batch.h"
 #include "wg_tma.cuh"
 
 namespace wg {
@@ -36,7 +37,7 @@ struct TbArgs {
     float c2, c2b, gam, gamb, kappa, ks, kt, gs, gt, vmax, courant, courantb;
     long long t0;             // step counter before the pass
     const float *osc;         // oscillating_bc values of the pass, [K][ny]
-    const float *src;         // point-source increments of the pass, [K]
+    const double *src;        // point-source increments of the pass, [K]
     int *err;                 // set to 1 when a bounded wait gives up
 };
 
@@ -50,53 +51,14 @@ template <int COEF>
 __device__ __forceinline__ float tb_general(const DevParams &p, const TbArgs &a, int gi, int gj, int s, float x,
                                             float y, float nip, float nim, float njp, float njm, float cc, int act)
 {
-    const int NX = p.nx, NY = p.ny;
-    const bool bi = (gi == 0 || gi == NX - 1), bj = (gj == 0 || gj == NY - 1);
-    int mode = 0;  // 0 leapfrog (mirrored neighbours), 1 absorbing, 2 oscillating value
-    float nb = 0.f, kk = 0.f, gg = 0.f;
-    if (bj) {
-        if (p.osc_topbot && ((double)gi < p.tb_shift) && gi < NX - 1 && gi > 0) {
-            njp = x;
-            njm = x;
-        } else if (p.b_cond == WG_BC_DIRICHLET) {
-            if (gi == NX - 1) nip = x;
-            if (gi == 0) nim = x;
-            if (gj == NY - 1) njp = x; else njm = x;
-        } else {
-            mode = 1;
-            nb = (gj == NY - 1) ? njm : njp;
-            kk = a.kt;
-            gg = a.gt;
-        }
-    } else if (bi) {
-        if (gi == 0 && left_bc(p, gj)) {
-            mode = 2;
-        } else if (p.b_cond == WG_BC_DIRICHLET) {
-            if (gi == 0) nim = x; else nip = x;
-        } else {
-            mode = 1;
-            nb = (gi == 0) ? nip : nim;
-            kk = a.ks;
-            gg = a.gs;
-        }
-    }
-    if (p.osc_left && !p.beam && gi == 0 && (gj == 0 || (p.corner2_on && gj == NX - 1))) mode = 2;
-    const bool w = (mode == 2) || p.twospeeds || act;
-    float v = y;
-    if (w) {
-        if (mode == 0) {
-            const float ccv = (COEF == WG_COEF_TABLE) ? cc : (act ? a.c2 : a.c2b);
-            const float g = (COEF == WG_COEF_TABLE) ? a.gam : (act ? a.gam : a.gamb);
-            v = upd32(x, y, ccv, ((nip - x) + (nim - x)) + ((njp - x) + (njm - x)), a.kappa, g);
-        } else if (mode == 1) {
-            const float tcv = (COEF == WG_COEF_TABLE) ? a.tc[(size_t)gi * p.pitch + gj] : (act ? a.courant : a.courantb);
-            v = absorb32(x, y, tcv, nb, kk, gg);
-        } else {
-            v = a.osc[(size_t)(s - 1) * NY + gj];
-        }
-        if (p.floor_clamp && act) v = fminf(fmaxf(v, -a.vmax), a.vmax);
-    }
-    if (p.src_on && gi == p.src_i && gj == p.src_j) v += a.src[s - 1];
+    const float ccv = (COEF == WG_COEF_TABLE) ? cc : (act ? a.c2 : a.c2b);
+    const float g = (COEF == WG_COEF_TABLE) ? a.gam : (act ? a.gam : a.gamb);
+    const float tcv = (COEF == WG_COEF_TABLE) ? (a.tc ? a.tc[(size_t)gi * p.pitch + gj] : 0.f)
+                                              : (act ? a.courant : a.courantb);
+    const Edge32K k{a.kappa, a.ks, a.kt, a.gs, a.gt, a.vmax};
+    float v = edge32<true>(p, gi, gj, x, y, nip, nim, njp, njm, ccv, tcv, g, act != 0, k,
+                           [&] { return a.osc[(size_t)(s - 1) * p.ny + gj]; });
+    if (p.src_on && gi == p.src_i && gj == p.src_j) v = (float)A_((double)v, a.src[s - 1]);
     return v;
 }
 
@@ -139,14 +101,14 @@ __device__ __forceinline__ void tb_rows_interior(const DevParams &p, const TbArg
 
 // oscillating_bc(t0 + s, j) for s = 1..n (when OSCILLATE_LEFT) and the point-source
 // increment of update t0 + s, rounded to FP32, for the passes of one step() call.
-__global__ void k_boundary_values(const __grid_constant__ DevParams p, long long t0, int n, float *osc, float *src)
+__global__ void k_boundary_values(const __grid_constant__ DevParams p, long long t0, int n, float *osc, double *src)
 {
     const int idx = blockIdx.x * blockDim.x + threadIdx.x;
     if (p.osc_left && idx < n * p.ny) {
         const int s = idx / p.ny, j = idx % p.ny;
         osc[idx] = (float)osc_bc(p, (int)(t0 + s + 1), j);
     }
-    if (p.src_on && idx < n) src[idx] = (float)point_source(p, t0 + idx + 1);
+    if (p.src_on && idx < n) src[idx] = point_source(p, t0 + idx + 1);
 }
 
 // Shared-memory layout of one tile: F0, F1 (both levels), Cs (tcc, table mode),
@@ -311,7 +273,9 @@ __global__ void __launch_bounds__(256) k_step_tb(const __grid_constant__ DevPara
 // sv = i-1, e = j+1, w = j-1) and level s-2 (y).  cc is the cell's tcc, tcv its tc (table
 // mode).  GEN = false: a cell off the boundary lines and the source; PLAIN additionally
 // promises twospeeds and no FLOOR clamp, so every such cell takes the leapfrog update.
-template <int COEF, bool GEN, bool PLAIN>
+// INL: oscillating values and source increments are computed here (batches) instead of
+// read from the per-call arrays; both are the same double values, rounded the same way.
+template <int COEF, bool GEN, bool PLAIN, bool INL = false>
 __device__ __forceinline__ float skew_cell(const DevParams &p, const TbArgs &a, int gi, int gj, int s, float x, float y,
                                            float n, float sv, float e, float w, float cc, float tcv, bool act)
 {
@@ -326,49 +290,12 @@ __device__ __forceinline__ float skew_cell(const DevParams &p, const TbArgs &a, 
         }
         return v;
     }
-    const int NX = p.nx, NY = p.ny;
-    const bool bi0 = gi == 0, bi1 = gi == NX - 1, bj0 = gj == 0, bj1 = gj == NY - 1;
-    int mode = 0;  // 0 leapfrog with mirrored neighbours, 1 absorbing, 2 oscillating value
-    float nb = 0.f, kk = 0.f, gg = 0.f;
-    if (bj0 || bj1) {
-        if (p.osc_topbot && gi > 0 && gi < NX - 1 && ((double)gi < p.tb_shift)) {
-            e = x;
-            w = x;
-        } else if (p.b_cond == WG_BC_DIRICHLET) {
-            if (bi1) n = x;
-            if (bi0) sv = x;
-            if (bj1) e = x; else w = x;
-        } else {
-            mode = 1;
-            nb = bj1 ? w : e;
-            kk = a.kt;
-            gg = a.gt;
-        }
-    } else if (bi0 || bi1) {
-        if (bi0 && left_bc(p, gj)) {
-            mode = 2;
-        } else if (p.b_cond == WG_BC_DIRICHLET) {
-            if (bi0) sv = x; else n = x;
-        } else {
-            mode = 1;
-            nb = bi0 ? n : sv;
-            kk = a.ks;
-            gg = a.gs;
-        }
-    }
-    if (p.osc_left && !p.beam && bi0 && (bj0 || (p.corner2_on && gj == NX - 1))) mode = 2;
-    float v = y;
-    if (mode == 2 || p.twospeeds || act) {
-        if (mode == 0) {
-            v = upd32(x, y, ccv, ((n - x) + (sv - x)) + ((e - x) + (w - x)), a.kappa, g);
-        } else if (mode == 1) {
-            v = absorb32(x, y, (COEF == WG_COEF_TABLE) ? tcv : (act ? a.courant : a.courantb), nb, kk, gg);
-        } else {
-            v = a.osc[(size_t)(s - 1) * NY + gj];
-        }
-        if (p.floor_clamp && act) v = fminf(fmaxf(v, -a.vmax), a.vmax);
-    }
-    if (p.src_on && gi == p.src_i && gj == p.src_j) v += a.src[s - 1];
+    const float tce = (COEF == WG_COEF_TABLE) ? tcv : (act ? a.courant : a.courantb);
+    const Edge32K k{a.kappa, a.ks, a.kt, a.gs, a.gt, a.vmax};
+    float v = edge32<true>(p, gi, gj, x, y, n, sv, e, w, ccv, tce, g, act, k, [&] {
+        return INL ? (float)osc_bc(p, (int)(a.t0 + s), gj) : a.osc[(size_t)(s - 1) * p.ny + gj];
+    });
+    if (p.src_on && gi == p.src_i && gj == p.src_j) v = (float)A_((double)v, INL ? point_source(p, a.t0 + s) : a.src[s - 1]);
     return v;
 }
 
@@ -453,18 +380,18 @@ template <int COEF> struct SkewSlot {
 // GEN = false: inner tiles (fix = false) and tiles of column 0, of column ny-1 when ny is
 // a multiple of 4, or of the point source (fix = true), all away from rows 0 and nx-1.
 // GEN = true (fix = true): the others, with the general rule on rows 0 and nx-1.
-template <int COEF, int K, bool PLAIN, bool GEN>
+// Columns [lo, hi) of the tile are stored (lo, hi multiples of 4 but for hi = ny).
+template <int COEF, int K, bool PLAIN, bool GEN, bool INL = false>
 __device__ __forceinline__ void skew_strip(const DevParams &p, const TbArgs &a, int i_s, int i_e, int gj0, int lane,
-                                           float *ring, bool edge)
+                                           float *ring, bool edge, int lo, int hi)
 {
     using SL = SkewSlot<COEF>;
     constexpr int D = SL::DEPTH;
     constexpr int QD = D - 1;                    // rows in flight ahead of the one in use
-    constexpr int H = (K + 3) & ~3;
     constexpr bool NEED_ACT = !(PLAIN && COEF == WG_COEF_TABLE);  // the plain table update ignores the mask
     const bool need_tce = edge && COEF == WG_COEF_TABLE;           // tc of this lane's boundary column
     const int m0 = i_s - K - 1, m1 = i_e + K;                      // input rows [m0, m1)
-    const bool lane_core = 4 * lane >= H && 4 * lane < 128 - H;
+    const bool lane_core = gj0 >= lo && gj0 < hi;
     const bool grp_ok = gj0 >= 0 && gj0 < p.ny;  // the group holds at least one domain column
     // edge tiles: the lane's boundary column (0..3), or -1; the domain has ny >= 8 columns
     const int cr = p.ny - 1 - gj0;  // column ny-1 within the lane's group when 0..3
@@ -557,7 +484,7 @@ __device__ __forceinline__ void skew_strip(const DevParams &p, const TbArgs &a, 
                     const float e = (c < 3) ? Wc[c + 1 < 4 ? c + 1 : 3] : e3;
                     const float w = (c > 0) ? Wc[c > 0 ? c - 1 : 0] : w0;
                     const bool act = NEED_ACT ? ((aq >> (4 * lv + c)) & 1u) : true;
-                    v[c] = skew_cell<COEF, false, PLAIN>(p, a, r, gj0 + c, lv, Wc[c], Yl[c], W[lv - 1][2][c],
+                    v[c] = skew_cell<COEF, false, PLAIN, INL>(p, a, r, gj0 + c, lv, Wc[c], Yl[c], W[lv - 1][2][c],
                                                          W[lv - 1][0][c], e, w, T[lv][c], 0.f, act);
                 }
                 if (!GEN && edge) {  // warp-uniform
@@ -571,10 +498,10 @@ __device__ __forceinline__ void skew_strip(const DevParams &p, const TbArgs &a, 
                         v[3] = lf ? v[3] : res;
                     }
                     if (src_lane && r == p.src_i) {
-                        const float add = a.src[lv - 1];
+                        const double add = INL ? point_source(p, a.t0 + lv) : a.src[lv - 1];
                         const int cs = p.src_j - gj0;
 #pragma unroll
-                        for (int c = 0; c < 4; c++) v[c] += (cs == c) ? add : 0.f;
+                        for (int c = 0; c < 4; c++) v[c] = (cs == c) ? (float)A_((double)v[c], add) : v[c];
                     }
                 }
                 if (GEN) {
@@ -598,7 +525,7 @@ __device__ __forceinline__ void skew_strip(const DevParams &p, const TbArgs &a, 
                             const int gj = gj0 + c;
                             if (gj < 0 || gj >= p.ny) continue;
                             const float tcv = (COEF == WG_COEF_TABLE && a.tc) ? a.tc[(size_t)r * p.pitch + gj] : 0.f;
-                            const float res = skew_cell<COEF, true, false>(
+                            const float res = skew_cell<COEF, true, false, INL>(
                                 p, a, r, gj, lv, pick4(Wc[0], Wc[1], Wc[2], Wc[3], c), pick4(Yl[0], Yl[1], Yl[2], Yl[3], c),
                                 pick4(W[lv - 1][2][0], W[lv - 1][2][1], W[lv - 1][2][2], W[lv - 1][2][3], c),
                                 pick4(W[lv - 1][0][0], W[lv - 1][0][1], W[lv - 1][0][2], W[lv - 1][0][3], c),
@@ -611,10 +538,10 @@ __device__ __forceinline__ void skew_strip(const DevParams &p, const TbArgs &a, 
                             v[3] = (c == 3) ? res : v[3];
                         }
                     } else if (src_lane && r == p.src_i) {  // the general rule adds it on rows 0 and nx-1
-                        const float add = a.src[lv - 1];
+                        const double add = INL ? point_source(p, a.t0 + lv) : a.src[lv - 1];
                         const int cs = p.src_j - gj0;
 #pragma unroll
-                        for (int c = 0; c < 4; c++) v[c] += (cs == c) ? add : 0.f;
+                        for (int c = 0; c < 4; c++) v[c] = (cs == c) ? (float)A_((double)v[c], add) : v[c];
                     }
                 }
                 }  // levels in use
@@ -663,8 +590,9 @@ __global__ void __launch_bounds__(128, 4) k_step_skew(const __grid_constant__ De
     float *ring = reinterpret_cast<float *>(skew_smem) + (threadIdx.x >> 5) * SkewSlot<COEF>::DEPTH * SkewSlot<COEF>::SIZE;
     const int4 t = tasks[warp];
     const int gj0 = t.x * STEP - H + 4 * lane;
-    if (t.w == 2) skew_strip<COEF, K, PLAIN, true>(p, a, t.y, t.z, gj0, lane, ring, true);
-    else skew_strip<COEF, K, PLAIN, false>(p, a, t.y, t.z, gj0, lane, ring, t.w == 1);
+    const int lo = t.x * STEP, hi = lo + STEP;  // the core columns of tile t.x
+    if (t.w == 2) skew_strip<COEF, K, PLAIN, true>(p, a, t.y, t.z, gj0, lane, ring, true, lo, hi);
+    else skew_strip<COEF, K, PLAIN, false>(p, a, t.y, t.z, gj0, lane, ring, t.w == 1, lo, hi);
 }
 
 static bool skew_shape_ok(const DevParams &p, int K, int S)
@@ -736,18 +664,23 @@ static int skew_call(const DevParams &p, const TbArgs *a, int coef, int K, const
 // inner one.  Chunks are sized so that all warps carry about the same cost and the list
 // fills the resident warps once (inner chunks of at least min_rows rows).  Tasks are
 // ordered by row band so that the boundary chunks spread over the SMs.
+// shifted = false: tile tj spans columns [tj*step - H, tj*step - H + 128) and stores
+// [tj*step, (tj+1)*step).  shifted = true (batches): tile tj starts at column tj*step, so
+// the first tile needs no halo on the left and the last none on the right (column 0 and
+// ny-1 read no column outside the grid); a scene of 128 columns or fewer is one tile.
 #define SKEW_EDGE_COST 1.9  // per-warp timing of the 3840x2160 passes: 1.87 (K 4), 1.90 (K 5)
-static std::vector<int4> skew_plan(const DevParams &p, int K, int min_rows, int cap)
+static std::vector<int4> skew_plan(const DevParams &p, int K, int min_rows, int cap, bool shifted = false)
 {
-    const int H = (K + 3) & ~3, step = 128 - 2 * H, F = 2 * K + 1;
-    const int nx = p.nx, tiles_j = (p.ny + step - 1) / step;  // tile tj stores columns [tj*step, (tj+1)*step)
+    const int H = (K + 3) & ~3, step = 128 - 2 * H, F = 2 * K + 1, sh = shifted ? 0 : H;
+    const int nx = p.nx;
+    const int tiles_j = shifted ? 1 + std::max(0, (p.ny - 128 + step - 1) / step) : (p.ny + step - 1) / step;
     const int R = std::max(K + 1, 8);
     const bool segs = nx >= 2 * R + 1;  // else every task is of kind 2
     const int mid0 = segs ? R : 0, mid1 = segs ? nx - R : nx, nmid = mid1 - mid0;
     std::vector<int> col_kind(tiles_j);  // 0 inner, 1 column 0 or ny-1 (last of a group), 2 ny-1 elsewhere
     int n_edge = 0;
     for (int tj = 0; tj < tiles_j; tj++) {
-        const int t0 = tj * step - H;
+        const int t0 = tj * step - sh;
         const bool left = t0 < 1, right = t0 + 128 > p.ny - 1;
         col_kind[tj] = (right && (p.ny & 3) != 0) ? 2 : ((left || right) ? 1 : 0);
         n_edge += col_kind[tj] != 0;
@@ -771,7 +704,7 @@ static std::vector<int4> skew_plan(const DevParams &p, int K, int min_rows, int 
     struct T { double key; int4 t; };
     std::vector<T> ts;
     auto add = [&](int tj, int i_s, int i_e, int kind) {
-        const int t0 = tj * step - H;
+        const int t0 = tj * step - sh;
         const bool src = p.src_on && p.src_i >= i_s - K && p.src_i < i_e + K && p.src_j >= t0 && p.src_j < t0 + 128;
         if (kind == 0 && src) kind = 1;
         ts.push_back({(i_s + i_e) * 0.5 / nx + tj * 1e-9, make_int4(tj, i_s, i_e, kind)});
@@ -811,6 +744,135 @@ static wg_status skew_tasks(wg_scene *s, int K, int L, const int4 **tasks, int *
     *tasks = c.dev;
     *ntasks = c.n;
     return WG_OK;
+}
+
+// ---------------------------------------------------------------------------
+// Skewed passes over a batch of scenes (mask coefficients, FP32).  Persistent warps take
+// tasks from a ticket counter: table entry, first column of the tile (shifted tiling),
+// rows i_s | i_e << 16, kind.  Each task's parameters and arguments are staged in the
+// warp's shared memory; pass q of a frame reads pair (pair ^ q) of the scene (with the
+// scene's cur on the first pass, 0 after) and writes the other pair.  Oscillating values
+// and source increments are computed inline at update time + toff + level.
+// ---------------------------------------------------------------------------
+static_assert(sizeof(DevParams) % 4 == 0, "DevParams is copied as 32-bit words");
+
+template <int K>
+__global__ void __launch_bounds__(128, 4) k_batch_skew(const SlotDev *__restrict__ tab, const SlotDyn *__restrict__ dyn,
+                                                       const int4 *__restrict__ tasks, const int *__restrict__ ntasks,
+                                                       int *__restrict__ ticket, int q, int toff)
+{
+    constexpr int H = (K + 3) & ~3;
+    using SL = SkewSlot<WG_COEF_MASK>;
+    extern __shared__ float4 skew_smem[];
+    __shared__ DevParams s_p[4];
+    __shared__ TbArgs s_a[4];
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    float *ring = reinterpret_cast<float *>(skew_smem) + wid * SL::DEPTH * SL::SIZE;
+    DevParams &p = s_p[wid];
+    TbArgs &a = s_a[wid];
+    const int n = *ntasks;
+    for (;;) {
+        int t = 0;
+        if (lane == 0) t = atomicAdd(ticket, 1);
+        t = __shfl_sync(0xffffffffu, t, 0);
+        if (t >= n) break;  // warp-uniform
+        const int4 w = tasks[t];
+        const SlotDev &sd = tab[w.x];
+        __syncwarp();  // every lane is done with the previous task's parameters
+        const int *src = reinterpret_cast<const int *>(&sd.p);
+        int *dst = reinterpret_cast<int *>(&p);
+        for (int k = lane; k < (int)(sizeof(DevParams) / 4); k += 32) dst[k] = src[k];
+        if (lane == 0) {
+            const SlotDyn dy = dyn[sd.slot];
+            const int pin = dy.pair ^ (q & 1), cin = q == 0 ? dy.cur : 0, pout = pin ^ 1;
+            a.phi = (const float *)sd.f[2 * pin + cin];
+            a.psi = (const float *)sd.f[2 * pin + 1 - cin];
+            a.phi_out = (float *)sd.f[2 * pout];
+            a.psi_out = (float *)sd.f[2 * pout + 1];
+            a.act = sd.act;
+            a.tcc = a.tc = nullptr;
+            a.c2 = (float)sd.p.c2;
+            a.c2b = (float)sd.p.c2b;
+            a.gam = (float)sd.p.gam;
+            a.gamb = (float)sd.p.gamb;
+            a.kappa = (float)sd.p.kappa;
+            a.ks = (float)sd.p.kappa_sides;
+            a.kt = (float)sd.p.kappa_topbot;
+            a.gs = (float)sd.p.gamma_sides;
+            a.gt = (float)sd.p.gamma_topbot;
+            a.vmax = (float)sd.p.vmax;
+            a.courant = (float)sd.p.courant;
+            a.courantb = (float)sd.p.courantb;
+            a.t0 = dy.time + toff;
+            a.osc = nullptr;
+            a.src = nullptr;
+            a.err = nullptr;
+        }
+        __syncwarp();
+        const int i_s = w.z & 0xFFFF, i_e = (int)((unsigned)w.z >> 16);
+        const int gjs = w.y, gj0 = gjs + 4 * lane;
+        const int lo = gjs <= 0 ? 0 : gjs + H;
+        const int hi = gjs + 128 >= p.ny ? p.ny : gjs + 128 - H;
+        if (w.w == 2) skew_strip<WG_COEF_MASK, K, false, true, true>(p, a, i_s, i_e, gj0, lane, ring, true, lo, hi);
+        else skew_strip<WG_COEF_MASK, K, false, false, true>(p, a, i_s, i_e, gj0, lane, ring, w.w == 1, lo, hi);
+    }
+}
+
+template <int K>
+static int batch_skew_cap_k()
+{
+    constexpr size_t smem = 4 * SkewSlot<WG_COEF_MASK>::DEPTH * SkewSlot<WG_COEF_MASK>::SIZE * sizeof(float);
+    static int per_sm = 0;
+    if (!per_sm) {
+        cudaFuncSetAttribute(k_batch_skew<K>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        int nb = 0;
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_batch_skew<K>, 128, smem);
+        per_sm = nb > 0 ? nb : 1;
+    }
+    return per_sm * sm_count() * 4;
+}
+
+int batch_skew_capacity(int K)
+{
+    switch (K) {
+    case 2: return batch_skew_cap_k<2>();
+    case 3: return batch_skew_cap_k<3>();
+    case 4: return batch_skew_cap_k<4>();
+    case 5: return batch_skew_cap_k<5>();
+    case 6: return batch_skew_cap_k<6>();
+    default: return 0;
+    }
+}
+
+void launch_batch_skew(int K, const SlotDev *tab, const SlotDyn *dyn, const int4 *tasks, const int *ntasks, int *ticket,
+                       int q, int toff, cudaStream_t st)
+{
+    constexpr size_t smem = 4 * SkewSlot<WG_COEF_MASK>::DEPTH * SkewSlot<WG_COEF_MASK>::SIZE * sizeof(float);
+    const int blocks = std::max(1, batch_skew_capacity(K) / 4);
+    switch (K) {
+    case 2: k_batch_skew<2><<<blocks, 128, smem, st>>>(tab, dyn, tasks, ntasks, ticket, q, toff); break;
+    case 3: k_batch_skew<3><<<blocks, 128, smem, st>>>(tab, dyn, tasks, ntasks, ticket, q, toff); break;
+    case 4: k_batch_skew<4><<<blocks, 128, smem, st>>>(tab, dyn, tasks, ntasks, ticket, q, toff); break;
+    case 5: k_batch_skew<5><<<blocks, 128, smem, st>>>(tab, dyn, tasks, ntasks, ticket, q, toff); break;
+    case 6: k_batch_skew<6><<<blocks, 128, smem, st>>>(tab, dyn, tasks, ntasks, ticket, q, toff); break;
+    default: break;
+    }
+}
+
+bool batch_skew_ok(const wg_params &p, int prec)
+{
+    return prec == WG_FP32 && (p.b_cond == WG_BC_DIRICHLET || p.b_cond == WG_BC_ABSORBING) && !p.bc_neumann &&
+           p.ny >= 8 && p.nx >= 2 && p.nx <= 0xFFFF;
+}
+
+void batch_skew_plan(const DevParams &p, int entry, int K, int cap, std::vector<int4> &tasks, std::vector<float> &cost)
+{
+    const int H = (K + 3) & ~3, step = 128 - 2 * H, F = 2 * K + 1;
+    const std::vector<int4> v = skew_plan(p, K, 32, cap, true);
+    for (const int4 &t : v) {
+        tasks.push_back(make_int4(entry, t.x * step, (int)((unsigned)t.y | ((unsigned)t.z << 16)), t.w));
+        cost.push_back((float)((t.z - t.y + F) * (t.w ? SKEW_EDGE_COST : 1.0)));
+    }
 }
 
 static int tb_halo(int K) { return (K + 3) & ~3; }
@@ -921,10 +983,11 @@ wg_status tb_prepare(wg_scene *s, int n)
     if (need > s->bv_cap) {
         if (s->bv_osc) cudaFree(s->bv_osc);
         if (s->bv_src) cudaFree(s->bv_src);
-        s->bv_osc = s->bv_src = nullptr;
+        s->bv_osc = nullptr;
+        s->bv_src = nullptr;
         s->bv_cap = 0;
         WG_CUDA(cudaMalloc(&s->bv_osc, need * sizeof(float)));
-        WG_CUDA(cudaMalloc(&s->bv_src, need * sizeof(float)));
+        WG_CUDA(cudaMalloc(&s->bv_src, need * sizeof(double)));
         s->bv_cap = need;
     }
     s->bv_t0 = s->time;

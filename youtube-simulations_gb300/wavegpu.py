@@ -96,6 +96,8 @@ SIGNATURES = {
     "wg_batch_energy": (_I32, [_V, _I32, ctypes.POINTER(_D)]),
     "wg_batch_count": (_I32, [_V, ctypes.POINTER(_I32), ctypes.POINTER(_I64)]),
     "wg_batch_launch_count": (_I32, [_V, ctypes.POINTER(_I64)]),
+    "wg_batch_set_skew": (_I32, [_V, _I32]),
+    "wg_batch_skew_depths": (_I32, [_V, ctypes.POINTER(_I32), ctypes.POINTER(ctypes.c_double)]),
     "wg_server_create": (_I32, [_V, _V, ctypes.POINTER(_V)]),
     "wg_server_destroy": (_I32, [_V]),
     "wg_server_submit": (_I32, [_V, _V, _V, _V, _V, _I32, _I32, ctypes.POINTER(_I64)]),
@@ -417,8 +419,10 @@ def scene_bytes(params, precision=P.FP32, coef=P.COEF_MASK):
 
 
 class Batch:
-    """Uneven scenes advanced together by one persistent kernel per update, each frame
-    replayed as a CUDA graph (wg_batch_*).  Masks are 0/1 (WG_COEF_MASK coefficients)."""
+    """Uneven scenes advanced together, each frame replayed as a CUDA graph (wg_batch_*):
+    single updates by one persistent kernel per update, or skewed passes of 2..6 updates
+    for FP32 scenes with mirror or absorbing boundaries (same fields bit for bit).  Masks
+    are 0/1 (WG_COEF_MASK coefficients)."""
 
     def __init__(self, precision=P.FP32, stream=None):
         h = ctypes.c_void_p()
@@ -458,6 +462,18 @@ class Batch:
 
     def step(self, n):
         check(lib().wg_batch_step(self.h, int(n)))
+
+    def set_skew(self, mode):
+        """Skewed passes: -1 tuned per size class (default), 0 off, 2..6 a fixed depth."""
+        check(lib().wg_batch_set_skew(self.h, int(mode)))
+
+    def skew_depths(self):
+        """(depth per size class [16], autotuner ms per update [16, 8] by class and depth);
+        size class = floor(log2(cells)) - 10, clamped to 0..15."""
+        d = (_I32 * 16)()
+        ms = (ctypes.c_double * 128)()
+        check(lib().wg_batch_skew_depths(self.h, d, ms))
+        return list(d), np.array(ms[:]).reshape(16, 8)
 
     def download(self, slot):
         if slot not in self.params:  # let the library report the unknown slot
