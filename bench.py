@@ -285,6 +285,7 @@ def run_ours(args):
     e2e_value = world * CELLS * args.e2e_steps * UPDATES_PER_STEP / (e2e_ms / 1e3) / 1e9
 
     batch_res = run_batch(args, P, scenes, W, stream, rank) if not args.no_batch else None
+    sweep_res = run_sweep(args, P, scenes, W, stream, rank) if not args.no_sweep else None
     serve_res = run_serving(args, P, scenes, W, stream, rank) if not args.no_serving else None
 
     if rank != 0:
@@ -347,6 +348,8 @@ def run_ours(args):
     line["accuracy"] = accuracy
     if batch_res:
         line["batch"] = batch_res
+    if sweep_res:
+        line["sweep"] = sweep_res
     if serve_res:
         line["serving"] = serve_res
     print(json.dumps(line))
@@ -388,6 +391,55 @@ def run_batch(args, P, scenes, W, stream, rank):
     out["workload"] = ("uneven batch: 256 instances log-uniform 256x256..1280x720, mixed masks, Dirichlet/periodic, "
                        "one persistent kernel per update over a tile work queue, frame of 10 updates as a CUDA graph")
     out["energy_check_instance0"] = e_check
+    return out
+
+
+def run_sweep(args, P, scenes, W, stream, rank):
+    """Parameter-sweep batch: 4096 seeded instances, nx and ny log-uniform in 128..512, a
+    rectangle with 1-3 circular obstacles, absorbing, GAMMA U(0, 1e-3), COURANT
+    U(0.05, 0.2).  FP32 with skewed passes at the depth the autotuner picks per size
+    class, 2000 updates in frames of 10 (3 warm-up frames, the rest timed); the same
+    instances in FP64 give each instance's max-abs error after the 2000 updates."""
+    import numpy as np
+    import torch
+    rng = np.random.default_rng(3000 + rank)
+    members = [scenes.sweep_member(rng) for _ in range(args.sweep_instances)]
+    frames = max(4, args.sweep_steps // 10)
+    out, fields = {}, {}
+    for prec in ("fp32", "fp64"):
+        b = W.Batch(P.FP32 if prec == "fp32" else P.FP64, stream=stream.cuda_stream)
+        slots = [b.add(m.params, m.phi, m.psi, m.xy) for m in members]
+        n_active, cells = b.count()
+        for _ in range(3):
+            b.step(10)
+        torch.cuda.synchronize()
+        l0 = b.launches()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for _ in range(frames - 3):
+            b.step(10)
+        e1.record(stream)
+        e1.synchronize()
+        ms = e0.elapsed_time(e1)
+        out[prec] = {"value": cells * 10 * (frames - 3) / (ms / 1e3) / 1e9, "unit": METRIC,
+                     "ms_per_frame": ms / (frames - 3), "gpu_launches": b.launches() - l0}
+        if prec == "fp32":
+            depths, tune = b.skew_depths()
+            out["fp32"]["depth_per_size_class"] = {
+                f"2^{c + 10}..2^{c + 11} cells": depths[c] for c in range(16) if depths[c]}
+        fields[prec] = [b.download(s)[0] for s in slots]
+        b.close()
+    err = np.array([np.max(np.abs(a - b)) for a, b in zip(fields["fp32"], fields["fp64"])])
+    rel = np.array([np.max(np.abs(a - b)) / max(np.max(np.abs(b)), 1e-300)
+                    for a, b in zip(fields["fp32"], fields["fp64"])])
+    out.update({"instances": n_active, "cells": cells, "updates": 10 * frames,
+                "max_abs_err_vs_fp64": {"max": float(err.max()), "p50": float(np.median(err)),
+                                        "p99": float(np.quantile(err, 0.99)),
+                                        "max_rel_to_field_max": float(rel.max())},
+                "workload": f"parameter sweep: {n_active} instances, nx, ny log-uniform 128..512, rectangle with "
+                            "1-3 circular obstacles, absorbing, GAMMA U(0,1e-3), COURANT U(0.05,0.2), "
+                            f"{10 * frames} updates in frames of 10 (CUDA graphs), FP32 skewed passes at the "
+                            "autotuned depth per size class vs FP64 single updates"})
     return out
 
 
@@ -434,8 +486,9 @@ def run_serving(args, P, scenes, W, stream, rank):
 
 def run_probe(args):
     """Small, fixed cases for kernel captures (ncu): the config-2 scene with a given
-    precision and temporal blocking, stepped `--probe-updates` times, or a 64-instance
-    batch stepped 4 frames of 10 updates."""
+    precision and temporal blocking, stepped `--probe-updates` times, a 64-instance
+    batch stepped 4 frames of 10 updates, or 512 parameter-sweep instances (FP32,
+    skewed passes of depth `--probe-block` K) stepped 4 frames of 10 updates."""
     import numpy as np
     _package()
     from youtube_simulations_gb300 import params as P
@@ -450,6 +503,18 @@ def run_probe(args):
         for _ in range(4):
             b.step(10)
         print(json.dumps({"probe": "batch", "instances": b.count()[0], "energy0": b.energy(0)}))
+        b.close()
+        return 0
+    if args.probe == "sweep":
+        rng = np.random.default_rng(3000)
+        b = W.Batch(P.FP32)
+        b.set_skew(args.probe_block[0])
+        for _ in range(512):
+            m = scenes.sweep_member(rng)
+            b.add(m.params, m.phi, m.psi, m.xy)
+        for _ in range(4):
+            b.step(10)
+        print(json.dumps({"probe": "sweep", "instances": b.count()[0], "cells": b.count()[1], "energy0": b.energy(0)}))
         b.close()
         return 0
     sc = scenes.config2(seed=0, nx=NX, ny=NY)
@@ -477,11 +542,14 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--ref-updates", type=int, default=20, help="updates per reference step")
     ap.add_argument("--e2e-steps", type=int, default=20)
-    ap.add_argument("--probe", choices=["fp32", "fp64", "batch"], help="run a small fixed case for kernel captures")
+    ap.add_argument("--probe", choices=["fp32", "fp64", "batch", "sweep"], help="run a small fixed case for kernel captures")
     ap.add_argument("--probe-block", type=int, nargs=3, default=[3, 16, 256], metavar=("K", "L", "W"))
     ap.add_argument("--probe-updates", type=int, default=24)
     ap.add_argument("--no-batch", action="store_true")
     ap.add_argument("--no-serving", action="store_true")
+    ap.add_argument("--no-sweep", action="store_true")
+    ap.add_argument("--sweep-instances", type=int, default=4096)
+    ap.add_argument("--sweep-steps", type=int, default=2000)
     ap.add_argument("--batch-instances", type=int, default=256)
     ap.add_argument("--batch-frames", type=int, default=20)
     ap.add_argument("--serve-requests", type=int, default=32)

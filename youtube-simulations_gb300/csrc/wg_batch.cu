@@ -175,20 +175,20 @@ static int entry_skew_k(const wg_batch *b, const BatchSlotHost &h)
 }
 
 // Tasks of the pass depth d for the scenes of depth class K (table entries), largest first
-// so that the ticket order balances the warps; each scene gets a share of one wave of
-// resident warps in proportion to its cells.
+// so that the ticket order balances the warps.  Row chunks are sized from the whole
+// list's work: about two tasks per resident warp (at least 32 rows), so that no single
+// chunk outlasts the rest of the pass; the short top and bottom segments fill the end.
 static void build_skew_tasks(const std::vector<const BatchSlotHost *> &hs, const std::vector<int> &entries, int d,
                              std::vector<int4> &out)
 {
-    long long cells = 0;
-    for (const BatchSlotHost *h : hs) cells += (long long)h->prm.nx * h->prm.ny;
-    const int cap = batch_skew_capacity(d);
+    const int F = 2 * d + 1;
+    double rows = 0.0;
+    for (const BatchSlotHost *h : hs) rows += (double)batch_skew_tiles(h->dp, d) * (h->prm.nx + 3 * F);
+    const int cap = std::max(1, batch_skew_capacity(d));
+    const int chunk = std::max(32, std::min(4096, (int)(rows / (2.0 * cap))));
     std::vector<int4> t;
     std::vector<float> cost;
-    for (size_t k = 0; k < hs.size(); k++) {
-        const double share = cells > 0 ? (double)hs[k]->prm.nx * hs[k]->prm.ny / (double)cells : 1.0;
-        batch_skew_plan(hs[k]->dp, entries[k], d, std::max(1, (int)(cap * share + 0.5)), t, cost);
-    }
+    for (size_t k = 0; k < hs.size(); k++) batch_skew_plan(hs[k]->dp, entries[k], d, chunk, t, cost);
     std::vector<int> ord(t.size());
     for (size_t k = 0; k < ord.size(); k++) ord[k] = (int)k;
     std::stable_sort(ord.begin(), ord.end(), [&](int x, int y) { return cost[x] > cost[y]; });

@@ -47,7 +47,9 @@ __host__ __device__ inline int batch_pass_depth(int n, int P, int q) { return n 
 // first column of the 128-column tile, rows i_s | i_e << 16, kind) from a ticket counter;
 // pass q of a frame reads the pair the previous pass wrote, toff updates after the frame start.
 int batch_skew_capacity(int K);
-void batch_skew_plan(const DevParams &p, int entry, int K, int cap, std::vector<int4> &tasks, std::vector<float> &cost);
+int batch_skew_tiles(const DevParams &p, int K);  // column tiles of a scene (shifted tiling)
+// tasks of one scene, inner row chunks of rows..2*rows rows
+void batch_skew_plan(const DevParams &p, int entry, int K, int rows, std::vector<int4> &tasks, std::vector<float> &cost);
 void launch_batch_skew(int K, const SlotDev *tab, const SlotDyn *dyn, const int4 *tasks, const int *ntasks, int *ticket,
                        int q, int toff, cudaStream_t st);
 bool batch_skew_ok(const wg_params &p, int prec);

@@ -275,6 +275,10 @@ __global__ void __launch_bounds__(256) k_step_tb(const __grid_constant__ DevPara
 // promises twospeeds and no FLOOR clamp, so every such cell takes the leapfrog update.
 // INL: oscillating values and source increments are computed here (batches) instead of
 // read from the per-call arrays; both are the same double values, rounded the same way.
+// Out of line: they are rare, and inlined copies per level would crowd the instruction cache.
+__device__ __noinline__ float osc_inl(const DevParams &p, long long t, int j) { return (float)osc_bc(p, (int)t, j); }
+__device__ __noinline__ double src_inl(const DevParams &p, long long t) { return point_source(p, t); }
+
 template <int COEF, bool GEN, bool PLAIN, bool INL = false>
 __device__ __forceinline__ float skew_cell(const DevParams &p, const TbArgs &a, int gi, int gj, int s, float x, float y,
                                            float n, float sv, float e, float w, float cc, float tcv, bool act)
@@ -293,9 +297,9 @@ __device__ __forceinline__ float skew_cell(const DevParams &p, const TbArgs &a, 
     const float tce = (COEF == WG_COEF_TABLE) ? tcv : (act ? a.courant : a.courantb);
     const Edge32K k{a.kappa, a.ks, a.kt, a.gs, a.gt, a.vmax};
     float v = edge32<true>(p, gi, gj, x, y, n, sv, e, w, ccv, tce, g, act, k, [&] {
-        return INL ? (float)osc_bc(p, (int)(a.t0 + s), gj) : a.osc[(size_t)(s - 1) * p.ny + gj];
+        return INL ? osc_inl(p, a.t0 + s, gj) : a.osc[(size_t)(s - 1) * p.ny + gj];
     });
-    if (p.src_on && gi == p.src_i && gj == p.src_j) v = (float)A_((double)v, INL ? point_source(p, a.t0 + s) : a.src[s - 1]);
+    if (p.src_on && gi == p.src_i && gj == p.src_j) v = (float)A_((double)v, INL ? src_inl(p, a.t0 + s) : a.src[s - 1]);
     return v;
 }
 
@@ -498,7 +502,7 @@ __device__ __forceinline__ void skew_strip(const DevParams &p, const TbArgs &a, 
                         v[3] = lf ? v[3] : res;
                     }
                     if (src_lane && r == p.src_i) {
-                        const double add = INL ? point_source(p, a.t0 + lv) : a.src[lv - 1];
+                        const double add = INL ? src_inl(p, a.t0 + lv) : a.src[lv - 1];
                         const int cs = p.src_j - gj0;
 #pragma unroll
                         for (int c = 0; c < 4; c++) v[c] = (cs == c) ? (float)A_((double)v[c], add) : v[c];
@@ -538,7 +542,7 @@ __device__ __forceinline__ void skew_strip(const DevParams &p, const TbArgs &a, 
                             v[3] = (c == 3) ? res : v[3];
                         }
                     } else if (src_lane && r == p.src_i) {  // the general rule adds it on rows 0 and nx-1
-                        const double add = INL ? point_source(p, a.t0 + lv) : a.src[lv - 1];
+                        const double add = INL ? src_inl(p, a.t0 + lv) : a.src[lv - 1];
                         const int cs = p.src_j - gj0;
 #pragma unroll
                         for (int c = 0; c < 4; c++) v[c] = (cs == c) ? (float)A_((double)v[c], add) : v[c];
@@ -749,8 +753,8 @@ static wg_status skew_tasks(wg_scene *s, int K, int L, const int4 **tasks, int *
 // ---------------------------------------------------------------------------
 // Skewed passes over a batch of scenes (mask coefficients, FP32).  Persistent warps take
 // tasks from a ticket counter: table entry, first column of the tile (shifted tiling),
-// rows i_s | i_e << 16, kind.  Each task's parameters and arguments are staged in the
-// warp's shared memory; pass q of a frame reads pair (pair ^ q) of the scene (with the
+// rows i_s | i_e << 16, kind.  The scene's parameters are staged in the warp's shared
+// memory.  Pass q of a frame reads pair (pair ^ q) of the scene (with the
 // scene's cur on the first pass, 0 after) and writes the other pair.  Oscillating values
 // and source increments are computed inline at update time + toff + level.
 // ---------------------------------------------------------------------------
@@ -765,11 +769,9 @@ __global__ void __launch_bounds__(128, 4) k_batch_skew(const SlotDev *__restrict
     using SL = SkewSlot<WG_COEF_MASK>;
     extern __shared__ float4 skew_smem[];
     __shared__ DevParams s_p[4];
-    __shared__ TbArgs s_a[4];
     const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
     float *ring = reinterpret_cast<float *>(skew_smem) + wid * SL::DEPTH * SL::SIZE;
     DevParams &p = s_p[wid];
-    TbArgs &a = s_a[wid];
     const int n = *ntasks;
     for (;;) {
         int t = 0;
@@ -777,42 +779,45 @@ __global__ void __launch_bounds__(128, 4) k_batch_skew(const SlotDev *__restrict
         t = __shfl_sync(0xffffffffu, t, 0);
         if (t >= n) break;  // warp-uniform
         const int4 w = tasks[t];
+        // the scene's parameters are staged in the warp's shared memory; the pass
+        // arguments are built by every lane (the same values)
         const SlotDev &sd = tab[w.x];
         __syncwarp();  // every lane is done with the previous task's parameters
-        const int *src = reinterpret_cast<const int *>(&sd.p);
-        int *dst = reinterpret_cast<int *>(&p);
-        for (int k = lane; k < (int)(sizeof(DevParams) / 4); k += 32) dst[k] = src[k];
-        if (lane == 0) {
-            const SlotDyn dy = dyn[sd.slot];
-            const int pin = dy.pair ^ (q & 1), cin = q == 0 ? dy.cur : 0, pout = pin ^ 1;
-            a.phi = (const float *)sd.f[2 * pin + cin];
-            a.psi = (const float *)sd.f[2 * pin + 1 - cin];
-            a.phi_out = (float *)sd.f[2 * pout];
-            a.psi_out = (float *)sd.f[2 * pout + 1];
-            a.act = sd.act;
-            a.tcc = a.tc = nullptr;
-            a.c2 = (float)sd.p.c2;
-            a.c2b = (float)sd.p.c2b;
-            a.gam = (float)sd.p.gam;
-            a.gamb = (float)sd.p.gamb;
-            a.kappa = (float)sd.p.kappa;
-            a.ks = (float)sd.p.kappa_sides;
-            a.kt = (float)sd.p.kappa_topbot;
-            a.gs = (float)sd.p.gamma_sides;
-            a.gt = (float)sd.p.gamma_topbot;
-            a.vmax = (float)sd.p.vmax;
-            a.courant = (float)sd.p.courant;
-            a.courantb = (float)sd.p.courantb;
-            a.t0 = dy.time + toff;
-            a.osc = nullptr;
-            a.src = nullptr;
-            a.err = nullptr;
+        {
+            const int *src = reinterpret_cast<const int *>(&sd.p);
+            int *dst = reinterpret_cast<int *>(&p);
+            for (int k = lane; k < (int)(sizeof(DevParams) / 4); k += 32) dst[k] = src[k];
         }
         __syncwarp();
+        const SlotDyn dy = dyn[sd.slot];
+        const int pin = dy.pair ^ (q & 1), cin = q == 0 ? dy.cur : 0, pout = pin ^ 1;
+        TbArgs a;
+        a.phi = (const float *)sd.f[2 * pin + cin];
+        a.psi = (const float *)sd.f[2 * pin + 1 - cin];
+        a.phi_out = (float *)sd.f[2 * pout];
+        a.psi_out = (float *)sd.f[2 * pout + 1];
+        a.act = sd.act;
+        a.tcc = a.tc = nullptr;
+        a.c2 = (float)sd.p.c2;
+        a.c2b = (float)sd.p.c2b;
+        a.gam = (float)sd.p.gam;
+        a.gamb = (float)sd.p.gamb;
+        a.kappa = (float)sd.p.kappa;
+        a.ks = (float)sd.p.kappa_sides;
+        a.kt = (float)sd.p.kappa_topbot;
+        a.gs = (float)sd.p.gamma_sides;
+        a.gt = (float)sd.p.gamma_topbot;
+        a.vmax = (float)sd.p.vmax;
+        a.courant = (float)sd.p.courant;
+        a.courantb = (float)sd.p.courantb;
+        a.t0 = dy.time + toff;
+        a.osc = nullptr;
+        a.src = nullptr;
+        a.err = nullptr;
         const int i_s = w.z & 0xFFFF, i_e = (int)((unsigned)w.z >> 16);
         const int gjs = w.y, gj0 = gjs + 4 * lane;
         const int lo = gjs <= 0 ? 0 : gjs + H;
-        const int hi = gjs + 128 >= p.ny ? p.ny : gjs + 128 - H;
+        const int hi = gjs + 128 >= sd.p.ny ? sd.p.ny : gjs + 128 - H;
         if (w.w == 2) skew_strip<WG_COEF_MASK, K, false, true, true>(p, a, i_s, i_e, gj0, lane, ring, true, lo, hi);
         else skew_strip<WG_COEF_MASK, K, false, false, true>(p, a, i_s, i_e, gj0, lane, ring, w.w == 1, lo, hi);
     }
@@ -830,6 +835,12 @@ static int batch_skew_cap_k()
         per_sm = nb > 0 ? nb : 1;
     }
     return per_sm * sm_count() * 4;
+}
+
+int batch_skew_tiles(const DevParams &p, int K)
+{
+    const int step = 128 - 2 * ((K + 3) & ~3);
+    return 1 + std::max(0, (p.ny - 128 + step - 1) / step);
 }
 
 int batch_skew_capacity(int K)
@@ -865,10 +876,10 @@ bool batch_skew_ok(const wg_params &p, int prec)
            p.ny >= 8 && p.nx >= 2 && p.nx <= 0xFFFF;
 }
 
-void batch_skew_plan(const DevParams &p, int entry, int K, int cap, std::vector<int4> &tasks, std::vector<float> &cost)
+void batch_skew_plan(const DevParams &p, int entry, int K, int rows, std::vector<int4> &tasks, std::vector<float> &cost)
 {
     const int H = (K + 3) & ~3, step = 128 - 2 * H, F = 2 * K + 1;
-    const std::vector<int4> v = skew_plan(p, K, 32, cap, true);
+    const std::vector<int4> v = skew_plan(p, K, rows, 1 << 30, true);  // inner chunks of rows..2 rows rows
     for (const int4 &t : v) {
         tasks.push_back(make_int4(entry, t.x * step, (int)((unsigned)t.y | ((unsigned)t.z << 16)), t.w));
         cost.push_back((float)((t.z - t.y + F) * (t.w ? SKEW_EDGE_COST : 1.0)));

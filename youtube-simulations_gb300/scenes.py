@@ -187,3 +187,20 @@ def batch_member(rng, smin=(256, 256), smax=(1280, 720), bconds=(BC_DIRICHLET, B
     _, _, xc, yc = seeded_point_inside(rng, p, xy)
     phi = pulse(p, xy, xc, yc, variance=0.05 ** 2)
     return Scene(p, phi, phi.copy(), xy, tcc, tc, tg, meta=dict(shape=shape))
+
+
+def sweep_member(rng, smin=128, smax=512):
+    """One instance of the parameter-sweep batch: nx and ny log-uniform between smin and
+    smax, a rectangle domain (the whole box) with 1-3 seeded circular obstacles of
+    radius U(0.1, 0.3), absorbing boundary, GAMMA U(0, 1e-3), COURANT U(0.05, 0.2), one
+    Gaussian pulse at a seeded point inside, psi = phi."""
+    nx = int(round(math.exp(rng.uniform(math.log(smin), math.log(smax)))))
+    ny = int(round(math.exp(rng.uniform(math.log(smin), math.log(smax)))))
+    p = make_params(nx, ny, b_cond=BC_ABSORBING, courant=float(rng.uniform(0.05, 0.2)),
+                    gamma=float(rng.uniform(0.0, 1e-3)))
+    discs = seeded_discs(rng, int(rng.integers(1, 4)), 0.1, 0.3, box=(-1.6, 1.6, -0.8, 0.8))
+    xy = mask(p, D_CIRCLES, circles=discs)
+    _, _, xc, yc = seeded_point_inside(rng, p, xy, margin=2)
+    phi = pulse(p, xy, xc, yc, variance=0.05 ** 2)
+    return Scene(p, phi, phi.copy(), xy, None, None, None, meta=dict(discs=discs))
+
