@@ -364,7 +364,7 @@ def run_batch(args, P, scenes, W, stream, rank):
     import torch
     rng = np.random.default_rng(1000 + rank)
     members = [scenes.batch_member(rng) for _ in range(args.batch_instances)]
-    out = {}
+    out, prec_depths = {}, {}
     for prec in ("fp32", "fp64"):
         b = W.Batch(P.FP32 if prec == "fp32" else P.FP64, stream=stream.cuda_stream)
         for m in members:
@@ -385,11 +385,17 @@ def run_batch(args, P, scenes, W, stream, rank):
         e_check = b.energy(0)
         out[prec] = {"value": cells * 10 * frames / (ms / 1e3) / 1e9, "unit": METRIC, "ms_per_frame": ms / frames,
                      "gpu_launches": b.launches() - l0, "frames": frames}
+        if prec == "fp32":
+            depths, _ = b.skew_depths()
+            prec_depths = {f"2^{c + 10}..2^{c + 11} cells": depths[c] for c in range(16) if depths[c]}
         b.close()
     out["instances"] = n_active
     out["cells"] = cells
     out["workload"] = ("uneven batch: 256 instances log-uniform 256x256..1280x720, mixed masks, Dirichlet/periodic, "
-                       "one persistent kernel per update over a tile work queue, frame of 10 updates as a CUDA graph")
+                       "frame of 10 updates as a CUDA graph: FP32 Dirichlet scenes in skewed passes at the depth tuned "
+                       "per size class, the rest one persistent kernel per update over a tile work queue")
+    if prec_depths:
+        out["fp32"]["depth_per_size_class"] = prec_depths
     out["energy_check_instance0"] = e_check
     return out
 
