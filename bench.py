@@ -356,21 +356,29 @@ def run_ours(args):
     return 0
 
 
+def tuned_blocking(b):
+    """The batch autotuner's choice per size class: skewed depth and row chunk."""
+    depths, rows, _ = b.skew_tuning()
+    return {f"2^{c + 10}..2^{c + 11} cells": {"depth": depths[c], "chunk_rows": rows[c] or "list-wide"}
+            for c in range(16) if depths[c]}
+
+
 def run_batch(args, P, scenes, W, stream, rank):
     """Uneven batch: 256 seeded instances, sizes log-uniform between 256x256 and
     1280x720, ellipse/stadium/polygon/disc-array masks, Dirichlet or periodic 50/50,
-    COURANT U(0.05, 0.15), one pulse each; frames of 10 updates replayed as CUDA graphs."""
+    COURANT U(0.05, 0.15), one pulse each; frames of 10 updates replayed as CUDA graphs,
+    3 warm-up frames and `--batch-frames` timed frames in FP32 and in FP64.  The FP64
+    energy check: every instance's energy after the run, FP32 against FP64."""
     import numpy as np
     import torch
     rng = np.random.default_rng(1000 + rank)
     members = [scenes.batch_member(rng) for _ in range(args.batch_instances)]
-    out, prec_depths = {}, {}
+    out, prec_depths, energies = {}, {}, {}
+    frames = args.batch_frames
     for prec in ("fp32", "fp64"):
         b = W.Batch(P.FP32 if prec == "fp32" else P.FP64, stream=stream.cuda_stream)
-        for m in members:
-            b.add(m.params, m.phi, m.psi, m.xy)
+        slots = [b.add(m.params, m.phi, m.psi, m.xy) for m in members]
         n_active, cells = b.count()
-        frames = args.batch_frames if prec == "fp32" else max(2, args.batch_frames // 5)
         for _ in range(3):
             b.step(10)
         torch.cuda.synchronize()
@@ -382,21 +390,24 @@ def run_batch(args, P, scenes, W, stream, rank):
         e1.record(stream)
         e1.synchronize()
         ms = e0.elapsed_time(e1)
-        e_check = b.energy(0)
+        energies[prec] = np.array([b.energy(s) for s in slots])
         out[prec] = {"value": cells * 10 * frames / (ms / 1e3) / 1e9, "unit": METRIC, "ms_per_frame": ms / frames,
                      "gpu_launches": b.launches() - l0, "frames": frames}
         if prec == "fp32":
-            depths, _ = b.skew_depths()
-            prec_depths = {f"2^{c + 10}..2^{c + 11} cells": depths[c] for c in range(16) if depths[c]}
+            prec_depths = tuned_blocking(b)
         b.close()
     out["instances"] = n_active
     out["cells"] = cells
+    out["updates"] = 10 * (frames + 3)
     out["workload"] = ("uneven batch: 256 instances log-uniform 256x256..1280x720, mixed masks, Dirichlet/periodic, "
                        "frame of 10 updates as a CUDA graph: FP32 Dirichlet scenes in skewed passes at the depth tuned "
                        "per size class, the rest one persistent kernel per update over a tile work queue")
     if prec_depths:
-        out["fp32"]["depth_per_size_class"] = prec_depths
-    out["energy_check_instance0"] = e_check
+        out["fp32"]["blocking_per_size_class"] = prec_depths
+    rel = np.abs(energies["fp32"] - energies["fp64"]) / np.maximum(np.abs(energies["fp64"]), 1e-300)
+    out["energy_check"] = {"against": "FP64 batch after the same updates (FP64-compensated energy sums)",
+                           "max_rel_diff": float(rel.max()), "median_rel_diff": float(np.median(rel)),
+                           "instance0_fp32": float(energies["fp32"][0]), "instance0_fp64": float(energies["fp64"][0])}
     return out
 
 
@@ -430,9 +441,7 @@ def run_sweep(args, P, scenes, W, stream, rank):
         out[prec] = {"value": cells * 10 * (frames - 3) / (ms / 1e3) / 1e9, "unit": METRIC,
                      "ms_per_frame": ms / (frames - 3), "gpu_launches": b.launches() - l0}
         if prec == "fp32":
-            depths, tune = b.skew_depths()
-            out["fp32"]["depth_per_size_class"] = {
-                f"2^{c + 10}..2^{c + 11} cells": depths[c] for c in range(16) if depths[c]}
+            out["fp32"]["blocking_per_size_class"] = tuned_blocking(b)
         fields[prec] = [b.download(s)[0] for s in slots]
         b.close()
     err = np.array([np.max(np.abs(a - b)) for a, b in zip(fields["fp32"], fields["fp64"])])
@@ -453,7 +462,8 @@ def run_serving(args, P, scenes, W, stream, rank):
     """Serving loop under a stated load: requests with sizes log-uniform between 256x256
     and 2560x1440 and U(50, 500) frames of 10 updates each arrive as a seeded Poisson
     process (rate per tick); the server admits them under a 150 GB HBM budget into the
-    running batch and returns a turbo-style RGB8 frame per scene per tick."""
+    running batch and returns a turbo-style RGB8 frame per scene per tick.  The same
+    request stream is served in FP32 and in plain FP64."""
     import numpy as np
     rng = np.random.default_rng(2000 + rank)
     lut = np.random.default_rng(5).integers(0, 256, size=(256, 3), dtype=np.uint8)
@@ -464,29 +474,34 @@ def run_serving(args, P, scenes, W, stream, rank):
         m = scenes.batch_member(rng, smin=(256, 256), smax=(2560, 1440))
         frames = int(rng.integers(args.serve_frames_min, args.serve_frames_max + 1))
         reqs.append((m, frames))
-    out = {}
-    srv = W.Server(lut, precision=P.FP32, steps_per_frame=10, hbm_budget=150 << 30, stream=stream.cuda_stream)
-    t0 = time.perf_counter()
-    tick, k = 0, 0
-    while k < n_req or srv.stats()["completed"] < n_req:
-        while k < n_req and arrivals[k] <= tick:
-            m, frames = reqs[k]
-            srv.submit(m.params, m.phi, m.psi, m.xy, frames)
-            k += 1
-        srv.tick()
-        tick += 1
-    wall = time.perf_counter() - t0
-    st = srv.stats()
-    srv.close()
-    out = {"frame_latency_p50_ms": st["frame_latency_p50_ms"], "frame_latency_p99_ms": st["frame_latency_p99_ms"],
-           "frame_latency_max_ms": st["frame_latency_max_ms"], "first_frame_p50_ms": st["first_frame_p50_ms"],
-           "first_frame_p99_ms": st["first_frame_p99_ms"], "frames": st["frames"], "ticks": st["ticks"],
-           "value": st["cell_updates"] / st["busy_seconds"] / 1e9, "unit": METRIC, "dtype": "f32",
-           "bytes_peak": st["bytes_peak"], "wall_s": wall,
-           "load": f"{n_req} requests, Poisson arrivals at {args.serve_rate} per tick, sizes log-uniform "
+    res = {}
+    for prec in ("fp32", "fp64"):
+        srv = W.Server(lut, precision=P.FP32 if prec == "fp32" else P.FP64, steps_per_frame=10,
+                       hbm_budget=150 << 30, stream=stream.cuda_stream)
+        t0 = time.perf_counter()
+        tick, k = 0, 0
+        while k < n_req or srv.stats()["completed"] < n_req:
+            while k < n_req and arrivals[k] <= tick:
+                m, frames = reqs[k]
+                srv.submit(m.params, m.phi, m.psi, m.xy, frames)
+                k += 1
+            srv.tick()
+            tick += 1
+        wall = time.perf_counter() - t0
+        st = srv.stats()
+        srv.close()
+        res[prec] = {"frame_latency_p50_ms": st["frame_latency_p50_ms"], "frame_latency_p99_ms": st["frame_latency_p99_ms"],
+                     "frame_latency_max_ms": st["frame_latency_max_ms"], "first_frame_p50_ms": st["first_frame_p50_ms"],
+                     "first_frame_p99_ms": st["first_frame_p99_ms"], "frames": st["frames"], "ticks": st["ticks"],
+                     "value": st["cell_updates"] / st["busy_seconds"] / 1e9, "unit": METRIC,
+                     "bytes_peak": st["bytes_peak"], "wall_s": wall}
+    out = dict(res["fp32"])
+    out["dtype"] = "f32"
+    out["fp64"] = res["fp64"]
+    out["load"] = (f"{n_req} requests, Poisson arrivals at {args.serve_rate} per tick, sizes log-uniform "
                    f"256x256..2560x1440, U({args.serve_frames_min},{args.serve_frames_max}) frames of 10 updates, "
-                   "150 GB budget, RGB8 frames (size 2) to host each tick",
-           "latency": "per frame: tick start to every resident scene's RGB8 frame in host memory"}
+                   "150 GB budget, RGB8 frames (size 2) to host each tick")
+    out["latency"] = "per frame: tick start to every resident scene's RGB8 frame in host memory"
     return out
 
 
@@ -557,7 +572,7 @@ def main():
     ap.add_argument("--sweep-instances", type=int, default=4096)
     ap.add_argument("--sweep-steps", type=int, default=2000)
     ap.add_argument("--batch-instances", type=int, default=256)
-    ap.add_argument("--batch-frames", type=int, default=20)
+    ap.add_argument("--batch-frames", type=int, default=497)
     ap.add_argument("--serve-requests", type=int, default=32)
     ap.add_argument("--serve-rate", type=float, default=0.25)
     ap.add_argument("--serve-frames-min", type=int, default=50)

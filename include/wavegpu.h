@@ -335,12 +335,15 @@ wg_status wg_batch_remove(wg_batch *b, int32_t slot);
  * nsteps >= 2, skewed passes of 2..6 updates at the depth of their size class; both
  * give the same fields bit for bit. */
 wg_status wg_batch_step(wg_batch *b, int32_t nsteps);
-/* Skewed passes: mode -1 (default) tunes a depth per size class (floor(log2(cells)) - 10,
- * 16 classes) at the first frame that needs it; 0 turns them off; 2..6 fixes the depth. */
+/* Skewed passes: mode -1 (default) tunes a depth and a row chunk per size class
+ * (floor(log2(cells)) - 10, 16 classes) at the first frame that needs it; 0 turns them
+ * off; 2..6 fixes the depth. */
 wg_status wg_batch_set_skew(wg_batch *b, int32_t mode);
-/* depths[16]: the depth of each size class (0: not tuned / none); ms_per_update[16*8]
- * (optional): the autotuner's time per update of class c at depth K, [c*8 + K]. */
-wg_status wg_batch_skew_depths(wg_batch *b, int32_t *depths, double *ms_per_update);
+/* depths[16]: the depth of each size class (0: not tuned / none); chunk_rows[16]
+ * (optional): the tuned rows of a task's row chunk (0: sized from the whole list's work);
+ * ms_per_update[16*8] (optional): the autotuner's best time per update of class c at
+ * depth K, [c*8 + K]. */
+wg_status wg_batch_skew_depths(wg_batch *b, int32_t *depths, int32_t *chunk_rows, double *ms_per_update);
 wg_status wg_batch_download(wg_batch *b, int32_t slot, double *phi, double *psi);
 wg_status wg_batch_energy(wg_batch *b, int32_t slot, double *total);
 wg_status wg_batch_count(wg_batch *b, int32_t *n_active, int64_t *cells);

@@ -1,5 +1,5 @@
 """Skewed passes in FP32 batches (k_batch_skew): frames of 2..6-update passes over many
-scenes, written between two buffer pairs, at a depth fixed or tuned per size class.
+scenes, written between two buffer pairs, at a depth (and row chunk) fixed or tuned per size class.
 
 The skewed cells are the single-update cells, so every scene must come out bit for bit
 as with the skewed passes off and as a native scene on the single-step kernels: over
@@ -86,8 +86,8 @@ def run_batch(mode, ms, frames):
                 b.remove(slots.pop(2))
         for k, sl in slots.items():
             out[k] = (b.download(sl), done[k])
-        depths, _ = b.skew_depths()
-    return out, depths
+        depths, rows, _ = b.skew_tuning()
+    return out, (depths, rows)
 
 
 @pytest.fixture(scope="module")
@@ -110,7 +110,7 @@ def test_single_updates_match_native_scenes(members, unskewed):
 
 @pytest.mark.parametrize("mode", [2, 3, 4, 5, 6, -1])
 def test_skewed_passes_bit_identical(mode, members, unskewed):
-    out, depths = run_batch(mode, members, FRAMES)
+    out, (depths, rows) = run_batch(mode, members, FRAMES)
     assert out.keys() == unskewed.keys()
     for k in out:
         (phi, psi), n = out[k]
@@ -125,6 +125,7 @@ def test_skewed_passes_bit_identical(mode, members, unskewed):
             c = min(15, max(0, int(np.floor(np.log2(nx * ny))) - 10))
             if bc != P.BC_PERIODIC and ny >= 8:
                 assert 2 <= depths[c] <= 6, (c, depths)
+                assert rows[c] in (0, 32, 64, 128, 256), (c, rows)
 
 
 def test_energy_after_skewed_frames_matches(members):

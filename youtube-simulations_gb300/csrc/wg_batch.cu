@@ -175,11 +175,12 @@ static int entry_skew_k(const wg_batch *b, const BatchSlotHost &h)
 }
 
 // Tasks of the pass depth d for the scenes of depth class K (table entries), largest first
-// so that the ticket order balances the warps.  Row chunks are sized from the whole
-// list's work: about two tasks per resident warp (at least 32 rows), so that no single
-// chunk outlasts the rest of the pass; the short top and bottom segments fill the end.
-static void build_skew_tasks(const std::vector<const BatchSlotHost *> &hs, const std::vector<int> &entries, int d,
-                             std::vector<int4> &out)
+// so that the ticket order balances the warps.  Row chunks: the rows tuned for the scene's
+// size class, or (untuned, fixed depth) sized from the whole list's work, about two tasks
+// per resident warp (at least 32 rows), so that no single chunk outlasts the rest of the
+// pass; the short top and bottom segments fill the end.  force_rows > 0 overrides both.
+static void build_skew_tasks(const wg_batch *b, const std::vector<const BatchSlotHost *> &hs,
+                             const std::vector<int> &entries, int d, std::vector<int4> &out, int force_rows = 0)
 {
     const int F = 2 * d + 1;
     double rows = 0.0;
@@ -188,7 +189,10 @@ static void build_skew_tasks(const std::vector<const BatchSlotHost *> &hs, const
     const int chunk = std::max(32, std::min(4096, (int)(rows / (2.0 * cap))));
     std::vector<int4> t;
     std::vector<float> cost;
-    for (size_t k = 0; k < hs.size(); k++) batch_skew_plan(hs[k]->dp, entries[k], d, chunk, t, cost);
+    for (size_t k = 0; k < hs.size(); k++) {
+        const int tuned = b->skew_mode < 0 ? b->class_rows[hs[k]->cls] : 0;
+        batch_skew_plan(hs[k]->dp, entries[k], d, force_rows > 0 ? force_rows : (tuned > 0 ? tuned : chunk), t, cost);
+    }
     std::vector<int> ord(t.size());
     for (size_t k = 0; k < ord.size(); k++) ord[k] = (int)k;
     std::stable_sort(ord.begin(), ord.end(), [&](int x, int y) { return cost[x] > cost[y]; });
@@ -217,7 +221,7 @@ static wg_status build_list(wg_batch *b, int K, int d, const std::vector<int> &t
         }
     }
     std::vector<int4> tasks;
-    build_skew_tasks(hs, entries, d, tasks);
+    build_skew_tasks(b, hs, entries, d, tasks);
     if ((int)tasks.size() > L.cap) {
         if (L.dev) cudaFree(L.dev);
         L.dev = nullptr;
@@ -412,9 +416,11 @@ static void batch_enqueue_frame(wg_batch *b, int n, bool skewed)
     k_batch_advance<<<(cap + 255) / 256, 256, 0, b->st>>>(b->d_hdr, b->d_tab, b->d_dyn, n, skewed ? 1 : 0);
 }
 
-// Depth per size class: each candidate depth times one skewed pass over the class's
-// scenes (reading their current fields, writing the other pair, so the state does not
-// change) and the fastest per update is kept.
+// Depth and row chunk per size class, in two stages: depths 2..6 with the list-wide
+// chunk, then chunks of 32, 64, 128 and 256 rows at the best depth.  Each candidate
+// times one skewed pass over the class's scenes (reading their current fields, writing
+// the other pair, so the state does not change); the fastest per update is kept.  Nine
+// short passes per class keep the tuning frame of a server tick short.
 static wg_status batch_autotune(wg_batch *b)
 {
     bool tuned = false;
@@ -434,13 +440,16 @@ static wg_status batch_autotune(wg_batch *b)
         cudaEvent_t e0, e1;
         WG_CUDA(cudaEventCreate(&e0));
         WG_CUDA(cudaEventCreate(&e1));
-        int best = 0;
+        int best = 0, best_rows = 0;
         double best_ms = 1e30;
         int4 *dev = nullptr;
         cudaError_t err = cudaSuccess;
-        for (int K = 2; K <= WG_SKEW_MAX_K && err == cudaSuccess; K++) {
+        static const int ROWS[] = {32, 64, 128, 256};
+        const int ndepth = WG_SKEW_MAX_K - 1;
+        for (int cand = 0; cand < ndepth + 4 && err == cudaSuccess; cand++) {
+            const int K = cand < ndepth ? 2 + cand : best, R = cand < ndepth ? 0 : ROWS[cand - ndepth];
             std::vector<int4> tasks;
-            build_skew_tasks(hs, entries, K, tasks);
+            build_skew_tasks(b, hs, entries, K, tasks, R);
             const int nt = (int)tasks.size();
             err = cudaMallocAsync((void **)&dev, sizeof(int4) * std::max(nt, 1), b->st);
             if (err == cudaSuccess && nt) err = cudaMemcpyAsync(dev, tasks.data(), sizeof(int4) * nt, cudaMemcpyHostToDevice, b->st);
@@ -462,16 +471,18 @@ static wg_status batch_autotune(wg_batch *b)
             dev = nullptr;
             if (err == cudaSuccess) err = cudaStreamSynchronize(b->st);  // tasks outlives its copy
             const double per = ms / (reps * K);
-            b->tune_ms[c * 8 + K] = per;
+            if (R == 0 || per < b->tune_ms[c * 8 + K]) b->tune_ms[c * 8 + K] = per;
             if (per < best_ms) {
                 best_ms = per;
                 best = K;
+                best_rows = R;
             }
         }
         cudaEventDestroy(e0);
         cudaEventDestroy(e1);
         if (err != cudaSuccess) return cuda_fail(err, "batch autotune");
         b->class_k[c] = best;
+        b->class_rows[c] = best_rows;
         tuned = true;
     }
     if (tuned) return batch_refresh_table(b);
@@ -679,11 +690,12 @@ wg_status wg_batch_set_skew(wg_batch *b, int32_t mode)
     return batch_refresh_table(b);
 }
 
-wg_status wg_batch_skew_depths(wg_batch *b, int32_t *depths, double *ms_per_update)
+wg_status wg_batch_skew_depths(wg_batch *b, int32_t *depths, int32_t *chunk_rows, double *ms_per_update)
 {
     if (!b || !depths) { set_error("NULL argument"); return WG_ERR_INVALID; }
     for (int c = 0; c < BATCH_CLASSES; c++) {
         depths[c] = b->skew_mode >= 0 ? b->skew_mode : b->class_k[c];
+        if (chunk_rows) chunk_rows[c] = b->skew_mode >= 0 ? 0 : b->class_rows[c];
         if (ms_per_update)
             for (int K = 0; K < 8; K++)
                 ms_per_update[c * 8 + K] = b->tune_ms.empty() ? 0.0 : b->tune_ms[c * 8 + K];

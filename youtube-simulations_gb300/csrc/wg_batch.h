@@ -100,6 +100,7 @@ struct wg_batch {
     // skewed passes
     int skew_mode = -1;                                   // -1 autotuned per size class, 0 off, 2..6 fixed
     int class_k[wg::BATCH_CLASSES] = {0};                 // tuned depth per size class (0: not yet)
+    int class_rows[wg::BATCH_CLASSES] = {0};              // tuned row chunk per size class (0: list-wide size)
     std::map<std::pair<int, int>, BatchSkewList> lists;   // (depth class, pass depth) -> tasks
     int *d_skew_n = nullptr, *d_ticket = nullptr;        // task counts; tickets of a frame's passes
     int skew_n_cap = 0, ticket_cap = 0;

@@ -97,7 +97,7 @@ SIGNATURES = {
     "wg_batch_count": (_I32, [_V, ctypes.POINTER(_I32), ctypes.POINTER(_I64)]),
     "wg_batch_launch_count": (_I32, [_V, ctypes.POINTER(_I64)]),
     "wg_batch_set_skew": (_I32, [_V, _I32]),
-    "wg_batch_skew_depths": (_I32, [_V, ctypes.POINTER(_I32), ctypes.POINTER(ctypes.c_double)]),
+    "wg_batch_skew_depths": (_I32, [_V, ctypes.POINTER(_I32), ctypes.POINTER(_I32), ctypes.POINTER(ctypes.c_double)]),
     "wg_server_create": (_I32, [_V, _V, ctypes.POINTER(_V)]),
     "wg_server_destroy": (_I32, [_V]),
     "wg_server_submit": (_I32, [_V, _V, _V, _V, _V, _I32, _I32, ctypes.POINTER(_I64)]),
@@ -470,10 +470,16 @@ class Batch:
     def skew_depths(self):
         """(depth per size class [16], autotuner ms per update [16, 8] by class and depth);
         size class = floor(log2(cells)) - 10, clamped to 0..15."""
+        d, _, ms = self.skew_tuning()
+        return d, ms
+
+    def skew_tuning(self):
+        """(depth [16], row chunk [16] (0: list-wide size), ms per update [16, 8]) per size class."""
         d = (_I32 * 16)()
+        r = (_I32 * 16)()
         ms = (ctypes.c_double * 128)()
-        check(lib().wg_batch_skew_depths(self.h, d, ms))
-        return list(d), np.array(ms[:]).reshape(16, 8)
+        check(lib().wg_batch_skew_depths(self.h, d, r, ms))
+        return list(d), list(r), np.array(ms[:]).reshape(16, 8)
 
     def download(self, slot):
         if slot not in self.params:  # let the library report the unknown slot
