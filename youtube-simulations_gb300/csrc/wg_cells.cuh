@@ -67,17 +67,21 @@ __device__ __forceinline__ void vstore(T *ptr, const T (&v)[Vec<T>::n])
     *reinterpret_cast<typename Vec<T>::type *>(ptr) = t;
 }
 
-// FP32 boundary-line cell of a mirror or absorbing scene by edge32 (the rule of the
-// tiled and skewed FP32 steppers), neighbours read from the current level.
+// FP32 boundary-line cell of a mirror, periodic or absorbing scene by edge32 (the rule of
+// the tiled and skewed FP32 steppers), neighbours read from the current level (wrapped
+// around the grid for periodic scenes).
 template <int COEF>
 __device__ inline float fast_edge32(const DevParams &p, const FastArgs<float> &a, int i, int j, long long time, float y)
 {
     const size_t o = (size_t)i * p.pitch + j;
+    const bool per = p.b_cond == WG_BC_PERIODIC;
+    const int ip = (i + 1 < p.nx) ? i + 1 : (per ? 0 : i), im = (i > 0) ? i - 1 : (per ? p.nx - 1 : i);
+    const int jp = (j + 1 < p.ny) ? j + 1 : (per ? 0 : j), jm = (j > 0) ? j - 1 : (per ? p.ny - 1 : j);
     const float x = a.phi[o];
-    const float n = (i + 1 < p.nx) ? a.phi[o + p.pitch] : x;
-    const float sv = (i > 0) ? a.phi[o - p.pitch] : x;
-    const float e = (j + 1 < p.ny) ? a.phi[o + 1] : x;
-    const float w = (j > 0) ? a.phi[o - 1] : x;
+    const float n = a.phi[(size_t)ip * p.pitch + j];
+    const float sv = a.phi[(size_t)im * p.pitch + j];
+    const float e = a.phi[(size_t)i * p.pitch + jp];
+    const float w = a.phi[(size_t)i * p.pitch + jm];
     const bool act = ActBits{a.act, p.wpitch}(i, j);
     float ccv, tcv, g;
     if (COEF == WG_COEF_TABLE) {
@@ -107,7 +111,7 @@ template <int COEF> struct Edge32Path<float, COEF> {
     static __device__ __forceinline__ bool run(const DevParams &p, const FastArgs<float> &a, int i, int j, long long time,
                                                float y, float *out)
     {
-        if (p.b_cond != WG_BC_DIRICHLET && p.b_cond != WG_BC_ABSORBING) return false;
+        if (p.b_cond != WG_BC_DIRICHLET && p.b_cond != WG_BC_ABSORBING && p.b_cond != WG_BC_PERIODIC) return false;
         *out = fast_edge32<COEF>(p, a, i, j, time, y);
         return true;
     }
@@ -118,7 +122,7 @@ template <int COEF> struct Edge32Path<float, COEF> {
 template <class T, int COEF>
 __device__ inline T fast_edge(const DevParams &p, const FastArgs<T> &a, int i, int j, long long time, T y)
 {
-    T r;  // FP32 mirror / absorbing scenes: the FP32 rule
+    T r;  // FP32 mirror, periodic and absorbing scenes: the FP32 rule
     if (Edge32Path<T, COEF>::run(p, a, i, j, time, y, &r)) return r;
     Field<T> PHI{a.phi, p.pitch}, PSI{a.psi, p.pitch};
     ActBits ACT{a.act, p.wpitch}, NZ{a.nz, p.wpitch};

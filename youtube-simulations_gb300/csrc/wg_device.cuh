@@ -175,13 +175,14 @@ __device__ __forceinline__ bool left_bc(const DevParams &p, int j)
     return p.osc_left && j < p.ny - 1 && j > p.bc_jmin && j < p.bc_jmax;
 }
 
-// FP32 boundary-line cell (rows 0 and nx-1, columns 0 and ny-1) for mirror ("Dirichlet")
-// and absorbing boundaries: edge_cell's rules (below) in the FP32 increment form of
-// upd32 / absorb32, the neighbours the reference mirrors replaced by the cell itself.
-// x, y: phi and psi of the cell; n, sv, e, w: phi at i+1, i-1, j+1, j-1 (any value where
-// outside the grid); ccv, tcv, g: the cell's tcc, tc and tgamma; osc(): the oscillating
-// value.  Returns y where the reference writes nothing.  CLAMP: FLOOR on written cells
-// with act.  Every FP32 stepper (single updates, tiles, skewed passes) uses this rule.
+// FP32 boundary-line cell (rows 0 and nx-1, columns 0 and ny-1) for mirror ("Dirichlet"),
+// periodic and absorbing boundaries: edge_cell's rules (below) in the FP32 increment form
+// of upd32 / absorb32, the neighbours the reference mirrors replaced by the cell itself.
+// x, y: phi and psi of the cell; n, sv, e, w: phi at i+1, i-1, j+1, j-1 (wrapped around
+// the grid for periodic scenes; any value where outside the grid otherwise); ccv, tcv, g:
+// the cell's tcc, tc and tgamma; osc(): the oscillating value.  Returns y where the
+// reference writes nothing.  CLAMP: FLOOR on written cells with act.  Every FP32 stepper
+// (single updates, tiles, skewed passes) uses this rule.
 struct Edge32K {
     float kappa, ks, kt, gs, gt, vmax;
 };
@@ -202,6 +203,8 @@ __device__ __forceinline__ float edge32(const DevParams &p, int gi, int gj, floa
             if (bi1) n = x;
             if (bi0) sv = x;
             if (bj1) e = x; else w = x;
+        } else if (p.b_cond == WG_BC_PERIODIC) {
+            // the 5-point rule with the wrapped neighbours as given
         } else {
             mode = 1;
             nb = bj1 ? w : e;
@@ -213,6 +216,8 @@ __device__ __forceinline__ float edge32(const DevParams &p, int gi, int gj, floa
             mode = 2;
         } else if (p.b_cond == WG_BC_DIRICHLET) {
             if (bi0) sv = x; else n = x;
+        } else if (p.b_cond == WG_BC_PERIODIC) {
+            // the 5-point rule with the wrapped neighbours as given
         } else {
             mode = 1;
             nb = bi0 ? n : sv;
