@@ -98,6 +98,23 @@ def dist_env():
     return rank, world, local
 
 
+def max_over_ranks(t_ms, world, device):
+    """The job's time: the slowest rank's (one all-reduce MAX; every rank gets it)."""
+    if world <= 1:
+        return t_ms
+    import torch
+    import torch.distributed as dist
+    tt = torch.tensor([t_ms], dtype=torch.float64, device=device)
+    dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+    return float(tt.item())
+
+
+def whole_job_rate(world, cells, updates, t_ms):
+    """Gcell-updates/s of the whole job: every rank advances its own replica of `cells`
+    cells by `updates` updates, in the slowest rank's time t_ms."""
+    return world * cells * updates / (t_ms / 1e3) / 1e9
+
+
 # ---------------------------------------------------------------------------
 # Reference arm: the reference's own CPU stepper
 # ---------------------------------------------------------------------------
@@ -226,16 +243,12 @@ def run_ours(args):
         k, ti, tj = s.blocking()
         finals[prec] = s.download()[0]
         s.close()
-        t_ms = step_ms + energy_ms
-        if world > 1:
-            tt = torch.tensor([t_ms], device=dev)
-            torch.distributed.all_reduce(tt, op=torch.distributed.ReduceOp.MAX)
-            t_ms = float(tt.item())
+        t_ms = max_over_ranks(step_ms + energy_ms, world, dev)
         updates = args.steps * UPDATES_PER_STEP
         main_launches = args.steps * (UPDATES_PER_STEP // k if k > 1 else UPDATES_PER_STEP)
         per_launch_s = step_ms / 1e3 / main_launches
         algo = bytes_per_cell_update(prec, "table") * CELLS * max(k, 1)
-        results[prec] = dict(value=world * CELLS * updates / (t_ms / 1e3) / 1e9, ms=t_ms / args.steps,
+        results[prec] = dict(value=whole_job_rate(world, CELLS, updates, t_ms), ms=t_ms / args.steps,
                              step_ms=step_ms, energy_ms=energy_ms, wall=wall, launches=launches, clocks=ck,
                              blocking=(k, ti, tj), achieved_gbs=algo / per_launch_s / 1e9, per_launch_s=per_launch_s,
                              bytes_per_update=bytes_per_cell_update(prec, "table"), energies=energies)
@@ -278,11 +291,8 @@ def run_ours(args):
         e2e_ms += e0.elapsed_time(e1)
     s.close()
     barrier()
-    if world > 1:
-        tt = torch.tensor([e2e_ms], device=dev)
-        torch.distributed.all_reduce(tt, op=torch.distributed.ReduceOp.MAX)
-        e2e_ms = float(tt.item())
-    e2e_value = world * CELLS * args.e2e_steps * UPDATES_PER_STEP / (e2e_ms / 1e3) / 1e9
+    e2e_ms = max_over_ranks(e2e_ms, world, dev)
+    e2e_value = whole_job_rate(world, CELLS, args.e2e_steps * UPDATES_PER_STEP, e2e_ms)
 
     batch_res = run_batch(args, P, scenes, W, stream, rank) if not args.no_batch else None
     sweep_res = run_sweep(args, P, scenes, W, stream, rank) if not args.no_sweep else None
