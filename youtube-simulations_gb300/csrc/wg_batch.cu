@@ -143,6 +143,70 @@ __global__ void __launch_bounds__(256, 4) k_batch_step(const BatchHdr *__restric
     }
 }
 
+// Ghost cells of the input pair of pass q for the wrapped scenes of depth class K (K < 0:
+// every wrapped scene, the current pair): each ghost cell of both fields takes the value of
+// the real cell it wraps to.  Ghost cells are written and real cells read, so blocks need
+// no ordering.  Block (x, y): table entry x, a share y of its ghost cells.
+__global__ void k_batch_ghosts(const BatchHdr *__restrict__ hdr, const SlotDev *__restrict__ tab,
+                               const SlotDyn *__restrict__ dyn, int K, int q)
+{
+    const int e = blockIdx.x;
+    if (e >= hdr->nactive) return;
+    const SlotDev &sd = tab[e];
+    if (!sd.wrap || (K >= 0 && sd.skew_k != K)) return;
+    const SlotDyn dy = dyn[sd.slot];
+    const int pin = K < 0 ? dy.pair : dy.pair ^ (q & 1);
+    float *f0 = (float *)sd.f[2 * pin], *f1 = (float *)sd.f[2 * pin + 1];
+    const int nx = sd.p.nx, ny = sd.p.ny, pitch = sd.p.pitch;
+    constexpr int GC = BATCH_GHOST_COLS, GR = BATCH_GHOST_ROWS;
+    const int wide = ny + 2 * GC, ncol = 2 * GC * nx, total = ncol + 2 * GR * wide;
+    for (int t = blockIdx.y * blockDim.x + threadIdx.x; t < total; t += gridDim.y * blockDim.x) {
+        int i, j;
+        if (t < ncol) {  // the ghost columns of the real rows
+            i = t / (2 * GC);
+            const int g = t - i * 2 * GC;
+            j = g < GC ? g - GC : ny + g - GC;
+        } else {  // the ghost rows, over the extended width
+            const int u = t - ncol, rg = u / wide;
+            j = u - rg * wide - GC;
+            i = rg < GR ? rg - GR : nx + rg - GR;
+        }
+        const int si = ((i % nx) + nx) % nx, sj = ((j % ny) + ny) % ny;
+        const long long d = (long long)i * pitch + j, s = (long long)si * pitch + sj;
+        f0[d] = f0[s];
+        f1[d] = f1[s];
+    }
+}
+
+// The ghost words and rows of a wrapped scene's active plane: one thread per word of rows
+// -BATCH_GHOST_ROWS..nx+BATCH_GHOST_ROWS-1, words -1..(ny+BATCH_GHOST_COLS-1)/32; a bit of a
+// real cell keeps its value, a bit of a ghost cell takes the bit of the cell it wraps to.
+__global__ void k_act_ghosts(uint32_t *act, int wpitch, int nx, int ny)
+{
+    constexpr int GC = BATCH_GHOST_COLS, GR = BATCH_GHOST_ROWS;
+    const int w = (int)(blockIdx.x * blockDim.x + threadIdx.x) - 1;
+    const int i = (int)blockIdx.y - GR;
+    if (w > (ny + GC - 1) / 32 || i >= nx + GR) return;
+    const bool real_row = i >= 0 && i < nx;
+    if (real_row && w >= 0 && 32 * w + 31 < ny) return;  // all real cells
+    const long long base = (long long)i * wpitch + w;
+    uint32_t v = 0;
+    for (int bit = 0; bit < 32; bit++) {
+        const int j = 32 * w + bit;
+        uint32_t x;
+        if (real_row && j >= 0 && j < ny) {
+            x = (act[base] >> bit) & 1u;
+        } else if (j >= -GC && j < ny + GC) {
+            const int si = ((i % nx) + nx) % nx, sj = ((j % ny) + ny) % ny;
+            x = (act[(long long)si * wpitch + (sj >> 5)] >> (sj & 31)) & 1u;
+        } else {
+            x = 0;
+        }
+        v |= x << bit;
+    }
+    act[base] = v;
+}
+
 // skewed: the frame ran the skewed passes of the scenes with a depth class
 __global__ void k_batch_advance(const BatchHdr *__restrict__ hdr, const SlotDev *__restrict__ tab,
                                 SlotDyn *__restrict__ dyn, int n, int skewed)
@@ -167,6 +231,27 @@ using namespace wg;
 namespace wg {
 
 static void batch_drop_graphs(wg_batch *b);
+
+BatchLayout batch_layout(const wg_params &p, int prec)
+{
+    BatchLayout L;
+    const int esz = prec == WG_FP32 ? 4 : 8;
+    if (batch_wrap_ok(p, prec)) {  // ghost columns, ghost rows, one ghost mask word per row
+        L.pitch = pitch_for(p.ny + 2 * BATCH_GHOST_COLS + 64, esz);
+        const size_t rows = (size_t)p.nx + 2 * BATCH_GHOST_ROWS, wpitch = (L.pitch + 31) / 32;
+        L.field_bytes = rows * L.pitch * esz;
+        L.mask_bytes = rows * wpitch * 4;
+        L.field_off = (size_t)BATCH_GHOST_ROWS * L.pitch + BATCH_GHOST_COLS;
+        L.mask_off = (size_t)BATCH_GHOST_ROWS * wpitch + 1;
+    } else {
+        L.pitch = pitch_for(p.ny, esz);
+        const size_t wpitch = (L.pitch + 31) / 32;
+        L.field_bytes = (size_t)p.nx * L.pitch * esz;
+        L.mask_bytes = (size_t)p.nx * wpitch * 4;
+        L.field_off = L.mask_off = 0;
+    }
+    return L;
+}
 
 static int entry_skew_k(const wg_batch *b, const BatchSlotHost &h)
 {
@@ -244,7 +329,7 @@ wg_status batch_refresh_table(wg_batch *b)
     std::vector<SlotDev> tab;
     std::vector<int> tab_slot;
     std::vector<int4> items;
-    int base = 0, plain = 0, nskew = 0;
+    int base = 0, plain = 0, nskew = 0, nwrap = 0;
     long long cells = 0;
     unsigned sig = 0;
     // scenes without skewed passes first: their items are the first plain_tiles
@@ -262,6 +347,7 @@ wg_status batch_refresh_table(wg_batch *b)
             d.nz = h.nz;
             d.slot = k;
             d.skew_k = sk;
+            d.wrap = h.wrap ? 1 : 0;
             d.tiles_j = (h.dp.pitch / V + BT_THREADS - 1) / BT_THREADS;
             const int tiles_i = (h.prm.nx + BT_ROWS - 1) / BT_ROWS;
             d.ntiles = tiles_i * d.tiles_j;
@@ -273,6 +359,7 @@ wg_status batch_refresh_table(wg_batch *b)
             if (sk > 0) {
                 sig |= 1u << sk;
                 nskew++;
+                if (h.wrap) nwrap++;
             } else {
                 plain = base;
             }
@@ -281,6 +368,7 @@ wg_status batch_refresh_table(wg_batch *b)
         }
     }
     if (plain > 0) sig |= 1u;
+    if (nwrap > 0) sig |= 1u << 8;  // ghost refreshes in the branches
     if ((int)tab.size() > b->tab_cap) {
         if (b->d_tab) cudaFree(b->d_tab);
         b->d_tab = nullptr;
@@ -312,6 +400,7 @@ wg_status batch_refresh_table(wg_batch *b)
     b->total_cells = cells;
     b->plain_tiles = plain;
     b->skew_scenes = nskew;
+    b->wrap_scenes = nwrap;
     b->tab_slot = tab_slot;
     // the task lists in use follow the new table
     std::vector<std::pair<int, int>> keys;
@@ -399,6 +488,8 @@ static void batch_enqueue_frame(wg_batch *b, int n, bool skewed)
             for (int q = 0; q < P; q++) {
                 const int d = batch_pass_depth(n, P, q);
                 const BatchSkewList &L = b->lists.at({K, d});
+                if (b->graph_sig & (1u << 8))  // the wrapped scenes' ghosts of this pass's input pair
+                    k_batch_ghosts<<<dim3(std::max(b->tab_cap, 1), 8), 256, 0, ss>>>(b->d_hdr, b->d_tab, b->d_dyn, K, q);
                 launch_batch_skew(d, b->d_tab, b->d_dyn, L.dev, b->d_skew_n + L.index, b->d_ticket + ti++, q, toff, ss);
                 toff += d;
             }
@@ -423,7 +514,7 @@ static void batch_enqueue_frame(wg_batch *b, int n, bool skewed)
 // short passes per class keep the tuning frame of a server tick short.
 static wg_status batch_autotune(wg_batch *b)
 {
-    bool tuned = false;
+    bool tuned = false, ghosts = false;
     for (int c = 0; c < BATCH_CLASSES; c++) {
         if (b->class_k[c]) continue;
         std::vector<const BatchSlotHost *> hs;
@@ -437,6 +528,11 @@ static wg_status batch_autotune(wg_batch *b)
         }
         if (hs.empty()) continue;
         if (b->tune_ms.empty()) b->tune_ms.assign(BATCH_CLASSES * 8, 0.0);
+        if (!ghosts) {  // the wrapped scenes' ghosts of their current pair, read by the timed passes
+            k_batch_ghosts<<<dim3(std::max(b->nactive, 1), 8), 256, 0, b->st>>>(b->d_hdr, b->d_tab, b->d_dyn, -1, 0);
+            b->launches++;
+            ghosts = true;
+        }
         cudaEvent_t e0, e1;
         WG_CUDA(cudaEventCreate(&e0));
         WG_CUDA(cudaEventCreate(&e1));
@@ -537,7 +633,7 @@ wg_status wg_batch_destroy(wg_batch *b)
     batch_drop_graphs(b);
     for (auto &h : b->slots) {
         if (!h.used) continue;
-        void *ptrs[] = {h.f[0], h.f[1], h.f[2], h.f[3], h.act, h.nz, h.ebot, h.etop, h.eout};
+        void *ptrs[] = {h.mem[0], h.mem[1], h.mem[2], h.mem[3], h.act_mem, h.nz_mem, h.ebot, h.etop, h.eout};
         for (void *p : ptrs) if (p) cudaFree(p);
     }
     for (auto &kv : b->lists) if (kv.second.dev) cudaFree(kv.second.dev);
@@ -570,27 +666,33 @@ wg_status wg_batch_add(wg_batch *b, const wg_params *p, const double *phi, const
     BatchSlotHost &h = b->slots[k];
     h = BatchSlotHost();
     h.prm = *p;
-    const int pitch = pitch_for(p->ny, (int)b->esz);
-    h.dp = make_dev_params(*p, pitch);
     h.skew = batch_skew_ok(*p, b->prec);
+    h.wrap = batch_wrap_ok(*p, b->prec);
+    const BatchLayout L = batch_layout(*p, b->prec);
+    const int pitch = L.pitch;
+    h.dp = make_dev_params(*p, pitch);
     {
         const double cells = (double)p->nx * p->ny;
         h.cls = std::min(BATCH_CLASSES - 1, std::max(0, (int)std::floor(std::log2(cells)) - 10));
     }
-    const size_t fb = (size_t)p->nx * pitch * b->esz, mb = (size_t)p->nx * h.dp.wpitch * 4;
+    const size_t fb = L.field_bytes, mb = L.mask_bytes;
     cudaError_t e = cudaSuccess;
     const int nf = h.skew ? 4 : 2;  // the second pair takes the skewed passes' output
-    for (int q = 0; q < nf && e == cudaSuccess; q++) e = cudaMallocAsync(&h.f[q], fb, b->st);
-    for (int q = 2; q < nf && e == cudaSuccess; q++) e = cudaMemsetAsync(h.f[q], 0, fb, b->st);
-    if (e == cudaSuccess) e = cudaMallocAsync((void **)&h.act, mb, b->st);
-    if (e == cudaSuccess) e = cudaMallocAsync((void **)&h.nz, mb, b->st);
+    for (int q = 0; q < nf && e == cudaSuccess; q++) e = cudaMallocAsync(&h.mem[q], fb, b->st);
+    for (int q = (h.wrap ? 0 : 2); q < nf && e == cudaSuccess; q++) e = cudaMemsetAsync(h.mem[q], 0, fb, b->st);
+    if (e == cudaSuccess) e = cudaMallocAsync((void **)&h.act_mem, mb, b->st);
+    if (e == cudaSuccess) e = cudaMallocAsync((void **)&h.nz_mem, mb, b->st);
+    if (e == cudaSuccess && h.wrap) e = cudaMemsetAsync(h.act_mem, 0, mb, b->st);
+    for (int q = 0; q < nf; q++) h.f[q] = h.mem[q] ? (char *)h.mem[q] + L.field_off * b->esz : nullptr;
+    h.act = h.act_mem ? h.act_mem + L.mask_off : nullptr;
+    h.nz = h.nz_mem ? h.nz_mem + L.mask_off : nullptr;
     if (e == cudaSuccess) e = cudaMallocAsync((void **)&h.ebot, p->nx * sizeof(double2), b->st);
     if (e == cudaSuccess) e = cudaMallocAsync((void **)&h.etop, p->nx * sizeof(double2), b->st);
     if (e == cudaSuccess) e = cudaMallocAsync((void **)&h.eout, (p->nx + 8) * sizeof(double), b->st);
     void *stage = nullptr;
     if (e == cudaSuccess) e = cudaMallocAsync(&stage, n * sizeof(double), b->st);
     if (e != cudaSuccess) {
-        void *ptrs[] = {h.f[0], h.f[1], h.f[2], h.f[3], h.act, h.nz, h.ebot, h.etop, h.eout, stage};
+        void *ptrs[] = {h.mem[0], h.mem[1], h.mem[2], h.mem[3], h.act_mem, h.nz_mem, h.ebot, h.etop, h.eout, stage};
         for (void *q : ptrs) if (q) cudaFreeAsync(q, b->st);
         h = BatchSlotHost();
         return cuda_fail(e, "wg_batch_add");
@@ -599,6 +701,11 @@ wg_status wg_batch_add(wg_batch *b, const wg_params *p, const double *phi, const
     // mask planes, then the two fields (FP64 host values rounded on the device)
     WG_CUDA(cudaMemcpyAsync(stage, xy, n * sizeof(int16_t), cudaMemcpyHostToDevice, b->st));
     launch_pack_mask(p->nx, p->ny, h.dp.wpitch, (const int16_t *)stage, h.act, h.nz, b->st);
+    if (h.wrap) {  // the mask's ghost words and rows, once (the mask does not change)
+        const int words = (p->ny + BATCH_GHOST_COLS + 31) / 32 + 1, rows = p->nx + 2 * BATCH_GHOST_ROWS;
+        k_act_ghosts<<<dim3((words + 63) / 64, rows), 64, 0, b->st>>>(h.act, h.dp.wpitch, p->nx, p->ny);
+        b->launches++;
+    }
     const double *src[2] = {phi, psi};
     for (int q = 0; q < 2; q++) {
         WG_CUDA(cudaMemcpyAsync(stage, src[q], n * sizeof(double), cudaMemcpyHostToDevice, b->st));
@@ -641,7 +748,7 @@ wg_status wg_batch_remove(wg_batch *b, int32_t slot)
     BatchSlotHost &h = b->slots[slot];
     h.used = false;
     wg_status st = batch_refresh_table(b);  // the kernels stop seeing the slot first
-    void *ptrs[] = {h.f[0], h.f[1], h.f[2], h.f[3], h.act, h.nz, h.ebot, h.etop, h.eout};
+    void *ptrs[] = {h.mem[0], h.mem[1], h.mem[2], h.mem[3], h.act_mem, h.nz_mem, h.ebot, h.etop, h.eout};
     for (void *p : ptrs) if (p) WG_CUDA(cudaFreeAsync(p, b->st));
     h = BatchSlotHost();
     return st;
@@ -672,7 +779,7 @@ wg_status wg_batch_step(wg_batch *b, int32_t nsteps)
     long long n = 1;  // the advance kernel
     if (!skewed || (b->graph_sig & 1u)) n += nsteps;
     if (skewed)
-        for (int K : batch_groups(b)) n += batch_passes(nsteps, K);
+        for (int K : batch_groups(b)) n += batch_passes(nsteps, K) * ((b->graph_sig & (1u << 8)) ? 2 : 1);
     b->launches += n;
     return WG_OK;
 }

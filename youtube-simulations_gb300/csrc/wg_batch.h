@@ -17,7 +17,8 @@ struct __align__(16) SlotDev {   // one entry of the compact table of active sce
     int slot;                    // index into the per-slot dynamic state
     int tiles_j, tile_base, ntiles;
     int skew_k;                  // depth class of the scene's skewed passes; 0: single updates only
-    int pad_[3];
+    int wrap;                    // periodic scene in the ghost layout (skewed passes read wrapped halos)
+    int pad_[2];
 };
 struct SlotDyn {
     long long time;
@@ -30,6 +31,15 @@ struct BatchHdr {
 };
 
 constexpr int BATCH_CLASSES = 16;   // size classes: floor(log2(cells)) - 10, clamped to 0..15
+
+// Ghost layout of a periodic scene taking skewed passes: every field row carries
+// BATCH_GHOST_COLS copies of the opposite side's columns on each side, and the field
+// BATCH_GHOST_ROWS copies of the opposite rows above row 0 and below row nx-1, so that a
+// pass reads its wrapped halo as ordinary neighbours.  The scene's pointers address cell
+// (0, 0); the ghosts sit at negative offsets and in the row padding.  Mask planes carry one
+// ghost word on the left of every row and the same ghost rows.
+constexpr int BATCH_GHOST_COLS = 8;   // the widest column halo of a pass (depth 5..6)
+constexpr int BATCH_GHOST_ROWS = 7;   // the deepest row halo of a pass (depth 6 + 1)
 constexpr int BATCH_GROUPS = WG_SKEW_MAX_K + 1;
 
 // Skewed passes of a frame of n updates with depth class K: P passes of n/P or n/P+1
@@ -53,8 +63,16 @@ void batch_skew_plan(const DevParams &p, int entry, int K, int rows, std::vector
 void launch_batch_skew(int K, const SlotDev *tab, const SlotDyn *dyn, const int4 *tasks, const int *ntasks, int *ticket,
                        int q, int toff, cudaStream_t st);
 bool batch_skew_ok(const wg_params &p, int prec);
+bool batch_wrap_ok(const wg_params &p, int prec);   // periodic scenes the skewed passes take (ghost layout)
 
 wg_status batch_refresh_table(::wg_batch *b);
+
+struct BatchLayout {            // device layout of one batch scene
+    int pitch;                  // elements per field row
+    size_t field_bytes, mask_bytes;  // one field, one mask plane
+    size_t field_off, mask_off;      // cell (0, 0) within the allocation (elements, words)
+};
+BatchLayout batch_layout(const wg_params &p, int prec);
 
 }  // namespace wg
 
@@ -63,11 +81,14 @@ struct BatchSlotHost {
     wg_params prm;
     wg::DevParams dp;
     void *f[4] = {nullptr, nullptr, nullptr, nullptr};  // f[2], f[3]: second pair of skewed scenes
+    void *mem[4] = {nullptr, nullptr, nullptr, nullptr};  // the allocations behind f (ghost layout: f is inside)
+    uint32_t *act_mem = nullptr, *nz_mem = nullptr;
     uint32_t *act = nullptr, *nz = nullptr;
     double2 *ebot = nullptr, *etop = nullptr;
     double *eout = nullptr;
     size_t bytes = 0;
     bool skew = false;      // FP32 scene whose boundaries the skewed passes cover
+    bool wrap = false;      // periodic, in the ghost layout
     int cls = 0;            // size class
 };
 
@@ -107,7 +128,7 @@ struct wg_batch {
     cudaStream_t side[wg::BATCH_GROUPS] = {};             // one branch per depth class in a frame
     cudaEvent_t ev_fork = nullptr, ev_join[wg::BATCH_GROUPS] = {};
     unsigned graph_sig = 0;                               // depth classes present (bit K), plain chain (bit 0)
-    int plain_tiles = 0, skew_scenes = 0;
+    int plain_tiles = 0, skew_scenes = 0, wrap_scenes = 0;
     std::vector<int> tab_slot;                            // slot of each table entry
     int *d_tune_ticket = nullptr;                         // tickets of the autotuner's passes
     std::vector<double> tune_ms;                          // last autotune: ms per update, [class * 8 + K]

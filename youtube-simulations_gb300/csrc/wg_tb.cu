@@ -385,7 +385,10 @@ template <int COEF> struct SkewSlot {
 // a multiple of 4, or of the point source (fix = true), all away from rows 0 and nx-1.
 // GEN = true (fix = true): the others, with the general rule on rows 0 and nx-1.
 // Columns [lo, hi) of the tile are stored (lo, hi multiples of 4 but for hi = ny).
-template <int COEF, int K, bool PLAIN, bool GEN, bool INL = false>
+// WRAP: a periodic scene in the ghost layout (batches): rows -BATCH_GHOST_ROWS..nx +
+// BATCH_GHOST_ROWS - 1 and columns -BATCH_GHOST_COLS..ny + BATCH_GHOST_COLS - 1 hold the
+// wrapped field, so every cell takes the bulk rule and no edge rule applies.
+template <int COEF, int K, bool PLAIN, bool GEN, bool INL = false, bool WRAP = false>
 __device__ __forceinline__ void skew_strip(const DevParams &p, const TbArgs &a, int i_s, int i_e, int gj0, int lane,
                                            float *ring, bool edge, int lo, int hi)
 {
@@ -419,13 +422,18 @@ __device__ __forceinline__ void skew_strip(const DevParams &p, const TbArgs &a, 
     // row m goes to slot (m - m0) % D; each lane copies, and later reads, only its own bytes
     auto issue = [&](int m, int slot) {
         float *b = ring + slot * SL::SIZE;
-        const bool ok = grp_ok && m >= 0 && m < p.nx;
-        const size_t o = ok ? (size_t)m * p.pitch + gj0 : 0;
+        const bool ok = WRAP ? (gj0 >= -BATCH_GHOST_COLS && gj0 < p.ny + BATCH_GHOST_COLS && m >= -BATCH_GHOST_ROWS &&
+                                m < p.nx + BATCH_GHOST_ROWS)
+                             : (grp_ok && m >= 0 && m < p.nx);
+        const long long o = ok ? (long long)m * p.pitch + gj0 : 0;
         const int n16 = ok ? 16 : 0;
         cp_async16(b + 4 * lane, a.phi + o, n16);
         cp_async16(b + SL::PSI + 4 * lane, a.psi + o, n16);
         if (COEF == WG_COEF_TABLE) cp_async16(b + SL::TCC + 4 * lane, a.tcc + o, n16);
-        if (NEED_ACT) cp_async4(b + SL::ACT + lane, a.act + (ok ? (size_t)m * p.wpitch + (gj0 >> 5) : 0), ok ? 4 : 0);
+        // mask word of the group: floor division, so that the ghost columns left of column 0
+        // read the row's ghost word (index -1)
+        if (NEED_ACT)
+            cp_async4(b + SL::ACT + lane, a.act + (ok ? (long long)m * p.wpitch + ((gj0 + 32) / 32 - 1) : 0), ok ? 4 : 0);
         if (need_tce) {
             const bool te = ok && ce >= 0 && a.tc;  // the table exists with an absorbing boundary
             cp_async4(b + SL::TCE + lane, te ? a.tc + o + (unsigned)ce : a.phi, te ? 4 : 0);
@@ -816,6 +824,11 @@ __global__ void __launch_bounds__(128, 4) k_batch_skew(const SlotDev *__restrict
         a.err = nullptr;
         const int i_s = w.z & 0xFFFF, i_e = (int)((unsigned)w.z >> 16);
         const int gjs = w.y, gj0 = gjs + 4 * lane;
+        if (w.w == 3) {  // periodic, ghost layout: a halo on both sides of every tile
+            const int lo = max(gjs + H, 0), hi = min(gjs + 128 - H, sd.p.ny);
+            skew_strip<WG_COEF_MASK, K, false, false, true, true>(p, a, i_s, i_e, gj0, lane, ring, false, lo, hi);
+            continue;
+        }
         const int lo = gjs <= 0 ? 0 : gjs + H;
         const int hi = gjs + 128 >= sd.p.ny ? sd.p.ny : gjs + 128 - H;
         if (w.w == 2) skew_strip<WG_COEF_MASK, K, false, true, true>(p, a, i_s, i_e, gj0, lane, ring, true, lo, hi);
@@ -840,6 +853,7 @@ static int batch_skew_cap_k()
 int batch_skew_tiles(const DevParams &p, int K)
 {
     const int step = 128 - 2 * ((K + 3) & ~3);
+    if (p.b_cond == WG_BC_PERIODIC) return (p.ny + step - 1) / step;  // halo on both sides of every tile
     return 1 + std::max(0, (p.ny - 128 + step - 1) / step);
 }
 
@@ -870,8 +884,15 @@ void launch_batch_skew(int K, const SlotDev *tab, const SlotDyn *dyn, const int4
     }
 }
 
+bool batch_wrap_ok(const wg_params &p, int prec)
+{
+    return prec == WG_FP32 && p.b_cond == WG_BC_PERIODIC && !p.bc_neumann && !p.src_on && !p.oscillate_left &&
+           !p.oscillate_topbot && p.ny >= 8 && p.nx >= 2 && p.nx <= 0xFFFF;
+}
+
 bool batch_skew_ok(const wg_params &p, int prec)
 {
+    if (batch_wrap_ok(p, prec)) return true;
     return prec == WG_FP32 && (p.b_cond == WG_BC_DIRICHLET || p.b_cond == WG_BC_ABSORBING) && !p.bc_neumann &&
            p.ny >= 8 && p.nx >= 2 && p.nx <= 0xFFFF;
 }
@@ -879,6 +900,17 @@ bool batch_skew_ok(const wg_params &p, int prec)
 void batch_skew_plan(const DevParams &p, int entry, int K, int rows, std::vector<int4> &tasks, std::vector<float> &cost)
 {
     const int H = (K + 3) & ~3, step = 128 - 2 * H, F = 2 * K + 1;
+    if (p.b_cond == WG_BC_PERIODIC) {  // ghost layout: every tile inner (kind 3), rows in chunks of rows..2 rows
+        const int tiles_j = (p.ny + step - 1) / step, nl = std::max(1, p.nx / std::max(rows, 1));
+        for (int tj = 0; tj < tiles_j; tj++)
+            for (int q = 0; q < nl; q++) {
+                const int i_s = (int)((long long)q * p.nx / nl), i_e = (int)((long long)(q + 1) * p.nx / nl);
+                if (i_s >= i_e) continue;
+                tasks.push_back(make_int4(entry, tj * step - H, (int)((unsigned)i_s | ((unsigned)i_e << 16)), 3));
+                cost.push_back((float)(i_e - i_s + F));
+            }
+        return;
+    }
     const std::vector<int4> v = skew_plan(p, K, rows, 1 << 30, true);  // inner chunks of rows..2 rows rows
     for (const int4 &t : v) {
         tasks.push_back(make_int4(entry, t.x * step, (int)((unsigned)t.y | ((unsigned)t.z << 16)), t.w));
