@@ -63,6 +63,13 @@ __device__ __forceinline__ float upd32(float x, float y, float cc, float delta, 
     float inc = fmaf(cc, delta, fmaf(-g, w, w) - kappa * x);
     return x + inc;
 }
+// upd32 with KAPPA = 0: the kappa*x term is then an exact zero, so leaving it out changes
+// at most the sign of a zero result, never a value.
+__device__ __forceinline__ float upd32_k0(float x, float y, float cc, float delta, float g)
+{
+    float w = x - y;
+    return x + fmaf(cc, delta, fmaf(-g, w, w));
+}
 __device__ __forceinline__ float absorb32(float x, float y, float tc, float nb, float k, float g)
 {
     return x - (tc * (x - nb) + k * x + g * (x - y));

@@ -279,12 +279,13 @@ __global__ void __launch_bounds__(256) k_step_tb(const __grid_constant__ DevPara
 __device__ __noinline__ float osc_inl(const DevParams &p, long long t, int j) { return (float)osc_bc(p, (int)t, j); }
 __device__ __noinline__ double src_inl(const DevParams &p, long long t) { return point_source(p, t); }
 
-template <int COEF, bool GEN, bool PLAIN, bool INL = false>
+template <int COEF, bool GEN, bool PLAIN, bool INL = false, bool KZ = false>
 __device__ __forceinline__ float skew_cell(const DevParams &p, const TbArgs &a, int gi, int gj, int s, float x, float y,
                                            float n, float sv, float e, float w, float cc, float tcv, bool act)
 {
     const float ccv = (COEF == WG_COEF_TABLE) ? cc : (act ? a.c2 : a.c2b);
     const float g = (COEF == WG_COEF_TABLE) ? a.gam : (act ? a.gam : a.gamb);
+    if (!GEN && PLAIN && KZ) return upd32_k0(x, y, ccv, ((n - x) + (sv - x)) + ((e - x) + (w - x)), g);
     if (!GEN && PLAIN) return upd32(x, y, ccv, ((n - x) + (sv - x)) + ((e - x) + (w - x)), a.kappa, g);
     if (!GEN) {
         float v = y;
@@ -388,7 +389,8 @@ template <int COEF> struct SkewSlot {
 // WRAP: a periodic scene in the ghost layout (batches): rows -BATCH_GHOST_ROWS..nx +
 // BATCH_GHOST_ROWS - 1 and columns -BATCH_GHOST_COLS..ny + BATCH_GHOST_COLS - 1 hold the
 // wrapped field, so every cell takes the bulk rule and no edge rule applies.
-template <int COEF, int K, bool PLAIN, bool GEN, bool INL = false, bool WRAP = false>
+// KZ (with PLAIN): KAPPA = 0, the bulk update without its kappa term.
+template <int COEF, int K, bool PLAIN, bool GEN, bool INL = false, bool WRAP = false, bool KZ = false>
 __device__ __forceinline__ void skew_strip(const DevParams &p, const TbArgs &a, int i_s, int i_e, int gj0, int lane,
                                            float *ring, bool edge, int lo, int hi)
 {
@@ -496,7 +498,7 @@ __device__ __forceinline__ void skew_strip(const DevParams &p, const TbArgs &a, 
                     const float e = (c < 3) ? Wc[c + 1 < 4 ? c + 1 : 3] : e3;
                     const float w = (c > 0) ? Wc[c > 0 ? c - 1 : 0] : w0;
                     const bool act = NEED_ACT ? ((aq >> (4 * lv + c)) & 1u) : true;
-                    v[c] = skew_cell<COEF, false, PLAIN, INL>(p, a, r, gj0 + c, lv, Wc[c], Yl[c], W[lv - 1][2][c],
+                    v[c] = skew_cell<COEF, false, PLAIN, INL, KZ>(p, a, r, gj0 + c, lv, Wc[c], Yl[c], W[lv - 1][2][c],
                                                          W[lv - 1][0][c], e, w, T[lv][c], 0.f, act);
                 }
                 if (!GEN && edge) {  // warp-uniform
@@ -589,8 +591,9 @@ __device__ __forceinline__ void skew_strip(const DevParams &p, const TbArgs &a, 
 
 // One warp per task: column tile tj (x), rows [i_s, i_e) (y, z), and its kind (w): 0 inner,
 // 1 column 0 / column ny-1 / point source, 2 rows 0 and nx-1 or a column ny-1 that is not
-// a group's last.  The task list fills one wave of resident warps.
-template <int COEF, int K, bool PLAIN>
+// a group's last.  The task list fills one wave of resident warps.  PL: 0 general, 1 PLAIN,
+// 2 PLAIN with KAPPA = 0.
+template <int COEF, int K, int PL>
 __global__ void __launch_bounds__(128, 4) k_step_skew(const __grid_constant__ DevParams p, const __grid_constant__ TbArgs a,
                                                       const int4 *__restrict__ tasks, int ntasks)
 {
@@ -603,8 +606,9 @@ __global__ void __launch_bounds__(128, 4) k_step_skew(const __grid_constant__ De
     const int4 t = tasks[warp];
     const int gj0 = t.x * STEP - H + 4 * lane;
     const int lo = t.x * STEP, hi = lo + STEP;  // the core columns of tile t.x
-    if (t.w == 2) skew_strip<COEF, K, PLAIN, true>(p, a, t.y, t.z, gj0, lane, ring, true, lo, hi);
-    else skew_strip<COEF, K, PLAIN, false>(p, a, t.y, t.z, gj0, lane, ring, t.w == 1, lo, hi);
+    constexpr bool PLAIN = PL >= 1, KZ = PL == 2;
+    if (t.w == 2) skew_strip<COEF, K, PLAIN, true, false, false, KZ>(p, a, t.y, t.z, gj0, lane, ring, true, lo, hi);
+    else skew_strip<COEF, K, PLAIN, false, false, false, KZ>(p, a, t.y, t.z, gj0, lane, ring, t.w == 1, lo, hi);
 }
 
 static bool skew_shape_ok(const DevParams &p, int K, int S)
@@ -624,38 +628,38 @@ static int sm_count()
     return n;
 }
 
-template <int COEF, int K, bool PLAIN>
+template <int COEF, int K, int PL>
 static int skew_capacity()
 {
     constexpr size_t smem = 4 * SkewSlot<COEF>::DEPTH * SkewSlot<COEF>::SIZE * sizeof(float);  // 4 warps
     static int per_sm = 0;
     if (!per_sm) {
-        cudaFuncSetAttribute(k_step_skew<COEF, K, PLAIN>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        cudaFuncSetAttribute(k_step_skew<COEF, K, PL>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
         int nb = 0;
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_step_skew<COEF, K, PLAIN>, 128, smem);
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_step_skew<COEF, K, PL>, 128, smem);
         per_sm = nb > 0 ? nb : 1;
     }
     return per_sm * sm_count() * 4;
 }
 
-template <int COEF, int K, bool PLAIN>
+template <int COEF, int K, int PL>
 static void launch_skew_k(const DevParams &p, const TbArgs &a, const int4 *tasks, int ntasks, cudaStream_t st)
 {
     constexpr size_t smem = 4 * SkewSlot<COEF>::DEPTH * SkewSlot<COEF>::SIZE * sizeof(float);
-    skew_capacity<COEF, K, PLAIN>();  // sets the shared-memory attribute once
-    k_step_skew<COEF, K, PLAIN><<<(ntasks + 3) / 4, 128, smem, st>>>(p, a, tasks, ntasks);
+    skew_capacity<COEF, K, PL>();  // sets the shared-memory attribute once
+    k_step_skew<COEF, K, PL><<<(ntasks + 3) / 4, 128, smem, st>>>(p, a, tasks, ntasks);
 }
 
-template <int COEF, bool PLAIN>
+template <int COEF, int PL>
 static int skew_dispatch(const DevParams &p, const TbArgs *a, int K, const int4 *tasks, int ntasks, cudaStream_t st)
 {
     // a == nullptr: return the number of resident warps instead of launching
     switch (K) {
-    case 2: if (!a) return skew_capacity<COEF, 2, PLAIN>(); launch_skew_k<COEF, 2, PLAIN>(p, *a, tasks, ntasks, st); break;
-    case 3: if (!a) return skew_capacity<COEF, 3, PLAIN>(); launch_skew_k<COEF, 3, PLAIN>(p, *a, tasks, ntasks, st); break;
-    case 4: if (!a) return skew_capacity<COEF, 4, PLAIN>(); launch_skew_k<COEF, 4, PLAIN>(p, *a, tasks, ntasks, st); break;
-    case 5: if (!a) return skew_capacity<COEF, 5, PLAIN>(); launch_skew_k<COEF, 5, PLAIN>(p, *a, tasks, ntasks, st); break;
-    default: if (!a) return skew_capacity<COEF, 6, PLAIN>(); launch_skew_k<COEF, 6, PLAIN>(p, *a, tasks, ntasks, st); break;
+    case 2: if (!a) return skew_capacity<COEF, 2, PL>(); launch_skew_k<COEF, 2, PL>(p, *a, tasks, ntasks, st); break;
+    case 3: if (!a) return skew_capacity<COEF, 3, PL>(); launch_skew_k<COEF, 3, PL>(p, *a, tasks, ntasks, st); break;
+    case 4: if (!a) return skew_capacity<COEF, 4, PL>(); launch_skew_k<COEF, 4, PL>(p, *a, tasks, ntasks, st); break;
+    case 5: if (!a) return skew_capacity<COEF, 5, PL>(); launch_skew_k<COEF, 5, PL>(p, *a, tasks, ntasks, st); break;
+    default: if (!a) return skew_capacity<COEF, 6, PL>(); launch_skew_k<COEF, 6, PL>(p, *a, tasks, ntasks, st); break;
     }
     return 0;
 }
@@ -663,11 +667,15 @@ static int skew_dispatch(const DevParams &p, const TbArgs *a, int K, const int4 
 static int skew_call(const DevParams &p, const TbArgs *a, int coef, int K, const int4 *tasks, int ntasks, cudaStream_t st)
 {
     const bool plain = p.twospeeds && !p.floor_clamp;
-    if (coef == WG_COEF_TABLE)
-        return plain ? skew_dispatch<WG_COEF_TABLE, true>(p, a, K, tasks, ntasks, st)
-                     : skew_dispatch<WG_COEF_TABLE, false>(p, a, K, tasks, ntasks, st);
-    return plain ? skew_dispatch<WG_COEF_MASK, true>(p, a, K, tasks, ntasks, st)
-                 : skew_dispatch<WG_COEF_MASK, false>(p, a, K, tasks, ntasks, st);
+    const int pl = !plain ? 0 : (p.kappa == 0.0 ? 2 : 1);
+    if (coef == WG_COEF_TABLE) {
+        if (pl == 2) return skew_dispatch<WG_COEF_TABLE, 2>(p, a, K, tasks, ntasks, st);
+        return pl ? skew_dispatch<WG_COEF_TABLE, 1>(p, a, K, tasks, ntasks, st)
+                  : skew_dispatch<WG_COEF_TABLE, 0>(p, a, K, tasks, ntasks, st);
+    }
+    if (pl == 2) return skew_dispatch<WG_COEF_MASK, 2>(p, a, K, tasks, ntasks, st);
+    return pl ? skew_dispatch<WG_COEF_MASK, 1>(p, a, K, tasks, ntasks, st)
+              : skew_dispatch<WG_COEF_MASK, 0>(p, a, K, tasks, ntasks, st);
 }
 
 // Task list of a skewed pass.  Every column tile is cut into a top and a bottom segment
