@@ -392,7 +392,7 @@ template <int COEF> struct SkewSlot {
 // KZ (with PLAIN): KAPPA = 0, the bulk update without its kappa term.
 template <int COEF, int K, bool PLAIN, bool GEN, bool INL = false, bool WRAP = false, bool KZ = false>
 __device__ __forceinline__ void skew_strip(const DevParams &p, const TbArgs &a, int i_s, int i_e, int gj0, int lane,
-                                           float *ring, bool edge, int lo, int hi)
+                                           float *ring, float *tring, bool edge, int lo, int hi)
 {
     using SL = SkewSlot<COEF>;
     constexpr int D = SL::DEPTH;
@@ -409,13 +409,15 @@ __device__ __forceinline__ void skew_strip(const DevParams &p, const TbArgs &a, 
 
     float W[K + 1][3][4];  // W[s][k][c] = level s at row m-s-2+k, column gj0+c
     float Yp[4];           // psi(t-1) at row m-1
-    float T[K + 1][4];     // tcc at rows m, m-1, ..., m-K
+    // tcc at rows m, m-1, ..., m-K (table scenes): the warp's shared ring tring of K+1 rows
+    // (slot ts holds row m), each lane writing and reading back only its own 16 bytes
+    int ts = 0;
     float TE[K + 1];       // tc of the lane's boundary column at the same rows (edge tiles, table)
     uint32_t aq = 0;       // bits 4d..4d+3 = active bits of row m-d
 #pragma unroll
     for (int q = 0; q <= K; q++) {
 #pragma unroll
-        for (int c = 0; c < 4; c++) { W[q][0][c] = W[q][1][c] = W[q][2][c] = 0.f; T[q][c] = 0.f; }
+        for (int c = 0; c < 4; c++) { W[q][0][c] = W[q][1][c] = W[q][2][c] = 0.f; }
         TE[q] = 0.f;
     }
 #pragma unroll
@@ -461,7 +463,7 @@ __device__ __forceinline__ void skew_strip(const DevParams &p, const TbArgs &a, 
             const float tein = need_tce ? b[SL::TCE + lane] : 0.f;
             const float xin[4] = {xq.x, xq.y, xq.z, xq.w};
             const float yin[4] = {yq.x, yq.y, yq.z, yq.w};
-            const float cin[4] = {cq.x, cq.y, cq.z, cq.w};
+            if (COEF == WG_COEF_TABLE) *reinterpret_cast<float4 *>(tring + ts * 128 + 4 * lane) = cq;
             if (NEED_ACT) aq = (aq << 4) | ((aw >> (gj0 & 31)) & 0xFu);
             // the slot of row m-1 (read in the previous row) takes row m+QD
             issue(m + QD, slot == 0 ? D - 1 : slot - 1);
@@ -474,9 +476,6 @@ __device__ __forceinline__ void skew_strip(const DevParams &p, const TbArgs &a, 
                 W[0][2][c] = xin[c];
                 ylev1[c] = Yp[c];
                 Yp[c] = yin[c];
-#pragma unroll
-                for (int q = K; q > 0; q--) T[q][c] = T[q - 1][c];
-                T[0][c] = cin[c];
             }
 #pragma unroll
             for (int q = K; q > 0; q--) TE[q] = TE[q - 1];
@@ -491,6 +490,15 @@ __device__ __forceinline__ void skew_strip(const DevParams &p, const TbArgs &a, 
                 if (m - m0 >= 2 * lv + 1) {
                 const float *Wc = W[lv - 1][1];
                 const float *Yl = (lv == 1) ? ylev1 : W[lv - 2 >= 0 ? lv - 2 : 0][0];
+                float Tl[4] = {0.f, 0.f, 0.f, 0.f};  // tcc at row r
+                if (COEF == WG_COEF_TABLE) {
+                    const int tsl = ts >= lv ? ts - lv : ts - lv + K + 1;
+                    const float4 tq = *reinterpret_cast<const float4 *>(tring + tsl * 128 + 4 * lane);
+                    Tl[0] = tq.x;
+                    Tl[1] = tq.y;
+                    Tl[2] = tq.z;
+                    Tl[3] = tq.w;
+                }
                 const float e3 = __shfl_down_sync(0xffffffffu, Wc[0], 1);
                 const float w0 = __shfl_up_sync(0xffffffffu, Wc[3], 1);
 #pragma unroll
@@ -499,7 +507,7 @@ __device__ __forceinline__ void skew_strip(const DevParams &p, const TbArgs &a, 
                     const float w = (c > 0) ? Wc[c > 0 ? c - 1 : 0] : w0;
                     const bool act = NEED_ACT ? ((aq >> (4 * lv + c)) & 1u) : true;
                     v[c] = skew_cell<COEF, false, PLAIN, INL, KZ>(p, a, r, gj0 + c, lv, Wc[c], Yl[c], W[lv - 1][2][c],
-                                                         W[lv - 1][0][c], e, w, T[lv][c], 0.f, act);
+                                                         W[lv - 1][0][c], e, w, Tl[c], 0.f, act);
                 }
                 if (!GEN && edge) {  // warp-uniform
                     if (ce >= 0 && r > 0 && r < p.nx - 1) {  // the lane holding column 0 (c = 0) or ny-1 (c = 3)
@@ -507,7 +515,7 @@ __device__ __forceinline__ void skew_strip(const DevParams &p, const TbArgs &a, 
                         const float res = col_edge_cell<COEF>(
                             p, a, r, lf ? Wc[0] : Wc[3], lf ? Yl[0] : Yl[3], lf ? W[lv - 1][2][0] : W[lv - 1][2][3],
                             lf ? W[lv - 1][0][0] : W[lv - 1][0][3], lf ? Wc[1] : e3, lf ? w0 : Wc[2],
-                            lf ? T[lv][0] : T[lv][3], TE[lv], NEED_ACT ? ((aq >> (4 * lv + ce)) & 1u) : true, !lf);
+                            lf ? Tl[0] : Tl[3], TE[lv], NEED_ACT ? ((aq >> (4 * lv + ce)) & 1u) : true, !lf);
                         v[0] = lf ? res : v[0];
                         v[3] = lf ? v[3] : res;
                     }
@@ -526,7 +534,7 @@ __device__ __forceinline__ void skew_strip(const DevParams &p, const TbArgs &a, 
                             pick4(W[lv - 1][2][0], W[lv - 1][2][1], W[lv - 1][2][2], W[lv - 1][2][3], ce),
                             pick4(W[lv - 1][0][0], W[lv - 1][0][1], W[lv - 1][0][2], W[lv - 1][0][3], ce),
                             pick4(Wc[1], Wc[2], Wc[3], e3, ce), pick4(w0, Wc[0], Wc[1], Wc[2], ce),
-                            pick4(T[lv][0], T[lv][1], T[lv][2], T[lv][3], ce), TE[lv],
+                            pick4(Tl[0], Tl[1], Tl[2], Tl[3], ce), TE[lv],
                             NEED_ACT ? ((aq >> (4 * lv + ce)) & 1u) : true, gj0 != 0);
                         v[0] = (ce == 0) ? res : v[0];
                         v[1] = (ce == 1) ? res : v[1];
@@ -544,7 +552,7 @@ __device__ __forceinline__ void skew_strip(const DevParams &p, const TbArgs &a, 
                                 pick4(W[lv - 1][2][0], W[lv - 1][2][1], W[lv - 1][2][2], W[lv - 1][2][3], c),
                                 pick4(W[lv - 1][0][0], W[lv - 1][0][1], W[lv - 1][0][2], W[lv - 1][0][3], c),
                                 pick4(Wc[1], Wc[2], Wc[3], e3, c), pick4(w0, Wc[0], Wc[1], Wc[2], c),
-                                pick4(T[lv][0], T[lv][1], T[lv][2], T[lv][3], c), tcv,
+                                pick4(Tl[0], Tl[1], Tl[2], Tl[3], c), tcv,
                                 NEED_ACT ? ((aq >> (4 * lv + c)) & 1u) : true);
                             v[0] = (c == 0) ? res : v[0];
                             v[1] = (c == 1) ? res : v[1];
@@ -566,6 +574,7 @@ __device__ __forceinline__ void skew_strip(const DevParams &p, const TbArgs &a, 
                     W[lv][2][c] = v[c];
                 }
             }
+            ts = (ts == K) ? 0 : ts + 1;  // row m+1's tcc slot
             const int r = m - K;
             if (lane_core && r >= i_s && r < i_e) {
                 const size_t o = (size_t)r * p.pitch + gj0;
@@ -603,12 +612,21 @@ __global__ void __launch_bounds__(128, 4) k_step_skew(const __grid_constant__ De
     const int warp = blockIdx.x * 4 + (threadIdx.x >> 5);
     if (warp >= ntasks) return;  // warp-uniform
     float *ring = reinterpret_cast<float *>(skew_smem) + (threadIdx.x >> 5) * SkewSlot<COEF>::DEPTH * SkewSlot<COEF>::SIZE;
+    float *tring = reinterpret_cast<float *>(skew_smem) + 4 * SkewSlot<COEF>::DEPTH * SkewSlot<COEF>::SIZE +
+                   (threadIdx.x >> 5) * (K + 1) * 128;  // table scenes: tcc of the last K+1 rows
     const int4 t = tasks[warp];
     const int gj0 = t.x * STEP - H + 4 * lane;
     const int lo = t.x * STEP, hi = lo + STEP;  // the core columns of tile t.x
     constexpr bool PLAIN = PL >= 1, KZ = PL == 2;
-    if (t.w == 2) skew_strip<COEF, K, PLAIN, true, false, false, KZ>(p, a, t.y, t.z, gj0, lane, ring, true, lo, hi);
-    else skew_strip<COEF, K, PLAIN, false, false, false, KZ>(p, a, t.y, t.z, gj0, lane, ring, t.w == 1, lo, hi);
+    if (t.w == 2) skew_strip<COEF, K, PLAIN, true, false, false, KZ>(p, a, t.y, t.z, gj0, lane, ring, tring, true, lo, hi);
+    else skew_strip<COEF, K, PLAIN, false, false, false, KZ>(p, a, t.y, t.z, gj0, lane, ring, tring, t.w == 1, lo, hi);
+}
+
+// dynamic shared memory of k_step_skew: 4 warps x (row ring + tcc ring of K+1 rows, table scenes)
+template <int COEF, int K>
+constexpr size_t skew_smem_bytes()
+{
+    return 4 * (SkewSlot<COEF>::DEPTH * SkewSlot<COEF>::SIZE + (COEF == WG_COEF_TABLE ? (K + 1) * 128 : 0)) * sizeof(float);
 }
 
 static bool skew_shape_ok(const DevParams &p, int K, int S)
@@ -631,7 +649,7 @@ static int sm_count()
 template <int COEF, int K, int PL>
 static int skew_capacity()
 {
-    constexpr size_t smem = 4 * SkewSlot<COEF>::DEPTH * SkewSlot<COEF>::SIZE * sizeof(float);  // 4 warps
+    constexpr size_t smem = skew_smem_bytes<COEF, K>();
     static int per_sm = 0;
     if (!per_sm) {
         cudaFuncSetAttribute(k_step_skew<COEF, K, PL>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
@@ -645,7 +663,7 @@ static int skew_capacity()
 template <int COEF, int K, int PL>
 static void launch_skew_k(const DevParams &p, const TbArgs &a, const int4 *tasks, int ntasks, cudaStream_t st)
 {
-    constexpr size_t smem = 4 * SkewSlot<COEF>::DEPTH * SkewSlot<COEF>::SIZE * sizeof(float);
+    constexpr size_t smem = skew_smem_bytes<COEF, K>();
     skew_capacity<COEF, K, PL>();  // sets the shared-memory attribute once
     k_step_skew<COEF, K, PL><<<(ntasks + 3) / 4, 128, smem, st>>>(p, a, tasks, ntasks);
 }
@@ -834,13 +852,13 @@ __global__ void __launch_bounds__(128, 4) k_batch_skew(const SlotDev *__restrict
         const int gjs = w.y, gj0 = gjs + 4 * lane;
         if (w.w == 3) {  // periodic, ghost layout: a halo on both sides of every tile
             const int lo = max(gjs + H, 0), hi = min(gjs + 128 - H, sd.p.ny);
-            skew_strip<WG_COEF_MASK, K, false, false, true, true>(p, a, i_s, i_e, gj0, lane, ring, false, lo, hi);
+            skew_strip<WG_COEF_MASK, K, false, false, true, true>(p, a, i_s, i_e, gj0, lane, ring, nullptr, false, lo, hi);
             continue;
         }
         const int lo = gjs <= 0 ? 0 : gjs + H;
         const int hi = gjs + 128 >= sd.p.ny ? sd.p.ny : gjs + 128 - H;
-        if (w.w == 2) skew_strip<WG_COEF_MASK, K, false, true, true>(p, a, i_s, i_e, gj0, lane, ring, true, lo, hi);
-        else skew_strip<WG_COEF_MASK, K, false, false, true>(p, a, i_s, i_e, gj0, lane, ring, w.w == 1, lo, hi);
+        if (w.w == 2) skew_strip<WG_COEF_MASK, K, false, true, true>(p, a, i_s, i_e, gj0, lane, ring, nullptr, true, lo, hi);
+        else skew_strip<WG_COEF_MASK, K, false, false, true>(p, a, i_s, i_e, gj0, lane, ring, nullptr, w.w == 1, lo, hi);
     }
 }
 
