@@ -23,7 +23,7 @@ pytestmark = pytest.mark.gpu
 SHAPES = [  # nx, ny, boundary, extras
     (64, 64, P.BC_DIRICHLET, {}),
     (40, 128, P.BC_ABSORBING, {}),
-    (37, 129, P.BC_DIRICHLET, dict(src=True)),
+    (130, 257, P.BC_PERIODIC, dict(floor=True)),   # ghost layout; leaves after the second frame
     (120, 250, P.BC_ABSORBING, dict(twospeeds=True)),
     (3, 40, P.BC_DIRICHLET, {}),
     (10, 13, P.BC_ABSORBING, {}),
@@ -32,11 +32,11 @@ SHAPES = [  # nx, ny, boundary, extras
     (90, 300, P.BC_ABSORBING, dict(floor=True)),
     (50, 5, P.BC_DIRICHLET, {}),          # ny < 8: single updates only
     (80, 96, P.BC_PERIODIC, {}),          # periodic: ghost layout
-    (33, 45, P.BC_PERIODIC, dict(twospeeds=True)),  # narrower than a tile: wraps several times
-    (130, 257, P.BC_PERIODIC, dict(floor=True)),
+    (37, 129, P.BC_DIRICHLET, dict(src=True)),
     (9, 131, P.BC_PERIODIC, {}),          # fewer rows than the ghost rows
     (60, 70, P.BC_PERIODIC, dict(src=True)),  # a source: single updates only
     (200, 217, P.BC_DIRICHLET, dict(twospeeds=True, src=True)),
+    (33, 45, P.BC_PERIODIC, dict(twospeeds=True)),  # narrower than a tile; arrives after the first frame
 ]
 FRAMES = [10, 1, 3, 7, 2]
 
