@@ -110,7 +110,7 @@ def test_autotuned_blocking_and_launch_count():
 @pytest.mark.parametrize("name", ["dir_kappa_floor", "abs_twospeeds_src"])
 def test_skewed_blocking_on_small_and_odd_grids(nx, ny, name):
     """Grids where every task of the skewed pass takes the general rule (fewer than
-    2*8+1 rows), where one column tile holds both boundary columns, and odd widths."""
+    2(K+1)+1 rows), where one column tile holds both boundary columns, and odd widths."""
     p, f, xy = case(name, nx=nx, ny=ny, seed=1)
     n = 13
     new, prev, _, _ = oracle.run(p, f["phi"], f["psi"], f["tmp"], xy, f["tcc"], f["tc"], f["tgamma"], n)
