@@ -337,6 +337,40 @@ __global__ void __launch_bounds__(32 * ENERGY_COLS_PER_BLOCK)
         const T *re = phi + (size_t)ip * p.pitch, *rw = phi + (size_t)im * p.pitch, *rc = phi + row, *ry = psi + row;
         const float es2 = (float)p.e_scale2, hc2 = (float)p.ehalf_c2, hc2b = (float)p.ehalf_c2b;
         float kb = 0.f, kbc = 0.f, kt = 0.f, ktc = 0.f;  // FP32 Kahan sums (FP32 fields)
+        if (sizeof(T) == 4 && MASK == 1) {
+            // FP32 fields: four cells per lane and step as 16-byte loads of the rows i-1, i, i+1
+            // and psi; the j-1 / j+1 neighbours from the adjacent lanes (the row pitch is a
+            // multiple of 128 elements, so every load stays in the row)
+            const float *fc = (const float *)rc, *fy = (const float *)ry, *fe = (const float *)re,
+                        *fw = (const float *)rw;
+            const uint32_t *nzr = nz + (size_t)i * p.wpitch;
+            for (int base = 0; base < NY; base += 128) {
+                const int j0 = base + 4 * lane;
+                const float4 c4 = *reinterpret_cast<const float4 *>(fc + j0);
+                const float4 y4 = *reinterpret_cast<const float4 *>(fy + j0);
+                const float4 e4 = *reinterpret_cast<const float4 *>(fe + j0);
+                const float4 w4 = *reinterpret_cast<const float4 *>(fw + j0);
+                float left = __shfl_up_sync(0xffffffffu, c4.w, 1), right = __shfl_down_sync(0xffffffffu, c4.x, 1);
+                if (lane == 0) left = (j0 > 0) ? fc[j0 - 1] : c4.x;
+                if (lane == 31) right = (j0 + 4 < NY) ? fc[j0 + 4] : c4.w;
+                const uint32_t bits = (nzr[j0 >> 5] >> (j0 & 31)) & 0xFu;
+                const float xs[4] = {c4.x, c4.y, c4.z, c4.w}, ys[4] = {y4.x, y4.y, y4.z, y4.w};
+                const float es[4] = {e4.x, e4.y, e4.z, e4.w}, ws[4] = {w4.x, w4.y, w4.z, w4.w};
+#pragma unroll
+                for (int k = 0; k < 4; k++) {
+                    const int j = j0 + k;
+                    if (j >= NY) break;
+                    float jn = (k < 3) ? xs[k < 3 ? k + 1 : 3] : right;
+                    float js = (k > 0) ? xs[k > 0 ? k - 1 : 0] : left;
+                    if (j == NY - 1) jn = xs[k];  // clamped at the boundary lines
+                    if (j == 0) js = xs[k];
+                    const float en = cell_energy32(es2, hc2, hc2b, p.twospeeds, xs[k], ys[k], es[k], ws[k], jn, js,
+                                                   (int)((bits >> k) & 1u));
+                    if (j < jmid) kahan_add(kb, kbc, en);
+                    else kahan_add(kt, ktc, en);
+                }
+            }
+        } else
 #pragma unroll 4
         for (int j = lane; j < NY; j += 32) {
             const int jp = (j + 1 == NY) ? NY - 1 : j + 1, jm = (j == 0) ? 0 : j - 1;
