@@ -1,6 +1,7 @@
 """Seeded synthetic scenes: the host-side setup of the reference, restated in numpy.
 
-The reference builds its inputs once per scene on the host (SURVEY call stack 3.3):
+The reference builds its inputs once per scene on the host, in animation() before its time loop
+(wave_billiard.c:654-881):
   * the domain mask ``xy_in`` from ``xy_in_billiard_single_domain``
     (sub_wave.c:5712-6259) evaluated at ``ij_to_xy`` (sub_wave.c:469-476);
   * the speed/damping tables from ``init_ior_2d``'s constant branch
