@@ -914,8 +914,9 @@ void launch_batch_skew(int K, const SlotDev *tab, const SlotDyn *dyn, const int4
 
 bool batch_wrap_ok(const wg_params &p, int prec)
 {
+    // nx + 2 ghost-row bands within a grid dimension of the mask's ghost kernel (65535)
     return prec == WG_FP32 && p.b_cond == WG_BC_PERIODIC && !p.bc_neumann && !p.src_on && !p.oscillate_left &&
-           !p.oscillate_topbot && p.ny >= 8 && p.nx >= 2 && p.nx <= 0xFFFF;
+           !p.oscillate_topbot && p.ny >= 8 && p.nx >= 2 && p.nx + 2 * BATCH_GHOST_ROWS <= 0xFFFF;
 }
 
 bool batch_skew_ok(const wg_params &p, int prec)
