@@ -386,13 +386,15 @@ template <int COEF> struct SkewSlot {
 // a multiple of 4, or of the point source (fix = true), all away from rows 0 and nx-1.
 // GEN = true (fix = true): the others, with the general rule on rows 0 and nx-1.
 // Columns [lo, hi) of the tile are stored (lo, hi multiples of 4 but for hi = ny).
-// WRAP: a periodic scene in the ghost layout (batches): rows -BATCH_GHOST_ROWS..nx +
+// wrap: a periodic scene in the ghost layout (batches): rows -BATCH_GHOST_ROWS..nx +
 // BATCH_GHOST_ROWS - 1 and columns -BATCH_GHOST_COLS..ny + BATCH_GHOST_COLS - 1 hold the
 // wrapped field, so every cell takes the bulk rule and no edge rule applies.
 // KZ (with PLAIN): KAPPA = 0, the bulk update without its kappa term.
-template <int COEF, int K, bool PLAIN, bool GEN, bool INL = false, bool WRAP = false, bool KZ = false>
+// (a runtime flag, so that periodic and other inner tiles share one loop in the
+// instruction cache).
+template <int COEF, int K, bool PLAIN, bool GEN, bool INL = false, bool KZ = false>
 __device__ __forceinline__ void skew_strip(const DevParams &p, const TbArgs &a, int i_s, int i_e, int gj0, int lane,
-                                           float *ring, float *tring, bool edge, int lo, int hi)
+                                           float *ring, float *tring, bool edge, int lo, int hi, bool wrap = false)
 {
     using SL = SkewSlot<COEF>;
     constexpr int D = SL::DEPTH;
@@ -426,7 +428,7 @@ __device__ __forceinline__ void skew_strip(const DevParams &p, const TbArgs &a, 
     // row m goes to slot (m - m0) % D; each lane copies, and later reads, only its own bytes
     auto issue = [&](int m, int slot) {
         float *b = ring + slot * SL::SIZE;
-        const bool ok = WRAP ? (gj0 >= -BATCH_GHOST_COLS && gj0 < p.ny + BATCH_GHOST_COLS && m >= -BATCH_GHOST_ROWS &&
+        const bool ok = wrap ? (gj0 >= -BATCH_GHOST_COLS && gj0 < p.ny + BATCH_GHOST_COLS && m >= -BATCH_GHOST_ROWS &&
                                 m < p.nx + BATCH_GHOST_ROWS)
                              : (grp_ok && m >= 0 && m < p.nx);
         const long long o = ok ? (long long)m * p.pitch + gj0 : 0;
@@ -618,8 +620,8 @@ __global__ void __launch_bounds__(128, 4) k_step_skew(const __grid_constant__ De
     const int gj0 = t.x * STEP - H + 4 * lane;
     const int lo = t.x * STEP, hi = lo + STEP;  // the core columns of tile t.x
     constexpr bool PLAIN = PL >= 1, KZ = PL == 2;
-    if (t.w == 2) skew_strip<COEF, K, PLAIN, true, false, false, KZ>(p, a, t.y, t.z, gj0, lane, ring, tring, true, lo, hi);
-    else skew_strip<COEF, K, PLAIN, false, false, false, KZ>(p, a, t.y, t.z, gj0, lane, ring, tring, t.w == 1, lo, hi);
+    if (t.w == 2) skew_strip<COEF, K, PLAIN, true, false, KZ>(p, a, t.y, t.z, gj0, lane, ring, tring, true, lo, hi);
+    else skew_strip<COEF, K, PLAIN, false, false, KZ>(p, a, t.y, t.z, gj0, lane, ring, tring, t.w == 1, lo, hi);
 }
 
 // dynamic shared memory of k_step_skew: 4 warps x (row ring + tcc ring of K+1 rows, table scenes)
@@ -852,15 +854,12 @@ __global__ void __launch_bounds__(128, 4) k_batch_skew(const SlotDev *__restrict
         a.err = nullptr;
         const int i_s = w.z & 0xFFFF, i_e = (int)((unsigned)w.z >> 16);
         const int gjs = w.y, gj0 = gjs + 4 * lane;
-        if (w.w == 3) {  // periodic, ghost layout: a halo on both sides of every tile
-            const int lo = max(gjs + H, 0), hi = min(gjs + 128 - H, sd.p.ny);
-            skew_strip<WG_COEF_MASK, K, false, false, true, true>(p, a, i_s, i_e, gj0, lane, ring, nullptr, false, lo, hi);
-            continue;
-        }
-        const int lo = gjs <= 0 ? 0 : gjs + H;
-        const int hi = gjs + 128 >= sd.p.ny ? sd.p.ny : gjs + 128 - H;
+        // one call site per strip form, so that inner, edge and periodic tiles share a loop
+        const bool wrap = w.w == 3;  // periodic, ghost layout: a halo on both sides of every tile
+        const int lo = wrap ? max(gjs + H, 0) : (gjs <= 0 ? 0 : gjs + H);
+        const int hi = wrap ? min(gjs + 128 - H, sd.p.ny) : (gjs + 128 >= sd.p.ny ? sd.p.ny : gjs + 128 - H);
         if (w.w == 2) skew_strip<WG_COEF_MASK, K, false, true, true>(p, a, i_s, i_e, gj0, lane, ring, nullptr, true, lo, hi);
-        else skew_strip<WG_COEF_MASK, K, false, false, true>(p, a, i_s, i_e, gj0, lane, ring, nullptr, w.w == 1, lo, hi);
+        else skew_strip<WG_COEF_MASK, K, false, false, true>(p, a, i_s, i_e, gj0, lane, ring, nullptr, w.w == 1, lo, hi, wrap);
     }
 }
 
