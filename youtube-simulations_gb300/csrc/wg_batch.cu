@@ -510,8 +510,9 @@ static void batch_enqueue_frame(wg_batch *b, int n, bool skewed)
 // Depth and row chunk per size class, in two stages: depths 2..6 with the list-wide
 // chunk, then chunks of 32, 64, 128 and 256 rows at the best depth.  Each candidate
 // times one skewed pass over the class's scenes (reading their current fields, writing
-// the other pair, so the state does not change); the fastest per update is kept.  Nine
-// short passes per class keep the tuning frame of a server tick short.
+// the other pair, so the state does not change), best of three after one untimed pass;
+// the fastest per update is kept.  Nine candidates per class keep the tuning frame of a
+// server tick short.
 static wg_status batch_autotune(wg_batch *b)
 {
     bool tuned = false, ghosts = false;
@@ -533,9 +534,8 @@ static wg_status batch_autotune(wg_batch *b)
             b->launches++;
             ghosts = true;
         }
-        cudaEvent_t e0, e1;
-        WG_CUDA(cudaEventCreate(&e0));
-        WG_CUDA(cudaEventCreate(&e1));
+        cudaEvent_t ev[4];
+        for (int q = 0; q < 4; q++) WG_CUDA(cudaEventCreate(&ev[q]));
         int best = 0, best_rows = 0;
         double best_ms = 1e30;
         int4 *dev = nullptr;
@@ -551,22 +551,25 @@ static wg_status batch_autotune(wg_batch *b)
             if (err == cudaSuccess && nt) err = cudaMemcpyAsync(dev, tasks.data(), sizeof(int4) * nt, cudaMemcpyHostToDevice, b->st);
             const int idx = b->skew_n_cap - 1;  // the count slot kept for tuning
             if (err == cudaSuccess) err = cudaMemcpyAsync(b->d_skew_n + idx, &nt, sizeof(int), cudaMemcpyHostToDevice, b->st);
-            const int reps = 2;
+            const int reps = 3;  // one untimed pass, then the best of three
             for (int r = 0; r <= reps && err == cudaSuccess; r++) {
-                if (r == 1) cudaEventRecord(e0, b->st);
                 cudaMemsetAsync(b->d_tune_ticket + r, 0, sizeof(int), b->st);
                 launch_batch_skew(K, b->d_tab, b->d_dyn, dev, b->d_skew_n + idx, b->d_tune_ticket + r, 0, 0, b->st);
                 b->launches++;
                 err = cudaGetLastError();
+                if (err == cudaSuccess) err = cudaEventRecord(ev[r], b->st);
             }
-            if (err == cudaSuccess) err = cudaEventRecord(e1, b->st);
-            if (err == cudaSuccess) err = cudaEventSynchronize(e1);
-            float ms = 0.f;
-            if (err == cudaSuccess) err = cudaEventElapsedTime(&ms, e0, e1);
+            if (err == cudaSuccess) err = cudaEventSynchronize(ev[reps]);
+            float ms = 1e30f;
+            for (int r = 1; r <= reps && err == cudaSuccess; r++) {
+                float t = 0.f;
+                err = cudaEventElapsedTime(&t, ev[r - 1], ev[r]);
+                ms = std::min(ms, t);
+            }
             if (dev) cudaFreeAsync(dev, b->st);
             dev = nullptr;
             if (err == cudaSuccess) err = cudaStreamSynchronize(b->st);  // tasks outlives its copy
-            const double per = ms / (reps * K);
+            const double per = ms / K;
             if (R == 0 || per < b->tune_ms[c * 8 + K]) b->tune_ms[c * 8 + K] = per;
             if (per < best_ms) {
                 best_ms = per;
@@ -574,8 +577,7 @@ static wg_status batch_autotune(wg_batch *b)
                 best_rows = R;
             }
         }
-        cudaEventDestroy(e0);
-        cudaEventDestroy(e1);
+        for (int q = 0; q < 4; q++) cudaEventDestroy(ev[q]);
         if (err != cudaSuccess) return cuda_fail(err, "batch autotune");
         b->class_k[c] = best;
         b->class_rows[c] = best_rows;
