@@ -312,9 +312,11 @@ __device__ __forceinline__ float skew_cell(const DevParams &p, const TbArgs &a, 
 // row m it computes level s at row m - s for s = 1..K (level 0 = phi(t), level -1 =
 // psi(t-1)), so each level keeps only a window of three rows in registers.  Column
 // neighbours inside a lane are registers; across lanes they are one warp shuffle each
-// way.  Input rows are prefetched QD rows ahead.  The loop is unrolled by 3, the period
-// of the row windows, so that rotating them is register renaming.  Core columns
-// [H, 128-H) store level K (new phi) and level K-1 (new psi) of the rows in the strip.
+// way.  Input rows are prefetched QD rows ahead through a per-warp shared-memory ring;
+// table scenes also keep the tcc values of the last K+1 rows in a second small ring.
+// One row per loop trip (SKEW_UNROLL): longer trips turn the window rotation into
+// register renaming but miss the instruction cache.  Core columns [H, 128-H) store level
+// K (new phi) and level K-1 (new psi) of the rows in the strip.
 //
 // Tiles that reach an edge row or column or hold the point source (edge tiles) take three
 // extra steps after the common update: the lane holding column 0 or ny-1 redoes that
@@ -375,7 +377,7 @@ __device__ __forceinline__ void cp_async_wait() { asm volatile("cp.async.wait_gr
 // Row slot of a warp's shared-memory ring (floats): phi[128], psi[128], tcc[128] (table
 // scenes), then one active word and one edge-column tc per lane.
 #ifndef SKEW_UNROLL
-#define SKEW_UNROLL 1  // rows per loop trip: 3 turns the row windows by renaming registers
+#define SKEW_UNROLL 1  // rows per loop trip (2 and 3 measured slower)
 #endif
 template <int COEF> struct SkewSlot {
     static constexpr int PSI = 128, TCC = 256, ACT = (COEF == WG_COEF_TABLE) ? 384 : 256, TCE = ACT + 32, SIZE = TCE + 32;
