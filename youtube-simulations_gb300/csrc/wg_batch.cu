@@ -1,18 +1,19 @@
 // wg_batch.cu — many scenes of uneven sizes advanced together.
 //
-// Every active scene is cut into tiles of 8 rows x (64 threads x V) columns; a frame
-// of n updates is n launches of one persistent kernel (k_batch_step, sized to fill
-// every SM) whose CTAs take (scene, tile) work items from a device-side atomic counter,
-// plus one kernel that advances each scene's step counter.  The whole frame is
-// recorded once as a CUDA graph and replayed; the scene table, the work counts and the
-// per-scene time and buffer parity live in device memory, so admitting or removing
-// scenes changes data, not the graph.
+// Single updates: every active scene is cut into work items of BT_ROWS rows x (64
+// threads x V) columns; a frame of n updates is n launches of one persistent kernel
+// (k_batch_step, sized to fill every SM) whose CTAs take (scene, item) pairs from a
+// device-side atomic counter, plus one kernel that advances each scene's step counter.
+// The whole frame is recorded once as a CUDA graph and replayed; the scene table, the
+// work counts and the per-scene time and buffer parity live in device memory, so
+// admitting or removing scenes changes data, not the graph.
 //
 // The per-cell arithmetic is the single-scene kernels' (k_step_bulk / fast_edge), so a
 // scene advanced in a batch is bit-identical to the same scene advanced alone.
 //
-// FP32 scenes with mirror ("Dirichlet") or absorbing boundaries take skewed passes
-// instead (k_batch_skew, wg_tb.cu): a frame of n updates is a few passes of 2..6 updates
+// FP32 scenes with mirror ("Dirichlet"), absorbing or periodic boundaries (periodic ones
+// in the ghost layout of wg_batch.h) take skewed passes instead (k_batch_skew, wg_tb.cu):
+// a frame of n updates is a few passes of 2..6 updates
 // each, at the depth class tuned for the scene's size class, writing between two buffer
 // pairs.  Each depth class runs as its own branch of the frame's graph, beside the chain
 // of single updates of the other scenes.  The skewed cells are the single-update cells
