@@ -120,6 +120,35 @@ def test_state_roundtrip_and_time():
         assert s.time == 103
 
 
+def test_state_copies_are_stream_ordered():
+    """wg_scene_upload_state returns before its copies and repacks finish: a state upload
+    followed at once, with no sync, by a step and a download (the end-to-end step) gives
+    the fields of the same state uploaded in FP64 and stepped (bit for bit, the same
+    skewed passes on both), twice in a row on one scene."""
+    sc = scenes.config2(seed=5, nx=1536, ny=1024)
+    lib = W.lib()
+    out = []
+    for fast in (False, True):
+        with W.Scene(sc.params, P.FP32, P.COEF_TABLE) as s:
+            s.upload(sc.phi, sc.psi, sc.xy, sc.tcc, sc.tc, sc.tgamma)
+            s.set_blocking(4, 16, 1)
+            for rep in range(2):
+                s.time = 0
+                if fast:
+                    a = np.ascontiguousarray(sc.phi, np.float32)
+                    b = np.ascontiguousarray(sc.psi, np.float32)
+                    W.check(lib.wg_scene_upload_state(s.h, a.ctypes.data, b.ctypes.data, P.FP32))
+                    W.check(lib.wg_scene_step(s.h, 40))
+                    x, y = np.empty_like(a), np.empty_like(b)
+                    W.check(lib.wg_scene_download(s.h, x.ctypes.data, y.ctypes.data, P.FP32))
+                else:
+                    s.upload(sc.phi, sc.psi, sc.xy, sc.tcc, sc.tc, sc.tgamma)
+                    s.step(40)
+                    x, y = s.download(native=True)
+            out.append((x, y))
+    assert np.array_equal(out[0][0], out[1][0]) and np.array_equal(out[0][1], out[1][1])
+
+
 def test_nonfinite_detector():
     """Blow-up detection through a host-side injected NaN (no device fault)."""
     p, f, xy, _ = variant_inputs("s_dir", seed=9)
