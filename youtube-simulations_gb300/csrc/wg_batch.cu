@@ -40,7 +40,8 @@ __device__ __noinline__ T batch_edge(const DevParams &p, const FastArgs<T> &a, i
     return v;
 }
 
-template <class T>
+// KZ (FP64 scenes with KAPPA = 0): the bulk update without its kappa term (values unchanged).
+template <class T, bool KZ = false>
 __device__ __forceinline__ void batch_tile(const DevParams &p, const T *__restrict__ phi, T *__restrict__ out,
                                            const uint32_t *__restrict__ act, const uint32_t *__restrict__ nz,
                                            int i0, int jt, long long time)
@@ -92,9 +93,8 @@ __device__ __forceinline__ void batch_tile(const DevParams &p, const T *__restri
                 const T w = (k == 0) ? wl : c[k - 1];
                 const T e = (k == V - 1) ? er : c[k + 1];
                 if (sizeof(T) == 8) {
-                    double delta = A_(A_(A_((double)n[k], (double)s[k]), (double)e), (double)w);
-                    delta = S_(delta, M_(4.0, (double)x));
-                    v = (T)upd64((double)x, (double)y[k], ac ? p.c2 : p.c2b, delta, p.kappa, ac ? p.gam : p.gamb);
+                    const double delta = L4_(A_(A_(A_((double)n[k], (double)s[k]), (double)e), (double)w), (double)x);
+                    v = (T)upd64<KZ>((double)x, (double)y[k], ac ? p.c2 : p.c2b, delta, p.kappa, ac ? p.gam : p.gamb);
                 } else {
                     const float xf = (float)x;
                     const float delta = (((float)n[k] - xf) + ((float)s[k] - xf)) + (((float)e - xf) + ((float)w - xf));
@@ -137,8 +137,14 @@ __global__ void __launch_bounds__(256, 4) k_batch_step(const BatchHdr *__restric
         const SlotDev &sd = tab[w.x];
         const SlotDyn d = dyn[w.w];
         const int phase = (d.cur + u) & 1, base = 2 * d.pair;
-        batch_tile<T>(sd.p, (const T *)sd.f[base + phase], (T *)sd.f[base + 1 - phase], sd.act, sd.nz, w.y, w.z,
-                      d.time + u + 1);
+        bool kz = false;
+        if constexpr (sizeof(T) == 8) kz = sd.p.kappa == 0.0;  // block-uniform
+        if (kz)
+            batch_tile<T, true>(sd.p, (const T *)sd.f[base + phase], (T *)sd.f[base + 1 - phase], sd.act, sd.nz, w.y,
+                                w.z, d.time + u + 1);
+        else
+            batch_tile<T>(sd.p, (const T *)sd.f[base + phase], (T *)sd.f[base + 1 - phase], sd.act, sd.nz, w.y, w.z,
+                          d.time + u + 1);
         if (tid == 0) s_next[buf ^ 1] = next;
         __syncthreads();  // the next ticket is visible; s_next[buf] is free again
     }

@@ -38,12 +38,24 @@ __device__ __forceinline__ double S_(double a, double b) { return __dsub_rn(a, b
 __device__ __forceinline__ double M_(double a, double b) { return __dmul_rn(a, b); }
 __device__ __forceinline__ double D_(double a, double b) { return __ddiv_rn(a, b); }
 
+// Products by 2 and 4 are exact (a change of exponent) while |x| < DBL_MAX / 4, so one
+// fused multiply-add rounds the same exact sum as the separate multiply and add, and
+// IEEE 754 gives an exactly zero result the same sign both ways:
+//   P2_(x, y)  == A_(-y, M_(2.0, x))       (-y + 2*x)
+//   L4_(d, x)  == S_(d, M_(4.0, x))        (d - 4.0*x)
+// One FP64 operation instead of two, bit for bit on every field short of overflow.
+__device__ __forceinline__ double P2_(double x, double y) { return __fma_rn(2.0, x, -y); }
+__device__ __forceinline__ double L4_(double d, double x) { return __fma_rn(-4.0, x, d); }
+
 // -y + 2*x + cc*delta - KAPPA*x - g*(x-y)   (wave_billiard.c:373)
+// KZ: KAPPA = 0, where KAPPA*x is a zero and subtracting it changes at most the sign of
+// a zero result, never a value; the term is then left out.
+template <bool KZ = false>
 __device__ __forceinline__ double upd64(double x, double y, double cc, double delta, double kappa, double g)
 {
-    double r = A_(-y, M_(2.0, x));
+    double r = P2_(x, y);
     r = A_(r, M_(cc, delta));
-    r = S_(r, M_(kappa, x));
+    if (!KZ) r = S_(r, M_(kappa, x));
     return S_(r, M_(g, S_(x, y)));
 }
 

@@ -41,8 +41,7 @@ __global__ void __launch_bounds__(256) k_step_exact(DevParams p, const double *_
         w = p.twospeeds || m > 0;
         if (w) {
             const double x = phi[c], y = psi[c];
-            double delta = A_(A_(A_(phi[c + p.pitch], phi[c - p.pitch]), phi[c + 1]), phi[c - 1]);
-            delta = S_(delta, M_(4.0, x));
+            const double delta = L4_(A_(A_(A_(phi[c + p.pitch], phi[c - p.pitch]), phi[c + 1]), phi[c - 1]), x);
             v = upd64(x, y, tcc[c], delta, p.kappa, tg[c]);
         }
     }
@@ -187,7 +186,7 @@ __global__ void k_point_source(DevParams p, T *out, long long time)
 // phi rows, psi, tcc, the j-1 / j+V neighbours, the mask word) issued before the
 // first use.  Boundary-line cells (j = 0, j = ny-1) and padding are written back
 // unchanged; k_step_edge computes them afterwards.
-template <class T, int COEF>
+template <class T, int COEF, bool KZ = false>
 __global__ void __launch_bounds__(256) k_step_bulk(const __grid_constant__ DevParams p,
                                                    const __grid_constant__ FastArgs<T> a)
 {
@@ -218,13 +217,12 @@ __global__ void __launch_bounds__(256) k_step_bulk(const __grid_constant__ DevPa
             const T w = (k == 0) ? wl : c[k - 1];
             const T e = (k == V - 1) ? er : c[k + 1];
             if (sizeof(T) == 8) {
-                double delta = A_(A_(A_((double)n[k], (double)s[k]), (double)e), (double)w);
-                delta = S_(delta, M_(4.0, (double)x));
+                const double delta = L4_(A_(A_(A_((double)n[k], (double)s[k]), (double)e), (double)w), (double)x);
                 const double ccv = (COEF == WG_COEF_TABLE) ? (double)cc[k] : (act ? p.c2 : p.c2b);
                 double g;
                 if (COEF == WG_COEF_TABLE) g = a.tg ? (double)a.tg[row + j] : p.gam;
                 else g = act ? p.gam : p.gamb;
-                v = (T)upd64((double)x, (double)y[k], ccv, delta, p.kappa, g);
+                v = (T)upd64<KZ>((double)x, (double)y[k], ccv, delta, p.kappa, g);
             } else {
                 const float xf = (float)x;
                 const float delta = (((float)n[k] - xf) + ((float)s[k] - xf)) + (((float)e - xf) + ((float)w - xf));
@@ -552,11 +550,18 @@ void launch_step_fast(const DevParams &p, const FastArgs<T> &a, int coef_mode, l
     constexpr int V = Vec<T>::n;
     dim3 blk(64, 4), grd((p.pitch / V + 63) / 64, (p.nx - 2 + 3) / 4);
     const int nedge = 2 * p.nx + 2 * (p.ny - 2) + 1;
+    // FP64 with KAPPA = 0: the bulk update without its kappa term (values unchanged)
+    bool kz = false;
+    if constexpr (sizeof(T) == 8) kz = p.kappa == 0.0;
     if (coef_mode == WG_COEF_MASK) {
-        k_step_bulk<T, WG_COEF_MASK><<<grd, blk, 0, st>>>(p, a);
+        if constexpr (sizeof(T) == 8)
+            if (kz) k_step_bulk<T, WG_COEF_MASK, true><<<grd, blk, 0, st>>>(p, a);
+        if (!kz) k_step_bulk<T, WG_COEF_MASK><<<grd, blk, 0, st>>>(p, a);
         k_step_edge<T, WG_COEF_MASK><<<(nedge + 255) / 256, 256, 0, st>>>(p, a, time);
     } else {
-        k_step_bulk<T, WG_COEF_TABLE><<<grd, blk, 0, st>>>(p, a);
+        if constexpr (sizeof(T) == 8)
+            if (kz) k_step_bulk<T, WG_COEF_TABLE, true><<<grd, blk, 0, st>>>(p, a);
+        if (!kz) k_step_bulk<T, WG_COEF_TABLE><<<grd, blk, 0, st>>>(p, a);
         k_step_edge<T, WG_COEF_TABLE><<<(nedge + 255) / 256, 256, 0, st>>>(p, a, time);
     }
 }
