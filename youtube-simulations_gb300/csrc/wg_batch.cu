@@ -40,8 +40,9 @@ __device__ __noinline__ T batch_edge(const DevParams &p, const FastArgs<T> &a, i
     return v;
 }
 
-// KZ (FP64 scenes with KAPPA = 0): the bulk update without its kappa term (values unchanged).
-template <class T, bool KZ = false>
+// Z (FP64 scenes): upd64's flags for KAPPA = 0 and GAMMA = GAMMAB = 0, the bulk update
+// without those zero terms (values unchanged).
+template <class T, int Z = 0>
 __device__ __forceinline__ void batch_tile(const DevParams &p, const T *__restrict__ phi, T *__restrict__ out,
                                            const uint32_t *__restrict__ act, const uint32_t *__restrict__ nz,
                                            int i0, int jt, long long time)
@@ -94,7 +95,7 @@ __device__ __forceinline__ void batch_tile(const DevParams &p, const T *__restri
                 const T e = (k == V - 1) ? er : c[k + 1];
                 if (sizeof(T) == 8) {
                     const double delta = L4_(A_(A_(A_((double)n[k], (double)s[k]), (double)e), (double)w), (double)x);
-                    v = (T)upd64<KZ>((double)x, (double)y[k], ac ? p.c2 : p.c2b, delta, p.kappa, ac ? p.gam : p.gamb);
+                    v = (T)upd64<Z>((double)x, (double)y[k], ac ? p.c2 : p.c2b, delta, p.kappa, ac ? p.gam : p.gamb);
                 } else {
                     const float xf = (float)x;
                     const float delta = (((float)n[k] - xf) + ((float)s[k] - xf)) + (((float)e - xf) + ((float)w - xf));
@@ -137,14 +138,17 @@ __global__ void __launch_bounds__(256, 4) k_batch_step(const BatchHdr *__restric
         const SlotDev &sd = tab[w.x];
         const SlotDyn d = dyn[w.w];
         const int phase = (d.cur + u) & 1, base = 2 * d.pair;
-        bool kz = false;
-        if constexpr (sizeof(T) == 8) kz = sd.p.kappa == 0.0;  // block-uniform
-        if (kz)
-            batch_tile<T, true>(sd.p, (const T *)sd.f[base + phase], (T *)sd.f[base + 1 - phase], sd.act, sd.nz, w.y,
-                                w.z, d.time + u + 1);
+        const T *in = (const T *)sd.f[base + phase];
+        T *out = (T *)sd.f[base + 1 - phase];
+        int z = 0;  // block-uniform
+        if constexpr (sizeof(T) == 8)
+            z = (sd.p.kappa == 0.0 ? Z_KAPPA : 0) | (sd.p.gam == 0.0 && sd.p.gamb == 0.0 ? Z_GAMMA : 0);
+        if (z == (Z_KAPPA | Z_GAMMA))
+            batch_tile<T, Z_KAPPA | Z_GAMMA>(sd.p, in, out, sd.act, sd.nz, w.y, w.z, d.time + u + 1);
+        else if (z == Z_KAPPA)
+            batch_tile<T, Z_KAPPA>(sd.p, in, out, sd.act, sd.nz, w.y, w.z, d.time + u + 1);
         else
-            batch_tile<T>(sd.p, (const T *)sd.f[base + phase], (T *)sd.f[base + 1 - phase], sd.act, sd.nz, w.y, w.z,
-                          d.time + u + 1);
+            batch_tile<T>(sd.p, in, out, sd.act, sd.nz, w.y, w.z, d.time + u + 1);
         if (tid == 0) s_next[buf ^ 1] = next;
         __syncthreads();  // the next ticket is visible; s_next[buf] is free again
     }

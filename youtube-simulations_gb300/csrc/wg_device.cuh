@@ -48,15 +48,18 @@ __device__ __forceinline__ double P2_(double x, double y) { return __fma_rn(2.0,
 __device__ __forceinline__ double L4_(double d, double x) { return __fma_rn(-4.0, x, d); }
 
 // -y + 2*x + cc*delta - KAPPA*x - g*(x-y)   (wave_billiard.c:373)
-// KZ: KAPPA = 0, where KAPPA*x is a zero and subtracting it changes at most the sign of
-// a zero result, never a value; the term is then left out.
-template <bool KZ = false>
+// Z bit 0 (Z_KAPPA): KAPPA = 0.  Bit 1 (Z_GAMMA): g = 0 on every cell.  A zero
+// coefficient makes its product a zero, and subtracting a zero changes at most the sign
+// of a zero result, never a value; such a term is then left out.
+constexpr int Z_KAPPA = 1, Z_GAMMA = 2;
+template <int Z = 0>
 __device__ __forceinline__ double upd64(double x, double y, double cc, double delta, double kappa, double g)
 {
     double r = P2_(x, y);
     r = A_(r, M_(cc, delta));
-    if (!KZ) r = S_(r, M_(kappa, x));
-    return S_(r, M_(g, S_(x, y)));
+    if (!(Z & Z_KAPPA)) r = S_(r, M_(kappa, x));
+    if (!(Z & Z_GAMMA)) r = S_(r, M_(g, S_(x, y)));
+    return r;
 }
 
 // x - tc*(x - nb) - K*x - G*(x-y)   (wave_billiard.c:418)

@@ -186,7 +186,7 @@ __global__ void k_point_source(DevParams p, T *out, long long time)
 // phi rows, psi, tcc, the j-1 / j+V neighbours, the mask word) issued before the
 // first use.  Boundary-line cells (j = 0, j = ny-1) and padding are written back
 // unchanged; k_step_edge computes them afterwards.
-template <class T, int COEF, bool KZ = false>
+template <class T, int COEF, int Z = 0>
 __global__ void __launch_bounds__(256) k_step_bulk(const __grid_constant__ DevParams p,
                                                    const __grid_constant__ FastArgs<T> a)
 {
@@ -222,7 +222,7 @@ __global__ void __launch_bounds__(256) k_step_bulk(const __grid_constant__ DevPa
                 double g;
                 if (COEF == WG_COEF_TABLE) g = a.tg ? (double)a.tg[row + j] : p.gam;
                 else g = act ? p.gam : p.gamb;
-                v = (T)upd64<KZ>((double)x, (double)y[k], ccv, delta, p.kappa, g);
+                v = (T)upd64<Z>((double)x, (double)y[k], ccv, delta, p.kappa, g);
             } else {
                 const float xf = (float)x;
                 const float delta = (((float)n[k] - xf) + ((float)s[k] - xf)) + (((float)e - xf) + ((float)w - xf));
@@ -544,24 +544,34 @@ void launch_point_source(const DevParams &p, T *out, long long time, cudaStream_
 template void launch_point_source<float>(const DevParams &, float *, long long, cudaStream_t);
 template void launch_point_source<double>(const DevParams &, double *, long long, cudaStream_t);
 
+// FP64: the bulk update without the terms whose coefficient is zero on every cell
+// (upd64's Z flags: KAPPA = 0; GAMMA = 0 as a uniform value); the values are unchanged.
+template <class T, int COEF>
+static void launch_bulk(const DevParams &p, const FastArgs<T> &a, dim3 grd, dim3 blk, cudaStream_t st)
+{
+    if constexpr (sizeof(T) == 8) {
+        const bool g0 = (COEF == WG_COEF_TABLE) ? (!a.tg && p.gam == 0.0) : (p.gam == 0.0 && p.gamb == 0.0);
+        switch ((p.kappa == 0.0 ? Z_KAPPA : 0) | (g0 ? Z_GAMMA : 0)) {
+        case Z_KAPPA: k_step_bulk<T, COEF, Z_KAPPA><<<grd, blk, 0, st>>>(p, a); return;
+        case Z_GAMMA: k_step_bulk<T, COEF, Z_GAMMA><<<grd, blk, 0, st>>>(p, a); return;
+        case Z_KAPPA | Z_GAMMA: k_step_bulk<T, COEF, Z_KAPPA | Z_GAMMA><<<grd, blk, 0, st>>>(p, a); return;
+        default: break;
+        }
+    }
+    k_step_bulk<T, COEF><<<grd, blk, 0, st>>>(p, a);
+}
+
 template <class T>
 void launch_step_fast(const DevParams &p, const FastArgs<T> &a, int coef_mode, long long time, cudaStream_t st)
 {
     constexpr int V = Vec<T>::n;
     dim3 blk(64, 4), grd((p.pitch / V + 63) / 64, (p.nx - 2 + 3) / 4);
     const int nedge = 2 * p.nx + 2 * (p.ny - 2) + 1;
-    // FP64 with KAPPA = 0: the bulk update without its kappa term (values unchanged)
-    bool kz = false;
-    if constexpr (sizeof(T) == 8) kz = p.kappa == 0.0;
     if (coef_mode == WG_COEF_MASK) {
-        if constexpr (sizeof(T) == 8)
-            if (kz) k_step_bulk<T, WG_COEF_MASK, true><<<grd, blk, 0, st>>>(p, a);
-        if (!kz) k_step_bulk<T, WG_COEF_MASK><<<grd, blk, 0, st>>>(p, a);
+        launch_bulk<T, WG_COEF_MASK>(p, a, grd, blk, st);
         k_step_edge<T, WG_COEF_MASK><<<(nedge + 255) / 256, 256, 0, st>>>(p, a, time);
     } else {
-        if constexpr (sizeof(T) == 8)
-            if (kz) k_step_bulk<T, WG_COEF_TABLE, true><<<grd, blk, 0, st>>>(p, a);
-        if (!kz) k_step_bulk<T, WG_COEF_TABLE><<<grd, blk, 0, st>>>(p, a);
+        launch_bulk<T, WG_COEF_TABLE>(p, a, grd, blk, st);
         k_step_edge<T, WG_COEF_TABLE><<<(nedge + 255) / 256, 256, 0, st>>>(p, a, time);
     }
 }
