@@ -262,7 +262,7 @@ def run_ours(args):
                     "energy_rel_drift_max": float(drift),
                     "energy_rel_drift_final": float(abs(e32[-1] - e64[-1]) / abs(e64[-1])),
                     "updates": args.steps * UPDATES_PER_STEP,
-                    "against": "the FP64 GPU form on the same run (bit-identical to the FP64 oracle in the parity tests)"}
+                    "against": "the FP64 GPU form on the same run (value-identical to the FP64 oracle in the parity tests)"}
 
     # end to end through the C ABI with pinned host buffers (FP32)
     s = make_scene("fp32")
