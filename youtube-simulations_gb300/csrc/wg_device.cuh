@@ -1,9 +1,10 @@
 // wg_device.cuh — device-side parameters and the per-cell rules of the reference's
 // stepper (wave_billiard.c:302-610), shared by every stepping kernel.
 //
-// Arithmetic of the FP64 forms uses __dadd_rn/__dsub_rn/__dmul_rn so that nothing is
-// contracted into an FMA and every operation happens in the reference's order: the
-// device result is then bit-identical to the CPU reference built without FMA.
+// Arithmetic of the FP64 forms uses __dadd_rn/__dsub_rn/__dmul_rn so that the compiler
+// contracts nothing into an FMA and every operation happens in the reference's order:
+// the device result is then bit-identical to the CPU reference built without FMA.  The
+// only fused operations are the explicit P2_ / L4_ below, whose products are exact.
 #pragma once
 #include <cstdint>
 #include <cuda_runtime.h>
@@ -31,7 +32,7 @@ struct DevParams {
 };
 
 // ---------------------------------------------------------------------------
-// Exactly rounded double operations (never contracted).
+// Exactly rounded double operations (never contracted by the compiler).
 // ---------------------------------------------------------------------------
 __device__ __forceinline__ double A_(double a, double b) { return __dadd_rn(a, b); }
 __device__ __forceinline__ double S_(double a, double b) { return __dsub_rn(a, b); }
