@@ -32,6 +32,8 @@ def members(seed, count=10):
             p.src_on, p.src_i, p.src_j, p.src_amp, p.src_period = 1, int(si), int(sj), 0.05, 23.0
         if k % 5 == 2:
             p.twospeeds, p.courantb, p.gammab = 1, p.courant / 1.5, 1e-4
+        if k % 7 == 3:
+            p.kappa = 1e-3  # every term of the update present (FP64: no zero-term form)
         f = dict(phi=sc.phi, psi=sc.psi * 0.99, tmp=np.zeros_like(sc.phi))
         f = equalize_unwritten(p, f, sc.xy)
         out.append((p, f, sc.xy))
