@@ -28,6 +28,8 @@ ROOT = Path(__file__).resolve().parent
 NX, NY, UPDATES_PER_STEP = 3840, 2160, 100
 METRIC = "Gcell-updates/s"
 CELLS = NX * NY
+# the scene both arms step (scenes.config2, seed 0 on rank 0)
+WORKLOAD = f"single grid {NX}x{NY}, 64 discs n=1.5 via tcc table, absorbing, GAMMA 1e-4, point source"
 
 
 def _package():
@@ -162,8 +164,8 @@ def run_reference(args):
             "warmup": args.warmup, "ms_per_step": 1e3 * total / len(times), "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
             "impl": "reference",
-            "config": {"workload": f"single grid {NX}x{NY}, 64 discs n=1.5, absorbing, point source",
-                       "updates_per_step": upd, "parallelism": f"openmp x{th}"},
+            "config": {"workload": f"{WORKLOAD}; step = a {upd}-update sample of the reference's stepping loop",
+                       "updates_per_step": upd, "cells": CELLS, "parallelism": f"openmp x{th}"},
             "cpu_baseline": {"value": value, "unit": METRIC, "cores": th, "kind": "reference",
                              "sample": f"{upd} updates of the {NX}x{NY} grid per step (stepping loop only)"},
             "e2e": {"value": value, "unit": METRIC, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
@@ -330,8 +332,7 @@ def run_ours(args):
         "metric": METRIC, "value": r32["value"], "unit": METRIC, "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": r32["ms"], "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded discs, pulse and source)",
-        "config": {"workload": f"single grid {NX}x{NY}, 64 discs n=1.5 via tcc table, absorbing, GAMMA 1e-4, "
-                               f"point source; step = {UPDATES_PER_STEP} updates + FP64 energy report",
+        "config": {"workload": f"{WORKLOAD}; step = {UPDATES_PER_STEP} updates + FP64 energy report",
                    "updates_per_step": UPDATES_PER_STEP, "cells": CELLS, "parallelism": f"replicas x{world}",
                    "l2": "flushed (256 MB write) before every timed step",
                    "temporal_block": r32["blocking"][0], "tile": list(r32["blocking"][1:])},
