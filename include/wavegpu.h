@@ -204,7 +204,11 @@ typedef struct wg_scene wg_scene;
 
 /* Creates a scene with device buffers for phi/psi, the packed mask and coefficients.
  * precision: WG_FP64 or WG_FP32.  coef_mode: WG_COEF_MASK or WG_COEF_TABLE.
- * stream: cudaStream_t to run on (NULL = a stream owned by the scene). */
+ * stream: cudaStream_t to run on (NULL = a stream owned by the scene).
+ * FP64 scenes give the values of the reference's stepper (evolve_wave_half,
+ * wave_billiard.c:302-610).  Where KAPPA = 0, or GAMMA is 0 on every cell, the zero
+ * term is left out of the update, so a zero result may differ in sign only; with
+ * every term present the fields are bit-identical.  The drop-in keeps every term. */
 wg_status wg_scene_create(const wg_params *p, int32_t precision, int32_t coef_mode,
                           void *stream, wg_scene **out);
 wg_status wg_scene_destroy(wg_scene *s);
