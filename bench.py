@@ -123,6 +123,21 @@ def whole_job_rate(world, cells, updates, t_ms):
 _REF_META = {}
 
 
+def active_cells(params, xy):
+    """Cells the bulk rule updates (wave_billiard.c:365): every cell when TWOSPEEDS, else
+    the cells with xy > 0.  The metric counts all grid cells; this is the active share."""
+    import numpy as np
+    if params.twospeeds:
+        return int(params.nx) * int(params.ny)
+    return int(np.count_nonzero(np.asarray(xy) > 0))
+
+
+def with_active_rate(res, active, cells):
+    """Adds the active-cell rate (the same run counted over active cells only)."""
+    res["active_cell_rate"] = res["value"] * active / cells
+    return res
+
+
 def reference_sample(updates, threads=None):
     """Times `updates` updates of the reference's own stepper (compiled from its sources,
     OpenMP on the host cores) on the workload's grid, discs, pulse and source."""
@@ -201,6 +216,7 @@ def run_ours(args):
 
     # replicas: every rank advances its own instance of the workload (seed = rank)
     sc = scenes.config2(seed=rank, nx=NX, ny=NY)
+    n_act = active_cells(sc.params, sc.xy)
     flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)  # > L2 (126 MB)
 
     def make_scene(prec):
@@ -345,6 +361,8 @@ def run_ours(args):
                                    "(CUDA events); with temporal blocking this effective rate can pass the copy peak",
                      "dram_gbs": (traffic / r32["per_launch_s"] / 1e9) if traffic else None,
                      "kernel": kernel},
+        "active_cells": {"cells": n_act, "share": n_act / CELLS, "fp32_rate": r32["value"] * n_act / CELLS,
+                         "definition": "cells the bulk rule updates: all when TWOSPEEDS, else xy > 0"},
         "cpu_baseline": cpu,
         "e2e": {"value": e2e_value, "unit": METRIC, "h2d_bytes_per_step": 2 * CELLS * 4,
                 "d2h_bytes_per_step": 2 * CELLS * 4 + 8},
@@ -384,6 +402,7 @@ def run_batch(args, P, scenes, W, stream, rank):
     import torch
     rng = np.random.default_rng(1000 + rank)
     members = [scenes.batch_member(rng) for _ in range(args.batch_instances)]
+    active = sum(active_cells(m.params, m.xy) for m in members)
     out, prec_depths, energies = {}, {}, {}
     frames = args.batch_frames
     for prec in ("fp32", "fp64"):
@@ -402,13 +421,15 @@ def run_batch(args, P, scenes, W, stream, rank):
         e1.synchronize()
         ms = e0.elapsed_time(e1)
         energies[prec] = np.array([b.energy(s) for s in slots])
-        out[prec] = {"value": cells * 10 * frames / (ms / 1e3) / 1e9, "unit": METRIC, "ms_per_frame": ms / frames,
-                     "gpu_launches": b.launches() - l0, "frames": frames}
+        out[prec] = with_active_rate({"value": cells * 10 * frames / (ms / 1e3) / 1e9, "unit": METRIC,
+                                      "ms_per_frame": ms / frames, "gpu_launches": b.launches() - l0,
+                                      "frames": frames}, active, cells)
         if prec == "fp32":
             prec_depths = tuned_blocking(b)
         b.close()
     out["instances"] = n_active
     out["cells"] = cells
+    out["active_cells"] = active
     out["updates"] = 10 * (frames + 3)
     out["workload"] = ("uneven batch: 256 instances log-uniform 256x256..1280x720, mixed masks, Dirichlet/periodic, "
                        "frame of 10 updates as a CUDA graph: FP32 Dirichlet scenes in skewed passes at the depth tuned "
@@ -432,6 +453,7 @@ def run_sweep(args, P, scenes, W, stream, rank):
     import torch
     rng = np.random.default_rng(3000 + rank)
     members = [scenes.sweep_member(rng) for _ in range(args.sweep_instances)]
+    active = sum(active_cells(m.params, m.xy) for m in members)
     frames = max(4, args.sweep_steps // 10)
     out, fields = {}, {}
     for prec in ("fp32", "fp64"):
@@ -449,8 +471,9 @@ def run_sweep(args, P, scenes, W, stream, rank):
         e1.record(stream)
         e1.synchronize()
         ms = e0.elapsed_time(e1)
-        out[prec] = {"value": cells * 10 * (frames - 3) / (ms / 1e3) / 1e9, "unit": METRIC,
-                     "ms_per_frame": ms / (frames - 3), "gpu_launches": b.launches() - l0}
+        out[prec] = with_active_rate({"value": cells * 10 * (frames - 3) / (ms / 1e3) / 1e9, "unit": METRIC,
+                                      "ms_per_frame": ms / (frames - 3), "gpu_launches": b.launches() - l0},
+                                     active, cells)
         if prec == "fp32":
             out["fp32"]["blocking_per_size_class"] = tuned_blocking(b)
         fields[prec] = [b.download(s)[0] for s in slots]
@@ -458,7 +481,7 @@ def run_sweep(args, P, scenes, W, stream, rank):
     err = np.array([np.max(np.abs(a - b)) for a, b in zip(fields["fp32"], fields["fp64"])])
     rel = np.array([np.max(np.abs(a - b)) / max(np.max(np.abs(b)), 1e-300)
                     for a, b in zip(fields["fp32"], fields["fp64"])])
-    out.update({"instances": n_active, "cells": cells, "updates": 10 * frames,
+    out.update({"instances": n_active, "cells": cells, "active_cells": active, "updates": 10 * frames,
                 "max_abs_err_vs_fp64": {"max": float(err.max()), "p50": float(np.median(err)),
                                         "p99": float(np.quantile(err, 0.99)),
                                         "max_rel_to_field_max": float(rel.max())},
