@@ -3,8 +3,8 @@ device-side tile work queue, frames replayed as CUDA graphs.
 
 Batch invariance: every instance gives bit-identical fields in a batch (with other
 instances admitted and removed around it) and alone (a native scene on the
-single-step kernels), in FP32 and FP64.  FP64 batches also match the oracle bit for
-bit (1e-12 relative where cos/exp/sin sources enter)."""
+single-step kernels), in FP32 and FP64.  FP64 batches also match the oracle's values
+(1e-12 relative where cos/exp/sin sources enter)."""
 import numpy as np
 import pytest
 
