@@ -200,6 +200,13 @@ wg_status wg_compute_energy_device_noalloc(const wg_params *p, const double *phi
 /* ------------------------------------------------------------------------- */
 /* 2. Native handle API: resident scenes                                       */
 /* ------------------------------------------------------------------------- */
+/* No counterpart in the reference's interface, which is one compile-time grid per
+ * program stepped through host arrays (wave_billiard.c:613-631 from animation(),
+ * :897-899).  A scene holds one such grid on the device with runtime sizes: upload
+ * replaces the set-up of phi/psi/xy_in and the tables (init_ior_2d, sub_wave.c:12983-
+ * 13002), step replaces the evolve_wave loop, energy replaces compute_energy /
+ * compute_energy_x / compute_energy_tblr, frames replace draw_wave_highres_palette
+ * (wave_common.c:1750-1848) without GL. */
 typedef struct wg_scene wg_scene;
 
 /* Creates a scene with device buffers for phi/psi, the packed mask and coefficients.
@@ -325,6 +332,8 @@ wg_status wg_scene_add_circular_wave(wg_scene *s, double init_amp, double factor
 /* ------------------------------------------------------------------------- */
 /* 3. Batches of uneven scenes: one persistent launch over a tile work queue   */
 /* ------------------------------------------------------------------------- */
+/* No counterpart in the reference (one grid per process): many scenes of different
+ * sizes and parameters stepped together, each by the reference's rules. */
 typedef struct wg_batch wg_batch;
 wg_status wg_batch_create(int32_t precision, void *stream, wg_batch **out);
 wg_status wg_batch_destroy(wg_batch *b);
@@ -356,6 +365,8 @@ wg_status wg_batch_launch_count(wg_batch *b, int64_t *n);
 /* ------------------------------------------------------------------------- */
 /* 4. Serving loop: continuous batching of scene requests under an HBM budget  */
 /* ------------------------------------------------------------------------- */
+/* No counterpart in the reference: requests admitted into a running batch, each frame
+ * colour-mapped as the reference's P_AMPLITUDE drawing does (wave_common.c:1053-1065). */
 typedef struct wg_server wg_server;
 typedef struct wg_server_config {
     int32_t precision;        /* WG_FP32 or WG_FP64 */
