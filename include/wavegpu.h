@@ -397,7 +397,8 @@ wg_status wg_server_submit(wg_server *s, const wg_params *p, const double *phi, 
  * launch for all of them), render and copy every scene's frame to host memory, retire
  * finished requests.  *frames_out = frames produced. */
 wg_status wg_server_tick(wg_server *s, int32_t *frames_out);
-/* The latest frame of a request (valid until the next tick). */
+/* The latest frame of a request.  Valid until the next tick that renders frames; after
+ * it the call returns WG_ERR_STATE (the host buffer holds that tick's frames). */
 wg_status wg_server_frame(wg_server *s, int64_t request_id, uint8_t *rgb, int32_t *frame_index,
                           int32_t *width, int32_t *height);
 /* Final phi/psi of a finished request submitted with keep_result. */

@@ -90,6 +90,7 @@ struct ServeReq {
     std::vector<double> phi, psi;
     std::vector<int16_t> xy;
     int frames = 0, keep = 0, state = WG_REQ_QUEUED, slot = -1, frames_done = 0, last_index = -1;
+    int64_t frame_tick = -1;  // the tick that rendered last_index into the host buffer
     double t_submit = 0.0, t_first = -1.0;
     uint64_t bytes = 0;
     int w = 0, h = 0;
@@ -296,6 +297,7 @@ wg_status wg_server_tick(wg_server *s, int32_t *frames_out)
         cells += (long long)r.p.nx * r.p.ny;
         r.frames_done++;
         r.last_index = r.frames_done - 1;
+        r.frame_tick = s->ticks;
         s->lat_ms.push_back(lat);
         if (r.t_first < 0.0) {
             r.t_first = t1;
@@ -342,6 +344,11 @@ wg_status wg_server_frame(wg_server *s, int64_t id, uint8_t *rgb, int32_t *frame
     if (it == s->reqs.end()) { set_error("unknown request %lld", (long long)id); return WG_ERR_NOTFOUND; }
     const ServeReq &r = it->second;
     if (r.last_index < 0) { set_error("request %lld has no frame yet", (long long)id); return WG_ERR_STATE; }
+    if (r.frame_tick != s->ticks - 1) {  // a later tick has rendered over the host buffer
+        set_error("the last frame of request %lld (tick %lld) was overwritten by tick %lld: read frames before the "
+                  "next tick", (long long)id, (long long)r.frame_tick, (long long)(s->ticks - 1));
+        return WG_ERR_STATE;
+    }
     if (width) *width = r.w;
     if (height) *height = r.h;
     if (frame_index) *frame_index = r.last_index;

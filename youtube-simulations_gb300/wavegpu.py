@@ -560,6 +560,8 @@ class Server:
         return st.value, fd.value
 
     def frame(self, rid):
+        """(frame index, RGB8 image) of the request's latest frame; read it before the next
+        tick renders over the host buffer (wg_server_frame refuses a stale frame)."""
         w, h, idx = _I32(), _I32(), _I32()
         check(lib().wg_server_frame(self.h, int(rid), None, ctypes.byref(idx), ctypes.byref(w), ctypes.byref(h)))
         out = np.empty((h.value, w.value, 3), np.uint8)
