@@ -1,6 +1,7 @@
 """Pins the CPU oracle against the reference itself, compiled headlessly from its own
-sources (oracle/build_ref.py).  Bit-for-bit equality is required for every FP64
-update, boundary rule, source schedule, Neumann gather, energy sum and setup table.
+sources (oracle/build_ref.py).  Bit-for-bit equality (every bit of every FP64 value,
+signs of zero included) is required for every update, boundary rule, source schedule,
+Neumann gather, energy sum and setup table.
 Skipped when the compiled reference is absent (tests/test_golden.py then pins the
 oracle against committed fixtures made by the same compiled reference)."""
 import numpy as np
@@ -14,6 +15,12 @@ from helpers import PULSE_CASES, params_of, pulse_inputs, variant_inputs
 pytestmark = pytest.mark.skipif(not refio.available("s_dir"), reason="compiled reference absent")
 
 STEP_VARIANTS = [n for n, v in ref_variants.VARIANTS.items() if v["kind"] == "wb_fn" and not v.get("dropin")]
+
+
+def same_bits(a, b):
+    """FP64 arrays equal in every bit (signs of zero and NaN payloads included)."""
+    a, b = np.ascontiguousarray(a, np.float64), np.ascontiguousarray(b, np.float64)
+    return a.shape == b.shape and np.array_equal(a.view(np.uint64), b.view(np.uint64))
 ENERGY_VARIANTS = [n for n, v in ref_variants.VARIANTS.items() if v["kind"] == "we_fn"]
 OSC_VARIANTS = [n for n, v in ref_variants.VARIANTS.items() if v["kind"] == "osc"]
 
@@ -26,9 +33,9 @@ def test_evolve_wave_bitexact(variant, nsteps):
     new, prev, third, t = oracle.run(p, f["phi"], f["psi"], f["tmp"], xy, f["tcc"], f["tc"], f["tgamma"],
                                      nsteps, nbc=nbc)
     assert t == nsteps
-    assert np.array_equal(new, ref["phi"])
-    assert np.array_equal(prev, ref["psi"])
-    assert np.array_equal(third, ref["tmp"])
+    assert same_bits(new, ref["phi"])
+    assert same_bits(prev, ref["psi"])
+    assert same_bits(third, ref["tmp"])
     assert oracle.energy_total(p, new, prev, xy, compensated=False) == ref["energy"]
 
 
@@ -40,7 +47,7 @@ def test_point_source_bitexact(variant):
     ref = refio.run(variant, p.nx, p.ny, refio.STEP, 40, fields=f, xy=xy,
                     src=(p.src_i, p.src_j, p.src_amp, p.src_period))
     new, prev, third, _ = oracle.run(p, f["phi"], f["psi"], f["tmp"], xy, f["tcc"], f["tc"], f["tgamma"], 40)
-    assert np.array_equal(new, ref["phi"]) and np.array_equal(prev, ref["psi"])
+    assert same_bits(new, ref["phi"]) and same_bits(prev, ref["psi"])
 
 
 @pytest.mark.parametrize("variant", OSC_VARIANTS)
@@ -49,7 +56,7 @@ def test_oscillating_bc_bitexact(variant):
     times = [1, 2, 3, 17, 100, 251, 999, 5000]
     ref = refio.run(variant, p.nx, p.ny, refio.OSC, times=times)
     mine = np.array([[oracle.oscillating_bc(p, t, j) for j in range(p.ny)] for t in times])
-    assert np.array_equal(mine, ref)
+    assert same_bits(mine, ref)
 
 
 @pytest.mark.parametrize("variant", ENERGY_VARIANTS)
@@ -63,13 +70,13 @@ def test_wave_energy_variant_bitexact(variant, nsteps):
     for s in range(1, nsteps + 1):
         oracle.evolve_wave_half_energy(p, s, bufs[cur], bufs[prv], bufs[fre], xy)
         cur, prv, fre = fre, cur, prv
-    assert np.array_equal(bufs[cur], ref["phi"])
-    assert np.array_equal(bufs[prv], ref["psi"])
-    assert np.array_equal(bufs[fre], ref["tmp"])
+    assert same_bits(bufs[cur], ref["phi"])
+    assert same_bits(bufs[prv], ref["psi"])
+    assert same_bits(bufs[fre], ref["tmp"])
     # compute_energy_x and compute_energy_tblr of the reference on the same state
-    assert np.array_equal(oracle.energy_x(p, bufs[cur], bufs[prv], xy), ref["energy_x"])
+    assert same_bits(oracle.energy_x(p, bufs[cur], bufs[prv], xy), ref["energy_x"])
     ileft, iright = box_limits(p, circles)
-    assert np.array_equal(oracle.energy_tblr(p, bufs[cur], bufs[prv], xy, ileft, iright), ref["tblr"])
+    assert same_bits(oracle.energy_tblr(p, bufs[cur], bufs[prv], xy, ileft, iright), ref["tblr"])
 
 
 def box_limits(p, circles):
@@ -100,8 +107,8 @@ def test_neumann_setup_bitexact(variant, domain, kw):
         assert np.array_equal(recs[name], ref["nbc"][name]), name
     # tables of init_ior_2d, which the reference builds before the ghosts are marked
     tcc, tc, tg = oracle.init_ior(p, xy0)
-    assert np.array_equal(tcc, ref["tcc"]) and np.array_equal(tg, ref["tgamma"])
-    assert np.array_equal(tc, ref["tc"])
+    assert same_bits(tcc, ref["tcc"]) and same_bits(tg, ref["tgamma"])
+    assert same_bits(tc, ref["tc"])
 
 
 def test_mask_and_tables_c2_discs():
@@ -116,7 +123,7 @@ def test_mask_and_tables_c2_discs():
     assert np.array_equal(xy, ref["xy"])
     assert np.array_equal(scenes.mask(p, 20, circles=discs), ref["xy"])
     tcc, tc, tg = scenes.tables(p, ref["xy"])
-    assert np.array_equal(tcc, ref["tcc"]) and np.array_equal(tc, ref["tc"]) and np.array_equal(tg, ref["tgamma"])
+    assert same_bits(tcc, ref["tcc"]) and same_bits(tc, ref["tc"]) and same_bits(tg, ref["tgamma"])
 
 
 @pytest.mark.parametrize("variant,domain,lam", [("c1", 1, 1.8), ("full_stadium", 2, 1.2)])
@@ -127,7 +134,7 @@ def test_mask_setup_bitexact(variant, domain, lam):
     assert np.array_equal(oracle.mask(p, domain, lam), ref["xy"])
     assert np.array_equal(scenes.mask(p, domain, lam=lam), ref["xy"])
     tcc, tc, tg = scenes.tables(p, ref["xy"])
-    assert np.array_equal(tcc, ref["tcc"]) and np.array_equal(tg, ref["tgamma"])
+    assert same_bits(tcc, ref["tcc"]) and same_bits(tg, ref["tgamma"])
 
 
 @pytest.mark.parametrize("variant,factor,x,y", PULSE_CASES)
@@ -140,6 +147,6 @@ def test_add_circular_wave_bitexact(variant, factor, x, y):
     ref = refio.run(variant, p.nx, p.ny, refio.PULSE, fields={"phi": phi, "psi": psi}, xy=xy, pulse=(factor, x, y))
     mine = oracle.add_circular_wave(p, m["INITIAL_AMP"], factor, x, y, m["INITIAL_VARIANCE"], m["INITIAL_WAVELENGTH"],
                                     phi, xy)
-    assert np.array_equal(mine, ref["phi"])
-    assert np.array_equal(psi, ref["psi"])
+    assert same_bits(mine, ref["phi"])
+    assert same_bits(psi, ref["psi"])
     assert not np.array_equal(mine, phi)
