@@ -44,6 +44,17 @@ def _package():
     return sys.modules[name]
 
 
+def kernel_source_digest():
+    """sha256 (first 16 hex digits) of the single-grid kernel sources; profiles/traffic.json
+    records the digest its ncu capture was made on, so a stale capture is not reported."""
+    import hashlib
+    h = hashlib.sha256()
+    csrc = ROOT / "youtube-simulations_gb300" / "csrc"
+    for name in ("wg_tb.cu", "wg_device.cuh", "wg_cells.cuh", "wg_tma.cuh"):
+        h.update((csrc / name).read_bytes())
+    return h.hexdigest()[:16]
+
+
 def bytes_per_cell_update(precision, coef):
     """Algorithmic bytes of one cell update (single-step compulsory traffic):
     read phi(t), psi(t-1), write phi(t+1), the 1-bit mask, and each spatially varying
@@ -138,6 +149,19 @@ def with_active_rate(res, active, cells):
     return res
 
 
+REF_BUILD_FLAGS = "gcc -O3 -fopenmp (the reference makefile's flags, default FP contraction)"
+
+
+def reference_variant():
+    """The timed reference build: the makefile's own flags (ref_c2_stock); the parity
+    build (ref_c2, contraction off) only if that one is absent."""
+    sys.path.insert(0, str(ROOT / "oracle"))
+    import refio
+    if refio.available("c2_stock"):
+        return "c2_stock", REF_BUILD_FLAGS
+    return "c2", "gcc -O2 -fopenmp -ffp-contract=off (the parity build)"
+
+
 def reference_sample(updates, threads=None):
     """Times `updates` updates of the reference's own stepper (compiled from its sources,
     OpenMP on the host cores) on the workload's grid, discs, pulse and source."""
@@ -149,7 +173,8 @@ def reference_sample(updates, threads=None):
         _REF_META.update(scenes.config2(seed=0, nx=NX, ny=NY).meta)
     m = _REF_META
     src = (m["source"][0], m["source"][1], 0.05, m["period"])
-    el, _, th = refio.time_reference("c2", NX, NY, updates, m["discs"], m["centre"], src=src, threads=threads)
+    el, _, th = refio.time_reference(reference_variant()[0], NX, NY, updates, m["discs"], m["centre"], src=src,
+                                     threads=threads)
     return el, th
 
 
@@ -159,10 +184,11 @@ def run_reference(args):
         return 0
     sys.path.insert(0, str(ROOT / "oracle"))
     import refio
-    if not refio.available("c2"):
+    if not (refio.available("c2") or refio.available("c2_stock")):
         print(json.dumps({"impl": "reference", "unavailable": "compiled reference (oracle/_ref) absent: "
                           "run oracle/build_ref.py where the reference sources are present"}))
         return 0
+    variant, flags = reference_variant()
     threads = os.cpu_count()
     upd = args.ref_updates
     _package()
@@ -170,7 +196,7 @@ def run_reference(args):
     m = scenes.config2(seed=0, nx=NX, ny=NY).meta
     src = (m["source"][0], m["source"][1], 0.05, m["period"])
     # one process: the reference's own set-up once, then warm-up and timed segments
-    segs, _, th = refio.time_reference("c2", NX, NY, upd, m["discs"], m["centre"], src=src, threads=threads,
+    segs, _, th = refio.time_reference(variant, NX, NY, upd, m["discs"], m["centre"], src=src, threads=threads,
                                        segments=args.warmup + args.steps + 1)
     times = segs[-args.steps:] if len(segs) > args.steps else segs
     total = sum(times)
@@ -181,7 +207,7 @@ def run_reference(args):
             "impl": "reference",
             "config": {"workload": f"{WORKLOAD}; step = a {upd}-update sample of the reference's stepping loop",
                        "updates_per_step": upd, "cells": CELLS, "parallelism": f"openmp x{th}"},
-            "cpu_baseline": {"value": value, "unit": METRIC, "cores": th, "kind": "reference",
+            "cpu_baseline": {"value": value, "unit": METRIC, "cores": th, "kind": "reference", "build": flags,
                              "sample": f"{upd} updates of the {NX}x{NY} grid per step (stepping loop only)"},
             "e2e": {"value": value, "unit": METRIC, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line))
@@ -254,12 +280,10 @@ def run_ours(args):
         return step_ms, energy_ms, wall, s.launches() - l0, ck, energies
 
     results = {}
-    finals = {}
     for prec in (["fp32", "fp64"] if not args.fp32_only else ["fp32"]):
         s = make_scene(prec)
         step_ms, energy_ms, wall, launches, ck, energies = timed(s, args.steps, args.warmup)
         k, ti, tj = s.blocking()
-        finals[prec] = s.download()[0]
         s.close()
         t_ms = max_over_ranks(step_ms + energy_ms, world, dev)
         updates = args.steps * UPDATES_PER_STEP
@@ -270,17 +294,7 @@ def run_ours(args):
                              step_ms=step_ms, energy_ms=energy_ms, wall=wall, launches=launches, clocks=ck,
                              blocking=(k, ti, tj), achieved_gbs=algo / per_launch_s / 1e9, per_launch_s=per_launch_s,
                              bytes_per_update=bytes_per_cell_update(prec, "table"), energies=energies)
-    accuracy = None
-    if "fp64" in results:
-        e32, e64 = results["fp32"]["energies"], results["fp64"]["energies"]
-        drift = max(abs(a - b) / abs(b) for a, b in zip(e32, e64))
-        f32, f64 = finals["fp32"], finals["fp64"]
-        accuracy = {"field_rel_err": float(abs(f32 - f64).max() / abs(f64).max()),
-                    "field_max_abs_err": float(abs(f32 - f64).max()),
-                    "energy_rel_drift_max": float(drift),
-                    "energy_rel_drift_final": float(abs(e32[-1] - e64[-1]) / abs(e64[-1])),
-                    "updates": args.steps * UPDATES_PER_STEP,
-                    "against": "the FP64 GPU form on the same run (value-identical to the FP64 oracle in the parity tests)"}
+    accuracy = run_accuracy(args, P, W, sc, stream) if (rank == 0 and not args.no_accuracy) else None
 
     # end to end through the C ABI with pinned host buffers (FP32)
     s = make_scene("fp32")
@@ -328,10 +342,15 @@ def run_ours(args):
     k32, ti32, tj32 = r32["blocking"]
     kernel = ("k_step_bulk<float, TABLE> + k_step_edge" if k32 <= 1 else
               "k_step_skew<TABLE>" if tj32 == 1 else "k_step_tb<TABLE>")
-    traffic = None
+    traffic, traffic_note = None, "no capture for this blocking"
     tf = ROOT / "profiles" / "traffic.json"
     if tf.exists():
-        traffic = json.loads(tf.read_text()).get(f"fp32_k{k32}_w{tj32}")
+        cap = json.loads(tf.read_text())
+        if cap.get("sources") != kernel_source_digest():
+            traffic_note = "stale: the kernel sources changed since the ncu capture (profiles/traffic.json)"
+        elif cap.get(f"fp32_k{k32}_w{tj32}"):
+            traffic = cap[f"fp32_k{k32}_w{tj32}"]
+            traffic_note = "ncu dram__bytes_read.sum + dram__bytes_write.sum per launch, captured on these sources"
     cpu = None
     if not args.no_cpu_baseline:
         try:
@@ -341,7 +360,7 @@ def run_ours(args):
                 upd = int(min(600, max(30, upd * 10.0 / max(el, 1e-3))))
                 el, th = reference_sample(upd)
             cpu = {"value": CELLS * upd / el / 1e9, "unit": METRIC, "cores": th, "kind": "reference",
-                   "sample": f"{upd} updates of the {NX}x{NY} grid (reference evolve_wave_half, OpenMP, stepping loop only)"}
+                   "build": reference_variant()[1], "sample": f"{upd} updates of the {NX}x{NY} grid (reference evolve_wave_half, OpenMP, stepping loop only)"}
         except Exception as exc:  # the compiled reference is absent on this machine
             cpu = {"value": None, "unit": METRIC, "cores": 0, "kind": "reference", "sample": f"unavailable: {exc}"}
     line = {
@@ -360,6 +379,7 @@ def run_ours(args):
                      "definition": "single-step algorithmic bytes x cell updates per launch / mean launch time "
                                    "(CUDA events); with temporal blocking this effective rate can pass the copy peak",
                      "dram_gbs": (traffic / r32["per_launch_s"] / 1e9) if traffic else None,
+                     "traffic_source": traffic_note,
                      "kernel": kernel},
         "active_cells": {"cells": n_act, "share": n_act / CELLS, "fp32_rate": r32["value"] * n_act / CELLS,
                          "definition": "cells the bulk rule updates: all when TWOSPEEDS, else xy > 0"},
@@ -383,6 +403,58 @@ def run_ours(args):
         line["serving"] = serve_res
     print(json.dumps(line))
     return 0
+
+
+ACCURACY_UPDATES, ACCURACY_REPORT = 10000, 100
+FIELD_TOL32, DRIFT_TOL32, TOL64 = 1e-5, 1e-6, 1e-12
+
+
+def run_accuracy(args, P, W, sc, stream):
+    """The workload's full 10^4 updates, energy every 100, against the reference's own
+    FP64 OpenMP stepper (compiled from its sources, oracle/_ref/bin/ref_c2) on the same
+    input bytes: FP32 field error relative to the field maximum and relative energy
+    difference at every report, FP64 the same; each against its stated tolerance.
+    Untimed, rank 0 only."""
+    import numpy as np
+    sys.path.insert(0, str(ROOT / "oracle"))
+    import refio
+    if not refio.available("c2"):
+        return {"against": "unavailable: compiled reference (oracle/_ref/bin/ref_c2) absent"}
+    p = sc.params
+    updates = args.accuracy_updates
+    fields = dict(phi=sc.phi, psi=sc.psi, tcc=sc.tcc, tc=sc.tc, tgamma=sc.tgamma)
+    t0 = time.perf_counter()
+    ref = refio.run("c2", p.nx, p.ny, refio.STEP, updates, fields=fields, xy=sc.xy,
+                    src=(p.src_i, p.src_j, p.src_amp, p.src_period), report=ACCURACY_REPORT, timeout=3600)
+    ref_s = time.perf_counter() - t0
+    out = {"against": "the reference's own FP64 OpenMP stepper (evolve_wave_half of wave_billiard.c, compiled "
+                      "from its sources with FP contraction off) on the same input bytes",
+           "updates": updates, "report_every": ACCURACY_REPORT, "reference_seconds": ref_s,
+           "reference_threads": ref["threads"]}
+    for prec, tol_f, tol_e in (("fp32", FIELD_TOL32, DRIFT_TOL32), ("fp64", TOL64, TOL64)):
+        s = W.Scene(p, P.FP32 if prec == "fp32" else P.FP64, P.COEF_TABLE, stream=stream.cuda_stream)
+        s.upload(sc.phi, sc.psi, sc.xy, sc.tcc, sc.tc, sc.tgamma)
+        if args.block and prec == "fp32":
+            s.set_blocking(*args.block)
+        energies = []
+        for _ in range(updates // ACCURACY_REPORT):
+            s.step(ACCURACY_REPORT)
+            energies.append(s.total_energy())
+        phi, psi = s.download()
+        s.close()
+        e = np.array(energies)
+        scale = float(np.max(np.abs(ref["phi"])))
+        ferr = float(np.max(np.abs(phi - ref["phi"])) / scale)
+        perr = float(np.max(np.abs(psi - ref["psi"])) / float(np.max(np.abs(ref["psi"]))))
+        drift = np.abs(e - ref["reports"]) / np.abs(ref["reports"])
+        out[prec] = {"field_rel_err": ferr, "psi_rel_err": perr,
+                     "field_max_abs_err": float(np.max(np.abs(phi - ref["phi"]))),
+                     "energy_rel_drift_max": float(drift.max()), "energy_rel_drift_final": float(drift[-1]),
+                     "field_tol": tol_f, "energy_tol": tol_e,
+                     "pass": bool(max(ferr, perr) <= tol_f and drift.max() <= tol_e)}
+    out["definition"] = ("field error = max |field - reference| / max |reference| after the run; energy drift = "
+                         "|E - E_ref| / |E_ref| at each report (E = sum of compute_energy over every cell)")
+    return out
 
 
 def tuned_blocking(b):
@@ -603,6 +675,9 @@ def main():
     ap.add_argument("--no-batch", action="store_true")
     ap.add_argument("--no-serving", action="store_true")
     ap.add_argument("--no-sweep", action="store_true")
+    ap.add_argument("--no-accuracy", action="store_true")
+    ap.add_argument("--accuracy-updates", type=int, default=ACCURACY_UPDATES,
+                    help="updates of the accuracy leg against the reference (a multiple of 100)")
     ap.add_argument("--sweep-instances", type=int, default=4096)
     ap.add_argument("--sweep-steps", type=int, default=2000)
     ap.add_argument("--batch-instances", type=int, default=256)

@@ -3,9 +3,9 @@
 
 Test infrastructure only.  Steps:
 
-1. ``snapshot``: when the reference checkout is present (REF_DIR, default
-   /root/reference), copy the C files its wave path is built from into
-   oracle/_ref/src/.  oracle/_ref/ is git-ignored (never committed) but travels with
+1. ``snapshot``: when a reference checkout is named (``--ref-dir DIR`` or the
+   REF_DIR environment variable), copy the C files its wave path is built from into
+   oracle/_ref/src/.  Without one, the existing snapshot is compiled.  oracle/_ref/ is git-ignored (never committed) but travels with
    the working tree, so a machine without the checkout can still compile it.
 2. ``generate``: for every configuration in oracle/ref_variants.py, write a
    translation unit into oracle/_ref/src/gen/ whose ``#define`` values are the
@@ -16,12 +16,15 @@ Test infrastructure only.  Steps:
    which lands outside row 0 when NX > NY, is guarded by ``if (NX <= NY)``.
 3. ``compile``: gcc -O2 -fopenmp -ffp-contract=off (no FMA contraction, no -march)
    of oracle/ref_driver.c around each unit, in parallel, into oracle/_ref/bin/.
+   Variants marked ``stock`` use the reference makefile's own flags instead
+   (gcc -O3 -fopenmp, the compiler's default contraction): those are timed as the CPU
+   baseline, never used for parity.
    The ``*__dropin`` variants are the same units with the reference's evolve_wave /
    evolve_wave_half replaced by include/wavegpu_dropin.h, linked to libwavegpu.so:
    the reference's own driver code stepping on the GPU (built once the library
    exists).
 
-Usage: python oracle/build_ref.py [--only NAME ...] [--jobs N]
+Usage: python oracle/build_ref.py [--ref-dir DIR] [--only NAME ...] [--jobs N]
 """
 import argparse
 import hashlib
@@ -37,7 +40,7 @@ HERE = Path(__file__).resolve().parent
 sys.path.insert(0, str(HERE))
 import ref_variants  # noqa: E402
 
-REF_DIR = Path(os.environ.get("REF_DIR", "/root/reference"))
+REF_DIR = Path(os.environ["REF_DIR"]) if os.environ.get("REF_DIR") else None
 OUT = HERE / "_ref"
 SRC = OUT / "src"
 GEN = SRC / "gen"
@@ -54,14 +57,15 @@ Q2_FROM = "phi_out[0][NX-1] = oscillating_bc(time, NX-1);"
 Q2_TO = "if (NX <= NY) phi_out[0][NX-1] = oscillating_bc(time, NX-1);"
 
 
-def snapshot():
-    """Copy the reference sources into oracle/_ref/src (when the checkout exists)."""
-    if not REF_DIR.is_dir():
+def snapshot(ref_dir=None):
+    """Copy the reference sources from the checkout `ref_dir` into oracle/_ref/src."""
+    ref_dir = Path(ref_dir) if ref_dir else REF_DIR
+    if ref_dir is None or not ref_dir.is_dir():
         return False
     SRC.mkdir(parents=True, exist_ok=True)
     manifest = []
     for name in SOURCES:
-        data = (REF_DIR / name).read_bytes()
+        data = (ref_dir / name).read_bytes()
         dst = SRC / name
         if not dst.exists() or dst.read_bytes() != data:
             dst.write_bytes(data)
@@ -168,7 +172,8 @@ def compile_one(name, spec, cc="gcc"):
     exe = BIN / f"ref_{name}"
     defs = {"wb_full": ["-DREF_KIND_WB", "-DREF_FULL"], "wb_fn": ["-DREF_KIND_WB"],
             "we_fn": ["-DREF_KIND_WE"], "osc": ["-DREF_KIND_OSC"]}[kind]
-    cmd = [cc, "-O2", "-fopenmp", "-ffp-contract=off", "-w", "-std=gnu99",
+    opt = ["-O3", "-fopenmp"] if spec.get("stock") else ["-O2", "-fopenmp", "-ffp-contract=off"]
+    cmd = [cc, *opt, "-w", "-std=gnu99",
            f"-I{STUBS}", f"-I{SRC}", f"-I{GEN}", f'-DREF_TU="{tu.name}"', *defs,
            str(HERE / "ref_driver.c"), "-o", str(exe), "-lm"]
     if spec.get("dropin"):
@@ -185,8 +190,8 @@ def available():
     return (SRC / "wave_billiard.c").exists()
 
 
-def build(only=None, jobs=None):
-    snapshot()
+def build(only=None, jobs=None, ref_dir=None):
+    snapshot(ref_dir)
     if not available():
         print("build_ref: reference sources not present; skipping", file=sys.stderr)
         return False
@@ -208,7 +213,8 @@ def build(only=None, jobs=None):
 
 if __name__ == "__main__":
     ap = argparse.ArgumentParser()
+    ap.add_argument("--ref-dir", help="reference checkout to snapshot from (default: $REF_DIR)")
     ap.add_argument("--only", nargs="*")
     ap.add_argument("--jobs", type=int)
     a = ap.parse_args()
-    sys.exit(0 if build(a.only, a.jobs) else 1)
+    sys.exit(0 if build(a.only, a.jobs, a.ref_dir) else 1)

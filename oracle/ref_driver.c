@@ -11,6 +11,8 @@
  * 4 doubles, circles, then the fields; see oracle/refio.py for the exact layout.
  * Modes: 0 STEP, 1 SETUP (full builds), 2 TIME, 3 OSC, 4 PULSE (full builds:
  * add_circular_wave(hd[0], hd[2], hd[3], phi, psi, xy_in) on the given fields).
+ * STEP with h[14] = R > 0 also reports the total energy (the sum of compute_energy
+ * over every cell) after every R updates; the reports follow the usual output.
  */
 #define main ref_main
 #include REF_TU
@@ -34,6 +36,22 @@ static void wr(FILE *f, const void *p, size_t n)
 
 #ifndef REF_KIND_OSC
 static t_neumann_bc drv_nbc[N_NEUMANN_POINTS];
+
+/* total energy of a field pair: compute_energy summed over every cell (rows in
+ * parallel, each row in order, then the rows in order) */
+static double total_energy(double **a, double **b, short int **xyr)
+{
+    static double rowsum[NX];
+    #pragma omp parallel for
+    for (int i = 0; i < NX; i++) {
+        double e = 0.0;
+        for (int j = 0; j < NY; j++) e += compute_energy(a, b, xyr, i, j);
+        rowsum[i] = e;
+    }
+    double e = 0.0;
+    for (int i = 0; i < NX; i++) e += rowsum[i];
+    return e;
+}
 #endif
 
 int main(int argc, char **argv)
@@ -46,7 +64,7 @@ int main(int argc, char **argv)
     rd(fi, h, sizeof h);
     rd(fi, hd, sizeof hd);
     const int64_t nx = h[1], ny = h[2], mode = h[3], nsteps = h[4], n_nbc = h[5];
-    const int64_t ncirc = h[6], src_on = h[9], src_i = h[10], src_j = h[11];
+    const int64_t ncirc = h[6], src_on = h[9], src_i = h[10], src_j = h[11], report = h[14];
     const double src_amp = hd[0], src_period = hd[1];
     if (h[0] != 0x57415645 || nx != NX || ny != NY) {
         fprintf(stderr, "ref_driver: header mismatch (built for %d x %d)\n", NX, NY);
@@ -91,6 +109,8 @@ int main(int argc, char **argv)
     double **phi = rows[0], **psi = rows[1], **tmp = rows[2];
     double **tcc = rows[3], **tc = rows[4], **tg = rows[5];
     double elapsed = 0.0;
+    int64_t nrep = 0;
+    double *reports = NULL;
     (void)tcc; (void)tc; (void)tg; (void)circ; (void)src_i; (void)src_j;
     (void)src_on; (void)src_amp; (void)src_period;
 
@@ -177,7 +197,8 @@ int main(int argc, char **argv)
         int cur = 0, prv = 1, fre = 2;
         double t0 = omp_get_wtime();
 #ifdef REF_KIND_WB
-        if (!src_on && nsteps % 3 == 0) {
+        if (report > 0) reports = calloc(nsteps / report + 1, sizeof(double));
+        if (!src_on && report <= 0 && nsteps % 3 == 0) {
             for (int64_t s = 0; s < nsteps / 3; s++) evolve_wave(phi, psi, tmp, xyrows, tcc, tc, tg, drv_nbc);
         } else {
             for (int64_t s = 0; s < nsteps; s++) {
@@ -185,6 +206,7 @@ int main(int argc, char **argv)
                 if (src_on) b[fre][src_i][src_j] += src_amp * sin(6.283185307179586 * (double)(s + 1) / src_period);
                 int nc = fre, np = cur, nf = prv;
                 cur = nc; prv = np; fre = nf;
+                if (report > 0 && (s + 1) % report == 0) reports[nrep++] = total_energy(b[cur], b[prv], xyrows);
             }
         }
 #else /* REF_KIND_WE */
@@ -200,7 +222,11 @@ int main(int argc, char **argv)
 #endif
         elapsed = omp_get_wtime() - t0;
         /* present the newest level as "phi", the previous one as "psi" */
+#ifdef REF_KIND_WB
+        if (!(nsteps % 3 == 0 && !src_on && report <= 0)) {
+#else
         if (!(nsteps % 3 == 0 && !src_on)) {
+#endif
             double *o0 = A[0], *o1 = A[1], *o2 = A[2];
             double *src[3] = {o0, o1, o2};
             double *newest = src[cur], *prev = src[prv], *third = src[fre];
@@ -241,6 +267,8 @@ int main(int argc, char **argv)
     wr(fo, &elapsed, sizeof elapsed);
     int64_t threads = omp_get_max_threads();
     wr(fo, &threads, sizeof threads);
+    wr(fo, &nrep, sizeof nrep);
+    wr(fo, reports, sizeof(double) * nrep);
     fclose(fo);
     return 0;
 #endif

@@ -45,6 +45,9 @@ VARIANTS = {
     # full programs
     "c1": dict(kind="wb_full", macros=C1),
     "c2": dict(kind="wb_full", macros=C2),
+    # config 2 built with the reference makefile's flags (-O3 -fopenmp, default FP
+    # contraction): the timed CPU baseline, not a parity pin
+    "c2_stock": dict(kind="wb_full", macros=C2, stock=True),
     "full_neu_ellipse": _v("wb_full", BC_NEUMANN=1, B_DOMAIN=1, LAMBDA=1.8),
     "full_neu_polygon": _v("wb_full", BC_NEUMANN=1, B_DOMAIN=8, LAMBDA=0.9, NPOLY=7, APOLY=0.3),
     "full_stadium": _v("wb_full", B_DOMAIN=2, LAMBDA=1.2, TWOSPEEDS=1, GAMMAB=2e-4),

@@ -2,14 +2,15 @@
 
 File layout read by oracle/ref_driver.c:
   int64[16]  magic 0x57415645, nx, ny, mode, nsteps, n_nbc, ncircles, ileft, iright,
-             src_on, src_i, src_j, n_times, 0, 0, 0
+             src_on, src_i, src_j, n_times, segments (TIME), report interval (STEP), 0
   double[4]  src_amp, src_period, 0, 0 (PULSE: factor, 0, x, y)
   double[3*ncircles] circles (xc, yc, r)
   mode OSC : int32[n_times]
   else     : double phi, psi, tmp, tcc, tc, tgamma [nx*ny each]; int16 xy [nx*ny];
              t_neumann_bc[n_nbc]
 Output (non-OSC): the six arrays, xy, int64 n_nbc + records, energy total,
-energy_x[nx], tblr[6], elapsed seconds, int64 threads.
+energy_x[nx], tblr[6], elapsed seconds, int64 threads, int64 n_reports + the total
+energy after every `report` updates (STEP with report > 0).
 """
 import os
 import subprocess
@@ -33,7 +34,7 @@ def _neumann_dtype():
 
 
 def run(variant, nx, ny, mode=STEP, nsteps=0, fields=None, xy=None, nbc=None, circles=None,
-        src=None, times=None, threads=None, timeout=600, pulse=None):
+        src=None, times=None, threads=None, timeout=600, pulse=None, report=0):
     circles = np.zeros((0, 3)) if circles is None else np.asarray(circles, np.float64)[:, :3]
     n_nbc = 0 if nbc is None else len(nbc)
     hdr = np.zeros(16, np.int64)
@@ -46,6 +47,7 @@ def run(variant, nx, ny, mode=STEP, nsteps=0, fields=None, xy=None, nbc=None, ci
         hdr[12] = len(times)
     if pulse is not None:  # PULSE: (factor, x, y) of add_circular_wave
         hd[0], hd[2], hd[3] = pulse
+    hdr[14] = int(report)
     with tempfile.TemporaryDirectory() as td:
         fin, fout = Path(td) / "in.bin", Path(td) / "out.bin"
         with open(fin, "wb") as f:
@@ -96,6 +98,10 @@ def run(variant, nx, ny, mode=STEP, nsteps=0, fields=None, xy=None, nbc=None, ci
     out["elapsed"] = float(np.frombuffer(raw, np.float64, 1, off)[0])
     off += 8
     out["threads"] = int(np.frombuffer(raw, np.int64, 1, off)[0])
+    off += 8
+    nrep = int(np.frombuffer(raw, np.int64, 1, off)[0])
+    off += 8
+    out["reports"] = np.frombuffer(raw, np.float64, nrep, off).copy()
     return out
 
 

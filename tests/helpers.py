@@ -14,12 +14,13 @@ def params_of(variant, **over):
     return P.make_params(nx, ny, **d)
 
 
-def variant_inputs(variant, seed=1, noisy_tmp=True, smooth=False):
+def variant_inputs(variant, seed=1, noisy_tmp=True, smooth=False, **over):
     """(params, fields dict, xy, nbc) for a variant: its mask, spatially varying
     tables, a pulse plus noise in phi/psi, and (optionally) noise in tmp so that
-    cells the stepper must not write are visible."""
+    cells the stepper must not write are visible.  `over` replaces parameter values
+    (e.g. oscillate_left=1 for a build of one oscillating_bc schedule)."""
     m = ref_variants.VARIANTS[variant]["macros"]
-    p = params_of(variant)
+    p = params_of(variant, **over)
     rng = np.random.default_rng(seed)
     dom = m["B_DOMAIN"]
     if dom == 20:

@@ -1,0 +1,170 @@
+"""Parity at the benchmark configurations, at their full sizes and lengths, against the
+reference itself (compiled from its sources by oracle/build_ref.py).
+
+Config 1: 1280x720 ellipse (semi-axes 1.8, 1), Dirichlet, COURANT 0.1, GAMMA 0, one
+seeded Gaussian pulse, psi = phi, 100 frames x 10 updates = 1000 updates
+(wave_billiard.c:302-631, driven at :882-899).  The mask and tables are the
+reference's own set-up (init_wave_flat, init_ior_2d); the pulse is the seeded host
+pulse, the same bytes on both sides.
+  * drop-in evolve_wave x 333 plus one evolve_wave_half: every bit of phi, psi and tmp
+    equals the reference's (signs of zero included);
+  * native FP64 scene: the reference's values (KAPPA = 0 and GAMMA = 0 leave out terms
+    that are exact zeros, so only the sign of a zero may differ);
+  * native FP32 scene: field error <= 1e-5 relative to the field maximum, energy
+    within 1e-6 relative at every 100-update report.
+
+Config 2: 3840x2160, 64 seeded discs of index 1.5 (TWOSPEEDS, COURANTB = COURANT/1.5),
+absorbing, GAMMA = 1e-4, the point source, 10^4 updates with the energy reported every
+100 updates.  The reference runs its own OpenMP stepper over the full 10^4 updates.
+  * FP32 scene (the bench's autotuned temporal blocking): field error <= 1e-5 relative
+    to the field maximum after 10^4 updates, relative energy difference <= 1e-6 at
+    every one of the 100 reports;
+  * FP64 scene: <= 1e-12 relative (CUDA's and glibc's sin of the source may differ in
+    the last bit), energies within 1e-12.
+The measured errors are printed (pytest -s shows them)."""
+import numpy as np
+import pytest
+
+import refio
+from helpers import params_of
+from youtube_simulations_gb300 import params as P
+from youtube_simulations_gb300 import scenes
+from youtube_simulations_gb300 import wavegpu as W
+
+pytestmark = pytest.mark.gpu
+
+FIELD_TOL32, DRIFT_TOL32 = 1e-5, 1e-6
+
+
+def bits(a):
+    return np.ascontiguousarray(a, np.float64).reshape(-1).view(np.uint64)
+
+
+def rel_to_max(a, ref):
+    return float(np.max(np.abs(np.asarray(a, np.float64) - ref)) / np.max(np.abs(ref)))
+
+
+def need(variant):
+    if not refio.available(variant):
+        pytest.skip(f"compiled reference ref_{variant} absent")
+
+
+# ---------------------------------------------------------------------------
+# Config 1
+# ---------------------------------------------------------------------------
+C1_UPDATES, C1_REPORT = 1000, 100
+
+
+@pytest.fixture(scope="module")
+def c1():
+    need("c1")
+    sc = scenes.config1(seed=0)
+    p = params_of("c1")
+    su = refio.run("c1", p.nx, p.ny, refio.SETUP)
+    f = dict(phi=sc.phi, psi=sc.psi, tmp=np.zeros_like(sc.phi), tcc=su["tcc"], tc=su["tc"], tgamma=su["tgamma"])
+    ref = refio.run("c1", p.nx, p.ny, refio.STEP, C1_UPDATES, fields=f, xy=su["xy"], report=C1_REPORT)
+    return p, f, su["xy"], ref
+
+
+def test_config1_dropin_bitwise(c1):
+    p, f, xy, ref = c1
+    W.configure(p)
+    W.set_mode(True)
+    W.set_dropin_time(0)
+    try:
+        rf = W.RowFields(p, f["phi"], f["psi"], f["tmp"], xy, f["tcc"], f["tc"], f["tgamma"])
+        for _ in range(C1_UPDATES // 3):
+            W.evolve_wave(rf)
+        W.evolve_wave_half(rf, src="phi", prev="psi", dst="tmp")
+        W.sync()
+        assert W.dropin_time() == C1_UPDATES
+    finally:
+        W.set_mode(False)
+    # after 999 updates the rotation is back at (phi, psi, tmp); update 1000 wrote tmp
+    assert np.array_equal(bits(rf.tmp), bits(ref["phi"]))
+    assert np.array_equal(bits(rf.phi), bits(ref["psi"]))
+    assert np.array_equal(bits(rf.psi), bits(ref["tmp"]))
+    print(f"\nconfig 1 drop-in FP64, {C1_UPDATES} updates: bit-identical to the reference")
+
+
+def test_config1_native_fp64_and_fp32(c1):
+    p, f, xy, ref = c1
+    out = {}
+    for prec in (P.FP64, P.FP32):
+        with W.Scene(p, prec, P.COEF_TABLE) as s:
+            s.upload(f["phi"], f["psi"], xy, f["tcc"], f["tc"], f["tgamma"])
+            energies = []
+            for _ in range(C1_UPDATES // C1_REPORT):
+                s.step(C1_REPORT)
+                energies.append(s.total_energy())
+            phi, psi = s.download()
+        out[prec] = (phi, psi, np.array(energies))
+    phi, psi, e64 = out[P.FP64]
+    assert np.array_equal(phi, ref["phi"]) and np.array_equal(psi, ref["psi"])
+    assert np.max(np.abs(e64 - ref["reports"]) / np.abs(ref["reports"])) <= 1e-12
+    phi, psi, e32 = out[P.FP32]
+    err = rel_to_max(phi, ref["phi"])
+    drift = float(np.max(np.abs(e32 - ref["reports"]) / np.abs(ref["reports"])))
+    print(f"\nconfig 1 FP64 scene: values equal the reference; FP32 scene: field {err:.2e}, energy {drift:.2e}")
+    assert err <= FIELD_TOL32
+    assert rel_to_max(psi, ref["psi"]) <= FIELD_TOL32
+    assert drift <= DRIFT_TOL32
+
+
+# ---------------------------------------------------------------------------
+# Config 2
+# ---------------------------------------------------------------------------
+C2_UPDATES, C2_REPORT = 10000, 100
+
+
+@pytest.fixture(scope="module")
+def c2():
+    need("c2")
+    sc = scenes.config2(seed=0)
+    p = params_of("c2")
+    for k in ("src_on", "src_i", "src_j", "src_amp", "src_period"):
+        setattr(p, k, getattr(sc.params, k))
+    m = sc.meta
+    su = refio.run("c2", p.nx, p.ny, refio.SETUP, circles=m["discs"])
+    assert np.array_equal(su["xy"], sc.xy)
+    f = dict(phi=sc.phi, psi=sc.psi, tmp=np.zeros_like(sc.phi), tcc=su["tcc"], tc=su["tc"], tgamma=su["tgamma"])
+    src = (p.src_i, p.src_j, p.src_amp, p.src_period)
+    ref = refio.run("c2", p.nx, p.ny, refio.STEP, C2_UPDATES, fields=f, xy=su["xy"], src=src, report=C2_REPORT,
+                    timeout=1800)
+    assert len(ref["reports"]) == C2_UPDATES // C2_REPORT
+    return p, f, su["xy"], ref
+
+
+def run_scene(p, f, xy, prec):
+    with W.Scene(p, prec, P.COEF_TABLE) as s:
+        s.upload(f["phi"], f["psi"], xy, f["tcc"], f["tc"], f["tgamma"])
+        energies = []
+        for _ in range(C2_UPDATES // C2_REPORT):
+            s.step(C2_REPORT)
+            energies.append(s.total_energy())
+        phi, psi = s.download()
+        blocking = s.blocking()
+    return phi, psi, np.array(energies), blocking
+
+
+def test_config2_fp32_10k_updates(c2):
+    p, f, xy, ref = c2
+    phi, psi, e32, blocking = run_scene(p, f, xy, P.FP32)
+    err = rel_to_max(phi, ref["phi"])
+    err_psi = rel_to_max(psi, ref["psi"])
+    drift = np.abs(e32 - ref["reports"]) / np.abs(ref["reports"])
+    print(f"\nconfig 2 FP32 ({blocking}), {C2_UPDATES} updates vs the reference: field {err:.2e} "
+          f"(psi {err_psi:.2e}), max abs {np.max(np.abs(phi - ref['phi'])):.2e}, energy drift max {drift.max():.2e} "
+          f"(final {drift[-1]:.2e})")
+    assert err <= FIELD_TOL32 and err_psi <= FIELD_TOL32
+    assert drift.max() <= DRIFT_TOL32
+
+
+def test_config2_fp64_10k_updates(c2):
+    p, f, xy, ref = c2
+    phi, psi, e64, _ = run_scene(p, f, xy, P.FP64)
+    err = rel_to_max(phi, ref["phi"])
+    de = float(np.max(np.abs(e64 - ref["reports"]) / np.abs(ref["reports"])))
+    print(f"\nconfig 2 FP64, {C2_UPDATES} updates vs the reference: field {err:.2e}, energy {de:.2e}")
+    assert err <= 1e-12 and rel_to_max(psi, ref["psi"]) <= 1e-12
+    assert de <= 1e-12

@@ -8,7 +8,9 @@ Checked through the C ABI on two calls in a row (different fields each time) aga
 the existing entry points on the same data: the total against an FP64 scene's
 wg_scene_energy, the six boxes against wg_compute_energy_tblr, the columns against
 wg_compute_energy_x_all, all within 1e-12 relative.  The device buffers here are
-allocated by the test (torch), not by the entry point.  This file is collected last."""
+allocated by the test (torch), not by the entry point, and the device's free memory is
+the same before and after the calls: the entry point itself allocates nothing.  This
+file is collected last."""
 import ctypes
 
 import numpy as np
@@ -50,14 +52,27 @@ def test_noalloc_energy_matches_existing_entry_points_twice():
     d_xy[:, :ny] = torch.from_numpy(xy.reshape(nx, ny)).to(dev)
     ileft, iright = nx // 5, (4 * nx) // 5
     L = W.lib()
+
+    def call_noalloc():
+        W.check(L.wg_compute_energy_device_noalloc(ctypes.byref(p), d_phi.data_ptr(), d_psi.data_ptr(),
+                                                   d_xy.data_ptr(), pitch, ileft, iright, d_out.data_ptr(), None))
+
+    # the first call in a process may load the library's device module (lazy loading);
+    # after it, further calls leave the device's free memory exactly as it was
+    call_noalloc()
+    torch.cuda.synchronize()
+    free_before = torch.cuda.mem_get_info(dev)[0]
+    for _ in range(3):
+        call_noalloc()
+    torch.cuda.synchronize()
+    assert torch.cuda.mem_get_info(dev)[0] == free_before
     for call, scale in enumerate((1.0, -2.5)):
         phi = f["phi"] * scale
         psi = f["psi"] * scale + 0.01 * call
         d_phi[:, :ny] = torch.from_numpy(phi.reshape(nx, ny)).to(dev)
         d_psi[:, :ny] = torch.from_numpy(psi.reshape(nx, ny)).to(dev)
         torch.cuda.synchronize()
-        W.check(L.wg_compute_energy_device_noalloc(ctypes.byref(p), d_phi.data_ptr(), d_psi.data_ptr(),
-                                                   d_xy.data_ptr(), pitch, ileft, iright, d_out.data_ptr(), None))
+        call_noalloc()
         torch.cuda.synchronize()
         out = d_out.cpu().numpy()
         total, boxes, cols = existing(p, phi, psi, xy, ileft, iright)

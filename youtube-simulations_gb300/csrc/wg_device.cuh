@@ -364,7 +364,9 @@ __device__ __forceinline__ double cell_energy(const DevParams &p, double x, doub
     return 0.0;
 }
 
-// Neumaier-compensated accumulator.
+// Neumaier-compensated accumulator (Neumaier's improvement of Kahan summation, 1974):
+// s is the running sum, c the sum of the rounding errors of every addition, taken
+// from whichever operand was larger in magnitude; the result is s + c.
 struct Neu {
     double s, c;
     __device__ __forceinline__ Neu() : s(0.0), c(0.0) {}

@@ -308,15 +308,39 @@ __device__ __forceinline__ float cell_energy32(float es2, float hc2, float hc2b,
     return 0.0f;
 }
 
+// Adds a lane's FP32 Kahan run (s - c) into an FP64 Neumaier accumulator and restarts it.
+__device__ __forceinline__ void flush_run(Neu &acc, float &s, float &c)
+{
+    acc.add(S_((double)s, (double)c));
+    s = 0.f;
+    c = 0.f;
+}
+
+// Merges the Neumaier accumulators of the 32 lanes into lane 0 (value and compensation
+// both travel, so nothing the lanes carried is dropped).
+__device__ __forceinline__ void warp_merge(Neu &a)
+{
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1) {
+        Neu o;
+        o.s = __shfl_down_sync(0xffffffffu, a.s, off);
+        o.c = __shfl_down_sync(0xffffffffu, a.c, off);
+        a.merge(o);
+    }
+}
+
 // One warp per column i, eight columns per block.  MASK: 0 = int16 (xy != 0), 1 =
 // "nonzero" bit plane.  Per cell compute_energy (wave_common.c:453-472): FP64 for FP64
-// fields, FP32 for FP32 fields.  Every cell energy is a sum of squares (>= 0), so plain
-// FP64 sums in a tree lose no more than a few ulps: each lane sums its cells (FP32
-// fields: a Kahan sum in FP32, turned into FP64 once), the warp sums its lanes, and
-// the block sums the six boxes of compute_energy_tblr (sub_wave_comp.c:1752-1800)
-// over its columns.  cols[i] = (sum over j < ny/2, sum over j >= ny/2);
-// part[6 b + k] = box k of block b (0..2 top left/mid/right, 3..5 bottom).
+// fields, FP32 for FP32 fields.  The reductions are FP64 and compensated (Neumaier):
+// FP64 fields add every cell energy into a per-lane Neumaier accumulator; FP32 fields
+// sum runs of 16 steps (64 cells per lane) in FP32 with Kahan and add each run into the
+// lane's FP64 Neumaier accumulator.  Lanes merge (value and compensation) into the
+// column sums of compute_energy_x (wave_energy.c:292-302); the block merges the six
+// boxes of compute_energy_tblr (sub_wave_comp.c:1752-1800) over its columns.
+// cols[i] = (sum over j < ny/2, sum over j >= ny/2); part[6 b + k] = box k of block b
+// (0..2 top left/mid/right, 3..5 bottom).
 #define ENERGY_COLS_PER_BLOCK 8
+#define ENERGY_RUN 16
 template <class T, int MASK>
 __global__ void __launch_bounds__(32 * ENERGY_COLS_PER_BLOCK)
     k_energy_cols(const __grid_constant__ DevParams p, const T *__restrict__ phi, const T *__restrict__ psi,
@@ -327,14 +351,14 @@ __global__ void __launch_bounds__(32 * ENERGY_COLS_PER_BLOCK)
     __shared__ int sbox[ENERGY_COLS_PER_BLOCK];
     const int wid = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int i = blockIdx.x * ENERGY_COLS_PER_BLOCK + wid;
-    double pb = 0.0, pt = 0.0;
+    Neu nb, nt;  // bottom (j < ny/2) and top halves of the column
     if (i < p.nx) {
         const int NX = p.nx, NY = p.ny, jmid = NY / 2;
         const size_t row = (size_t)i * p.pitch;
         const int ip = (i + 1 == NX) ? NX - 1 : i + 1, im = (i == 0) ? 0 : i - 1;
         const T *re = phi + (size_t)ip * p.pitch, *rw = phi + (size_t)im * p.pitch, *rc = phi + row, *ry = psi + row;
         const float es2 = (float)p.e_scale2, hc2 = (float)p.ehalf_c2, hc2b = (float)p.ehalf_c2b;
-        float kb = 0.f, kbc = 0.f, kt = 0.f, ktc = 0.f;  // FP32 Kahan sums (FP32 fields)
+        float kb = 0.f, kbc = 0.f, kt = 0.f, ktc = 0.f;  // FP32 Kahan runs (FP32 fields)
         if (sizeof(T) == 4 && MASK == 1) {
             // FP32 fields: four cells per lane and step as 16-byte loads of the rows i-1, i, i+1
             // and psi; the j-1 / j+1 neighbours from the adjacent lanes (the row pitch is a
@@ -342,7 +366,7 @@ __global__ void __launch_bounds__(32 * ENERGY_COLS_PER_BLOCK)
             const float *fc = (const float *)rc, *fy = (const float *)ry, *fe = (const float *)re,
                         *fw = (const float *)rw;
             const uint32_t *nzr = nz + (size_t)i * p.wpitch;
-            for (int base = 0; base < NY; base += 128) {
+            for (int base = 0, step = 0; base < NY; base += 128, step++) {
                 const int j0 = base + 4 * lane;
                 const float4 c4 = *reinterpret_cast<const float4 *>(fc + j0);
                 const float4 y4 = *reinterpret_cast<const float4 *>(fy + j0);
@@ -367,79 +391,100 @@ __global__ void __launch_bounds__(32 * ENERGY_COLS_PER_BLOCK)
                     if (j < jmid) kahan_add(kb, kbc, en);
                     else kahan_add(kt, ktc, en);
                 }
+                if ((step & (ENERGY_RUN - 1)) == ENERGY_RUN - 1) {
+                    flush_run(nb, kb, kbc);
+                    flush_run(nt, kt, ktc);
+                }
             }
-        } else
+        } else {
+            int step = 0;
 #pragma unroll 4
-        for (int j = lane; j < NY; j += 32) {
-            const int jp = (j + 1 == NY) ? NY - 1 : j + 1, jm = (j == 0) ? 0 : j - 1;
-            int m;
-            if (MASK == 0) m = xy[row + j] != 0;
-            else m = (nz[(size_t)i * p.wpitch + (j >> 5)] >> (j & 31)) & 1u;
-            if (sizeof(T) == 8) {
-                const double en = cell_energy(p, (double)rc[j], (double)ry[j], (double)re[j], (double)rw[j],
-                                              (double)rc[jp], (double)rc[jm], m);
-                if (j < jmid) pb += en; else pt += en;
-            } else {
-                const float en = cell_energy32(es2, hc2, hc2b, p.twospeeds, (float)rc[j], (float)ry[j], (float)re[j],
-                                               (float)rw[j], (float)rc[jp], (float)rc[jm], m);
-                if (j < jmid) kahan_add(kb, kbc, en);
-                else kahan_add(kt, ktc, en);
+            for (int j = lane; j < NY; j += 32, step++) {
+                const int jp = (j + 1 == NY) ? NY - 1 : j + 1, jm = (j == 0) ? 0 : j - 1;
+                int m;
+                if (MASK == 0) m = xy[row + j] != 0;
+                else m = (nz[(size_t)i * p.wpitch + (j >> 5)] >> (j & 31)) & 1u;
+                if (sizeof(T) == 8) {
+                    const double en = cell_energy(p, (double)rc[j], (double)ry[j], (double)re[j], (double)rw[j],
+                                                  (double)rc[jp], (double)rc[jm], m);
+                    if (j < jmid) nb.add(en); else nt.add(en);
+                } else {
+                    const float en = cell_energy32(es2, hc2, hc2b, p.twospeeds, (float)rc[j], (float)ry[j],
+                                                   (float)re[j], (float)rw[j], (float)rc[jp], (float)rc[jm], m);
+                    if (j < jmid) kahan_add(kb, kbc, en);
+                    else kahan_add(kt, ktc, en);
+                    if ((step & (4 * ENERGY_RUN - 1)) == 4 * ENERGY_RUN - 1) {
+                        flush_run(nb, kb, kbc);
+                        flush_run(nt, kt, ktc);
+                    }
+                }
             }
         }
         if (sizeof(T) == 4) {
-            pb = (double)kb - (double)kbc;
-            pt = (double)kt - (double)ktc;
+            flush_run(nb, kb, kbc);
+            flush_run(nt, kt, ktc);
         }
     }
-#pragma unroll
-    for (int off = 16; off > 0; off >>= 1) {
-        pb += __shfl_down_sync(0xffffffffu, pb, off);
-        pt += __shfl_down_sync(0xffffffffu, pt, off);
-    }
+    warp_merge(nb);
+    warp_merge(nt);
     if (lane == 0) {
-        if (i < p.nx) cols[i] = make_double2(pb, pt);
-        sh[wid][0] = pb;
-        sh[wid][1] = pt;
+        const double vb = nb.value(), vt = nt.value();
+        if (i < p.nx) cols[i] = make_double2(vb, vt);
+        sh[wid][0] = vb;
+        sh[wid][1] = vt;
         sbox[wid] = (i < ileft) ? 0 : (i < iright ? 1 : 2);
     }
     __syncthreads();
     if (threadIdx.x < 6) {
         const int k = threadIdx.x, box = k % 3, half = k < 3 ? 1 : 0;  // top boxes sum j >= ny/2
-        double acc = 0.0;
+        Neu acc;
 #pragma unroll
         for (int w = 0; w < ENERGY_COLS_PER_BLOCK; w++)
-            if (sbox[w] == box) acc += sh[w][half];
-        part[(size_t)blockIdx.x * 6 + k] = acc;
+            if (sbox[w] == box) acc.add(sh[w][half]);
+        part[(size_t)blockIdx.x * 6 + k] = acc.value();
     }
 }
 
 // out[0] = total, out[1..6] = boxes (top left/mid/right, bottom left/mid/right),
-// out[7..7+nx) = column sums over j < ny/2.  One block of 256 threads.
+// out[7..7+nx) = column sums over j < ny/2.  One block of 256 threads; every merge is an
+// FP64 Neumaier merge (value and compensation).
 __global__ void __launch_bounds__(256) k_energy_final(int nx, int nblocks, const double2 *__restrict__ cols,
                                                       const double *__restrict__ part, double *__restrict__ out)
 {
-    __shared__ double sh[6][8];
+    __shared__ double sh[6][8][2];
+    __shared__ double box[6];
     for (int i = threadIdx.x; i < nx; i += blockDim.x) out[7 + i] = cols[i].x;
-    double acc[6] = {0.0, 0.0, 0.0, 0.0, 0.0, 0.0};
+    Neu acc[6];
     for (int b = threadIdx.x; b < nblocks; b += blockDim.x)
 #pragma unroll
-        for (int k = 0; k < 6; k++) acc[k] += part[(size_t)b * 6 + k];
+        for (int k = 0; k < 6; k++) acc[k].add(part[(size_t)b * 6 + k]);
     const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
 #pragma unroll
     for (int k = 0; k < 6; k++) {
-#pragma unroll
-        for (int off = 16; off > 0; off >>= 1) acc[k] += __shfl_down_sync(0xffffffffu, acc[k], off);
-        if (lane == 0) sh[k][wid] = acc[k];
+        warp_merge(acc[k]);
+        if (lane == 0) {
+            sh[k][wid][0] = acc[k].s;
+            sh[k][wid][1] = acc[k].c;
+        }
     }
     __syncthreads();
     if (threadIdx.x < 6) {
-        double a = 0.0;
-        for (int w = 0; w < (int)(blockDim.x >> 5); w++) a += sh[threadIdx.x][w];
-        out[1 + threadIdx.x] = a;
-        sh[threadIdx.x][0] = a;
+        Neu a;
+        for (int w = 0; w < (int)(blockDim.x >> 5); w++) {
+            Neu o;
+            o.s = sh[threadIdx.x][w][0];
+            o.c = sh[threadIdx.x][w][1];
+            a.merge(o);
+        }
+        out[1 + threadIdx.x] = a.value();
+        box[threadIdx.x] = a.value();
     }
     __syncthreads();
-    if (threadIdx.x == 0) out[0] = ((sh[0][0] + sh[1][0]) + sh[2][0]) + ((sh[3][0] + sh[4][0]) + sh[5][0]);
+    if (threadIdx.x == 0) {
+        Neu t;
+        for (int k = 0; k < 6; k++) t.add(box[k]);
+        out[0] = t.value();
+    }
 }
 
 // ---------------------------------------------------------------------------
