@@ -572,7 +572,7 @@ def run_serving(args, P, scenes, W, stream, rank):
     request stream is served in FP32 and in plain FP64."""
     import numpy as np
     rng = np.random.default_rng(2000 + rank)
-    lut = np.random.default_rng(5).integers(0, 256, size=(256, 3), dtype=np.uint8)
+    lut, palette = frame_palette()
     n_req = args.serve_requests
     arrivals = np.cumsum(rng.exponential(1.0 / args.serve_rate, n_req)).astype(int)
     reqs = []
@@ -608,7 +608,25 @@ def run_serving(args, P, scenes, W, stream, rank):
                    f"256x256..2560x1440, U({args.serve_frames_min},{args.serve_frames_max}) frames of 10 updates, "
                    "150 GB budget, RGB8 frames (size 2) to host each tick")
     out["latency"] = "per frame: tick start to every resident scene's RGB8 frame in host memory"
+    out["palette"] = palette
     return out
+
+
+def frame_palette():
+    """(256x3 bytes, name): the reference's turbo palette (turbo_srgb_bytes of
+    turbo_colormap.c), read as data from the snapshot of the reference's sources kept
+    beside the compiled reference; a seeded byte table when that is absent (the frame
+    cost does not depend on the entries)."""
+    import re
+    import numpy as np
+    src = ROOT / "oracle" / "_ref" / "src" / "turbo_colormap.c"
+    if src.exists():
+        m = re.search(r"turbo_srgb_bytes\s*\[256\]\s*\[3\]\s*=\s*\{(.*?)\};", src.read_text(encoding="latin-1"), re.S)
+        if m:
+            vals = [int(v) for v in re.findall(r"\d+", m.group(1))]
+            if len(vals) == 768:
+                return np.array(vals, np.uint8).reshape(256, 3), "turbo_srgb_bytes of the reference"
+    return np.random.default_rng(5).integers(0, 256, size=(256, 3), dtype=np.uint8), "seeded 256x3 byte table"
 
 
 def run_probe(args):

@@ -13,6 +13,12 @@
  * add_circular_wave(hd[0], hd[2], hd[3], phi, psi, xy_in) on the given fields).
  * STEP with h[14] = R > 0 also reports the total energy (the sum of compute_energy
  * over every cell) after every R updates; the reports follow the usual output.
+ * 5 FRAME (full builds): the colours of draw_wave_highres_palette's sampled cells, from
+ * the reference's own wave_value (wave_common.c) with the palette COL_TURBO, for plot
+ * mode h[12], sampling step h[7], h[13] frames at times h[8], h[8]+1, ... on the given
+ * phi/psi (the running sums of the mean, average and flux modes carried between
+ * them), scale hd[0].  Output: the last frame's rgb doubles [NY/size][NX/size][3] and
+ * its values [NY/size][NX/size], then init_fade_table's factors at the same cells.
  */
 #define main ref_main
 #include REF_TU
@@ -23,7 +29,7 @@
 #include <string.h>
 #include <omp.h>
 
-enum { M_STEP = 0, M_SETUP = 1, M_TIME = 2, M_OSC = 3, M_PULSE = 4 };
+enum { M_STEP = 0, M_SETUP = 1, M_TIME = 2, M_OSC = 3, M_PULSE = 4, M_FRAME = 5 };
 
 static void rd(FILE *f, void *p, size_t n)
 {
@@ -164,6 +170,44 @@ int main(int argc, char **argv)
         return 0;
 #else
         fprintf(stderr, "TIME needs a full build\n");
+        return 3;
+#endif
+    }
+    if (mode == M_FRAME) {
+#if defined(REF_FULL) && defined(REF_KIND_WB)
+        const int size = (int)h[7], plot = (int)h[12];
+        const int64_t nframes = h[13] > 0 ? h[13] : 1, t0 = h[8];
+        const int w = NX / size, hh = NY / size;
+        double *te[NX], *ae[NX], *cs[NX];
+        double *flux = calloc((size_t)4 * NX * NY, sizeof(double));
+        double *fade = calloc(cells, sizeof(double));
+        double *rgbout = calloc((size_t)3 * w * hh, sizeof(double)), *valout = calloc((size_t)w * hh, sizeof(double));
+        for (int i = 0; i < NX; i++) {
+            te[i] = calloc(NY, sizeof(double));
+            ae[i] = calloc(NY, sizeof(double));
+            cs[i] = calloc(NY, sizeof(double));
+        }
+        init_fade_table(tcc, xyrows, fade);
+        for (int64_t f = 0; f < nframes; f++)
+            for (int i = 0; i < NX; i += size)
+                for (int j = 0; j < NY; j += size) {
+                    double rgb[3];
+                    const double v = wave_value(i, j, phi, psi, te, ae, flux, cs, xyrows, hd[0], (int)(t0 + f), plot,
+                                                COL_TURBO, rgb);
+                    if (f == nframes - 1 && i / size < w && j / size < hh) {
+                        const size_t k = (size_t)(j / size) * w + i / size;
+                        for (int c = 0; c < 3; c++) rgbout[3 * k + c] = rgb[c];
+                        valout[k] = v;
+                    }
+                }
+        wr(fo, rgbout, sizeof(double) * 3 * w * hh);
+        wr(fo, valout, sizeof(double) * w * hh);
+        for (int j = 0; j < hh; j++)
+            for (int i = 0; i < w; i++) wr(fo, &fade[(size_t)(i * size) * NY + j * size], sizeof(double));
+        fclose(fo);
+        return 0;
+#else
+        fprintf(stderr, "FRAME needs a full build\n");
         return 3;
 #endif
     }

@@ -51,6 +51,18 @@ VARIANTS = {
     "full_neu_ellipse": _v("wb_full", BC_NEUMANN=1, B_DOMAIN=1, LAMBDA=1.8),
     "full_neu_polygon": _v("wb_full", BC_NEUMANN=1, B_DOMAIN=8, LAMBDA=0.9, NPOLY=7, APOLY=0.3),
     "full_stadium": _v("wb_full", B_DOMAIN=2, LAMBDA=1.2, TWOSPEEDS=1, GAMMAB=2e-4),
+    # frames: wave_value with the C_ONEDIM scheme and the turbo palette (every plot mode),
+    # the frame parameters of wave_billiard.c; a second build with attenuation and the
+    # full colour range, a third with two speeds (drawn everywhere, fading by tcc)
+    "frame": _v("wb_full", NX=96, NY=64, B_DOMAIN=1, LAMBDA=1.8, COLOR_SCHEME=3, COLOR_PALETTE=10,
+                SLOPE=1.0, COLOR_RANGE=0.8, ATTENUATION=0.0, VSHIFT_AMPLITUDE=-0.2, VSCALE_AMPLITUDE=1.0,
+                LOG_SCALE=0.75, LOG_SHIFT=0.75, FLUX_SCALE=250.0, AVRG_E_FACTOR=0.95, RESCALE_COLOR_IN_CENTER=0),
+    "frame_att": _v("wb_full", NX=96, NY=64, B_DOMAIN=2, LAMBDA=1.2, COLOR_SCHEME=3, COLOR_PALETTE=10,
+                    SLOPE=1.5, COLOR_RANGE=1.0, ATTENUATION=0.01, VSHIFT_AMPLITUDE=0.1, VSCALE_AMPLITUDE=2.0,
+                    LOG_SCALE=0.5, LOG_SHIFT=1.0, FLUX_SCALE=100.0, AVRG_E_FACTOR=0.9, RESCALE_COLOR_IN_CENTER=0),
+    "frame_ts": _v("wb_full", NX=96, NY=64, B_DOMAIN=1, LAMBDA=1.8, TWOSPEEDS=1, COLOR_SCHEME=3, COLOR_PALETTE=10,
+                   SLOPE=1.0, COLOR_RANGE=0.8, ATTENUATION=0.0, VSHIFT_AMPLITUDE=-0.2, VSCALE_AMPLITUDE=1.0,
+                   LOG_SCALE=0.75, LOG_SHIFT=0.75, FLUX_SCALE=250.0, AVRG_E_FACTOR=0.95, RESCALE_COLOR_IN_CENTER=0),
     # hot path, every boundary rule
     "s_dir": _v("wb_fn", B_COND=0, KAPPA=0.001, FLOOR=1, VMAX=0.3),
     "s_per": _v("wb_fn", B_COND=1, TWOSPEEDS=1),

@@ -21,7 +21,7 @@ import numpy as np
 
 HERE = Path(__file__).resolve().parent
 BIN = HERE / "_ref" / "bin"
-STEP, SETUP, TIME, OSC, PULSE = 0, 1, 2, 3, 4
+STEP, SETUP, TIME, OSC, PULSE, FRAME = 0, 1, 2, 3, 4, 5
 
 
 def available(variant):
@@ -103,6 +103,37 @@ def run(variant, nx, ny, mode=STEP, nsteps=0, fields=None, xy=None, nbc=None, ci
     off += 8
     out["reports"] = np.frombuffer(raw, np.float64, nrep, off).copy()
     return out
+
+
+def frame(variant, nx, ny, phi, psi, xy, tcc, plot, size=2, frames=1, t0=0, scale=1.0, timeout=600):
+    """FRAME mode: the reference's wave_value colours (palette COL_TURBO) of the cells
+    draw_wave_highres_palette samples, after `frames` frames at times t0, t0+1, ...
+    Returns (rgb [ny/size][nx/size][3] doubles, values [ny/size][nx/size], fade factors
+    of init_fade_table at the same cells)."""
+    hdr = np.zeros(16, np.int64)
+    hdr[:7] = [0x57415645, nx, ny, FRAME, 0, 0, 0]
+    hdr[7], hdr[8], hdr[12], hdr[13] = size, t0, plot, frames
+    hd = np.zeros(4)
+    hd[0] = scale
+    n = nx * ny
+    with tempfile.TemporaryDirectory() as td:
+        fin, fout = Path(td) / "in.bin", Path(td) / "out.bin"
+        with open(fin, "wb") as f:
+            f.write(hdr.tobytes())
+            f.write(hd.tobytes())
+            for a in (phi, psi, np.zeros(n), tcc, np.zeros(n), np.zeros(n)):
+                f.write(np.ascontiguousarray(a, np.float64).reshape(-1).tobytes())
+            f.write(np.ascontiguousarray(xy, np.int16).reshape(-1).tobytes())
+        r = subprocess.run([str(BIN / f"ref_{variant}"), str(fin), str(fout)], capture_output=True, text=True,
+                           timeout=timeout)
+        if r.returncode != 0:
+            raise RuntimeError(f"ref_{variant} failed ({r.returncode}): {r.stderr[-1000:]}")
+        raw = fout.read_bytes()
+    w, h = nx // size, ny // size
+    rgb = np.frombuffer(raw, np.float64, 3 * w * h, 0).reshape(h, w, 3).copy()
+    vals = np.frombuffer(raw, np.float64, w * h, 24 * w * h).reshape(h, w).copy()
+    fade = np.frombuffer(raw, np.float64, w * h, 32 * w * h).reshape(h, w).copy()
+    return rgb, vals, fade
 
 
 def time_reference(variant, nx, ny, nsteps, circles, centre, src=None, threads=None, timeout=900, segments=1):

@@ -1,4 +1,7 @@
 """Shared test inputs: deterministic seeded scenes for every compiled-reference variant."""
+import re
+from pathlib import Path
+
 import numpy as np
 
 import oracle
@@ -111,3 +114,32 @@ def equalize_unwritten(p, f, xy, nbc=None):
     for k in ("psi", "tmp"):
         f[k] = np.where(w, f[k], f["phi"])
     return f
+
+
+_TURBO_SRC = Path(__file__).resolve().parents[1] / "oracle" / "_ref" / "src" / "turbo_colormap.c"
+
+
+def turbo_palette():
+    """The reference's turbo palette (turbo_colormap.c: turbo_srgb_bytes [256][3] and
+    turbo_srgb_floats [256][3]), read at run time from the snapshot of the reference's
+    sources that oracle/build_ref.py keeps beside the compiled reference (git-ignored,
+    never committed).  None when the snapshot is absent."""
+    if not _TURBO_SRC.exists():
+        return None
+    text = _TURBO_SRC.read_text(encoding="latin-1")
+
+    def table(name):
+        m = re.search(name + r"\s*\[256\]\s*\[3\]\s*=\s*\{(.*?)\};", text, re.S)
+        nums = re.findall(r"[-+]?\d*\.?\d+(?:[eE][-+]?\d+)?", m.group(1))
+        return np.array([float(x) for x in nums]).reshape(256, 3)
+    return table("turbo_srgb_bytes").astype(np.uint8), table("turbo_srgb_floats").astype(np.float32)
+
+
+def frame_lut(seed=0):
+    """The palette of the frame tests: the reference's turbo bytes where its snapshot is
+    present, else a seeded 256-entry byte table (the frame arithmetic does not depend on
+    the entries)."""
+    t = turbo_palette()
+    if t is not None:
+        return t[0]
+    return np.random.default_rng(seed).integers(0, 256, size=(256, 3), dtype=np.uint8)

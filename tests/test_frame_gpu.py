@@ -1,15 +1,16 @@
 """RGB8 frames of a scene (wg_scene_frame_rgb8) against the oracle's restatement of
 draw_wave_highres_palette / wave_value for every plot mode (amplitude, energy, mixed,
 mean, log, flux, total flux, average), with the running sums carried over frames.
-The palette is a seeded synthetic 256x3 byte table (the caller supplies the
-reference's own palette).  tanh, log and atan on the GPU and in numpy may differ in the
+The palette is the reference's turbo byte table (turbo_srgb_bytes, read at run time
+from the reference's sources beside the compiled reference; a seeded byte table where
+those are absent), the table test_frame_pin.py pins the oracle with.  tanh, log and atan on the GPU and in numpy may differ in the
 last bit, which can move a value across a palette boundary: a few pixels (0.1-0.2%)
 may differ."""
 import numpy as np
 import pytest
 
 import oracle
-from helpers import variant_inputs
+from helpers import frame_lut, variant_inputs
 from youtube_simulations_gb300 import params as P
 from youtube_simulations_gb300 import scenes
 from youtube_simulations_gb300 import wavegpu as W
@@ -18,7 +19,7 @@ pytestmark = pytest.mark.gpu
 
 
 def lut(seed=0):
-    return np.random.default_rng(seed).integers(0, 256, size=(256, 3), dtype=np.uint8)
+    return frame_lut(seed)
 
 
 @pytest.mark.parametrize("prec,coef", [(P.FP64, P.COEF_TABLE), (P.FP32, P.COEF_MASK), (P.FP32, P.COEF_TABLE)])

@@ -8,13 +8,13 @@ and each returned frame to the solo scene's frame at the same step."""
 import numpy as np
 import pytest
 
-from helpers import equalize_unwritten
+from helpers import equalize_unwritten, frame_lut
 from youtube_simulations_gb300 import params as P
 from youtube_simulations_gb300 import scenes
 from youtube_simulations_gb300 import wavegpu as W
 
 pytestmark = pytest.mark.gpu
-LUT = np.random.default_rng(7).integers(0, 256, size=(256, 3), dtype=np.uint8)
+LUT = frame_lut(7)
 
 
 def requests(seed, count):

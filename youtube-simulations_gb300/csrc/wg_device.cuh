@@ -71,20 +71,51 @@ __device__ __forceinline__ double absorb64(double x, double y, double tc, double
     return S_(r, M_(g, S_(x, y)));
 }
 
-// FP32 update in increment form: out = x + ((1-g)(x-y) + cc*delta - kappa*x) with the
-// Laplacian as differences from the centre.  Same mathematics as upd64.
+// FP32 update in increment form: out = x + ((1-g)(x-y) - kappa*x + cc*delta) with the
+// Laplacian as differences from the centre.  Same mathematics as upd64.  Every rounding
+// is spelled out as an explicit operation or fused multiply-add (nothing is left for the
+// compiler to contract), so the packed-pair form of the skewed kernels rounds each
+// element exactly the same way.
 __device__ __forceinline__ float upd32(float x, float y, float cc, float delta, float kappa, float g)
 {
-    float w = x - y;
-    float inc = fmaf(cc, delta, fmaf(-g, w, w) - kappa * x);
-    return x + inc;
+    const float w = __fsub_rn(x, y);
+    const float inc = fmaf(cc, delta, fmaf(-kappa, x, fmaf(-g, w, w)));
+    return __fadd_rn(x, inc);
 }
 // upd32 with KAPPA = 0: the kappa*x term is then an exact zero, so leaving it out changes
 // at most the sign of a zero result, never a value.
 __device__ __forceinline__ float upd32_k0(float x, float y, float cc, float delta, float g)
 {
-    float w = x - y;
-    return x + fmaf(cc, delta, fmaf(-g, w, w));
+    const float w = __fsub_rn(x, y);
+    return __fadd_rn(x, fmaf(cc, delta, fmaf(-g, w, w)));
+}
+
+// Packed FP32 pairs: one sm_100-family instruction (add/sub/fma .f32x2) works on
+// both elements of a float2, each rounded to nearest exactly as the scalar instruction.
+// Written as PTX with the explicit .rn modifier, which the code generator never fuses
+// with a neighbouring instruction (a product followed by a subtraction stays two
+// roundings, as in upd32).
+#define WG_F32X2_BINOP(name, op)                                                                      \
+    __device__ __forceinline__ float2 name(float2 a, float2 b)                                          \
+    {                                                                                                   \
+        float2 r;                                                                                       \
+        asm("{\n\t.reg .b64 ra, rb, rd;\n\tmov.b64 ra, {%2, %3};\n\tmov.b64 rb, {%4, %5};\n\t" op      \
+            " rd, ra, rb;\n\tmov.b64 {%0, %1}, rd;\n\t}"                                               \
+            : "=f"(r.x), "=f"(r.y)                                                                      \
+            : "f"(a.x), "f"(a.y), "f"(b.x), "f"(b.y));                                                  \
+        return r;                                                                                       \
+    }
+WG_F32X2_BINOP(add2, "add.rn.f32x2")
+WG_F32X2_BINOP(sub2, "sub.rn.f32x2")
+#undef WG_F32X2_BINOP
+__device__ __forceinline__ float2 fma2(float2 a, float2 b, float2 c)
+{
+    float2 r;
+    asm("{\n\t.reg .b64 ra, rb, rc, rd;\n\tmov.b64 ra, {%2, %3};\n\tmov.b64 rb, {%4, %5};\n\t"
+        "mov.b64 rc, {%6, %7};\n\tfma.rn.f32x2 rd, ra, rb, rc;\n\tmov.b64 {%0, %1}, rd;\n\t}"
+        : "=f"(r.x), "=f"(r.y)
+        : "f"(a.x), "f"(a.y), "f"(b.x), "f"(b.y), "f"(c.x), "f"(c.y));
+    return r;
 }
 __device__ __forceinline__ float absorb32(float x, float y, float tc, float nb, float k, float g)
 {
@@ -367,9 +398,9 @@ __device__ __forceinline__ double cell_energy(const DevParams &p, double x, doub
 // Neumaier-compensated accumulator (Neumaier's improvement of Kahan summation, 1974):
 // s is the running sum, c the sum of the rounding errors of every addition, taken
 // from whichever operand was larger in magnitude; the result is s + c.
+// An aggregate (no constructor, so it can live in shared memory): start it as {0.0, 0.0}.
 struct Neu {
     double s, c;
-    __device__ __forceinline__ Neu() : s(0.0), c(0.0) {}
     __device__ __forceinline__ void add(double x)
     {
         double t = A_(s, x);

@@ -11,6 +11,7 @@
 //  k_energy_cols  compute_energy (wave_common.c:453-472) per cell, one warp per
 //                 column: sums of j < ny/2 and j >= ny/2, box partials per block.
 //  k_energy_final total and the six compute_energy_tblr boxes from the partials.
+#include <type_traits>
 #include "wg_internal.h"
 #include "wg_cells.cuh"
 
@@ -288,13 +289,34 @@ __global__ void k_neumann_fast(DevParams p, const T *__restrict__ phi, T *__rest
 // ---------------------------------------------------------------------------
 // Energy
 // ---------------------------------------------------------------------------
-// Kahan step: s + c carries the running sum (c is minus the part lost so far).
-__device__ __forceinline__ void kahan_add(float &s, float &c, float x)
-{
-    const float y = x - c, t = s + y;
-    c = (t - s) - y;
-    s = t;
-}
+// Error-free FP32 double-word ("double-float") accumulator: h + l carries the running
+// sum to about 2^-48 relative.  Every addition is Knuth's TwoSum (the rounding error of
+// h + x, recovered exactly, goes into l); merges add the two high words by TwoSum and
+// renormalise.  All of it runs on the FP32 pipe: on this GPU an FP64 operation costs
+// about 64 FP32 operations, so the FP32 fields' sums stay off the FP64 pipe and are
+// converted to FP64 (exactly) only per column.
+// An aggregate like Neu: start it as {0.f, 0.f}.
+struct DF {
+    float h, l;
+    __device__ __forceinline__ void add(float x)
+    {
+        const float s = __fadd_rn(h, x);
+        const float bp = __fsub_rn(s, h);
+        const float e = __fadd_rn(__fsub_rn(h, __fsub_rn(s, bp)), __fsub_rn(x, bp));
+        h = s;
+        l = __fadd_rn(l, e);
+    }
+    __device__ __forceinline__ void merge(const DF &o)
+    {
+        const float s = __fadd_rn(h, o.h);
+        const float bp = __fsub_rn(s, h);
+        const float e = __fadd_rn(__fsub_rn(h, __fsub_rn(s, bp)), __fsub_rn(o.h, bp));
+        const float t = __fadd_rn(__fadd_rn(l, o.l), e);
+        h = __fadd_rn(s, t);                  // Fast2Sum renormalisation (|s| >= |t|)
+        l = __fsub_rn(t, __fsub_rn(h, s));
+    }
+    __device__ __forceinline__ double value() const { return A_((double)h, (double)l); }
+};
 
 // compute_energy in FP32 for FP32 fields (same formula and order as cell_energy).
 __device__ __forceinline__ float cell_energy32(float es2, float hc2, float hc2b, int twospeeds, float x, float psi,
@@ -308,57 +330,62 @@ __device__ __forceinline__ float cell_energy32(float es2, float hc2, float hc2b,
     return 0.0f;
 }
 
-// Adds a lane's FP32 Kahan run (s - c) into an FP64 Neumaier accumulator and restarts it.
-__device__ __forceinline__ void flush_run(Neu &acc, float &s, float &c)
-{
-    acc.add(S_((double)s, (double)c));
-    s = 0.f;
-    c = 0.f;
-}
-
-// Merges the Neumaier accumulators of the 32 lanes into lane 0 (value and compensation
-// both travel, so nothing the lanes carried is dropped).
+// Merges the accumulators of the 32 lanes into lane 0 (value and compensation travel).
 __device__ __forceinline__ void warp_merge(Neu &a)
 {
 #pragma unroll
     for (int off = 16; off > 0; off >>= 1) {
-        Neu o;
+        Neu o = {0.0, 0.0};
         o.s = __shfl_down_sync(0xffffffffu, a.s, off);
         o.c = __shfl_down_sync(0xffffffffu, a.c, off);
         a.merge(o);
     }
 }
+__device__ __forceinline__ void warp_merge(DF &a)
+{
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1) {
+        DF o = {0.f, 0.f};
+        o.h = __shfl_down_sync(0xffffffffu, a.h, off);
+        o.l = __shfl_down_sync(0xffffffffu, a.l, off);
+        a.merge(o);
+    }
+}
+__device__ __forceinline__ void acc_add(Neu &a, double x) { a.add(x); }
+__device__ __forceinline__ void acc_add(DF &a, float x) { a.add(x); }
+__device__ __forceinline__ void acc_merge(Neu &a, const Neu &o) { a.merge(o); }
+__device__ __forceinline__ void acc_merge(DF &a, const DF &o) { a.merge(o); }
 
 // One warp per column i, eight columns per block.  MASK: 0 = int16 (xy != 0), 1 =
 // "nonzero" bit plane.  Per cell compute_energy (wave_common.c:453-472): FP64 for FP64
-// fields, FP32 for FP32 fields.  The reductions are FP64 and compensated (Neumaier):
-// FP64 fields add every cell energy into a per-lane Neumaier accumulator; FP32 fields
-// sum runs of 16 steps (64 cells per lane) in FP32 with Kahan and add each run into the
-// lane's FP64 Neumaier accumulator.  Lanes merge (value and compensation) into the
+// fields, FP32 for FP32 fields.  Every reduction is compensated: FP64 fields add their
+// cell energies into FP64 Neumaier accumulators; FP32 fields into the error-free FP32
+// double-word accumulator DF above.  Lanes merge (value and compensation) into the
 // column sums of compute_energy_x (wave_energy.c:292-302); the block merges the six
-// boxes of compute_energy_tblr (sub_wave_comp.c:1752-1800) over its columns.
-// cols[i] = (sum over j < ny/2, sum over j >= ny/2); part[6 b + k] = box k of block b
-// (0..2 top left/mid/right, 3..5 bottom).
+// boxes of compute_energy_tblr (sub_wave_comp.c:1752-1800) over its columns, and its
+// total.  cols[i] = (sum over j < ny/2, sum over j >= ny/2); part[6 b + k] = box k of
+// block b (0..2 top left/mid/right, 3..5 bottom); the block's total overwrites
+// cols[8 b].y (already folded into the boxes).
 #define ENERGY_COLS_PER_BLOCK 8
-#define ENERGY_RUN 16
 template <class T, int MASK>
 __global__ void __launch_bounds__(32 * ENERGY_COLS_PER_BLOCK)
     k_energy_cols(const __grid_constant__ DevParams p, const T *__restrict__ phi, const T *__restrict__ psi,
                   const int16_t *__restrict__ xy, const uint32_t *__restrict__ nz, int ileft, int iright,
                   double2 *__restrict__ cols, double *__restrict__ part)
 {
-    __shared__ double sh[ENERGY_COLS_PER_BLOCK][2];
+    using Acc = typename std::conditional<sizeof(T) == 8, Neu, DF>::type;
+    __shared__ Acc sh[ENERGY_COLS_PER_BLOCK][2];
+    __shared__ Acc sbx[6];
     __shared__ int sbox[ENERGY_COLS_PER_BLOCK];
     const int wid = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int i = blockIdx.x * ENERGY_COLS_PER_BLOCK + wid;
-    Neu nb, nt;  // bottom (j < ny/2) and top halves of the column
+    Acc ab = {0, 0}, at = {0, 0};  // bottom (j < ny/2) and top halves of the column
     if (i < p.nx) {
         const int NX = p.nx, NY = p.ny, jmid = NY / 2;
         const size_t row = (size_t)i * p.pitch;
         const int ip = (i + 1 == NX) ? NX - 1 : i + 1, im = (i == 0) ? 0 : i - 1;
         const T *re = phi + (size_t)ip * p.pitch, *rw = phi + (size_t)im * p.pitch, *rc = phi + row, *ry = psi + row;
         const float es2 = (float)p.e_scale2, hc2 = (float)p.ehalf_c2, hc2b = (float)p.ehalf_c2b;
-        float kb = 0.f, kbc = 0.f, kt = 0.f, ktc = 0.f;  // FP32 Kahan runs (FP32 fields)
         if (sizeof(T) == 4 && MASK == 1) {
             // FP32 fields: four cells per lane and step as 16-byte loads of the rows i-1, i, i+1
             // and psi; the j-1 / j+1 neighbours from the adjacent lanes (the row pitch is a
@@ -366,7 +393,7 @@ __global__ void __launch_bounds__(32 * ENERGY_COLS_PER_BLOCK)
             const float *fc = (const float *)rc, *fy = (const float *)ry, *fe = (const float *)re,
                         *fw = (const float *)rw;
             const uint32_t *nzr = nz + (size_t)i * p.wpitch;
-            for (int base = 0, step = 0; base < NY; base += 128, step++) {
+            for (int base = 0; base < NY; base += 128) {
                 const int j0 = base + 4 * lane;
                 const float4 c4 = *reinterpret_cast<const float4 *>(fc + j0);
                 const float4 y4 = *reinterpret_cast<const float4 *>(fy + j0);
@@ -388,18 +415,12 @@ __global__ void __launch_bounds__(32 * ENERGY_COLS_PER_BLOCK)
                     if (j == 0) js = xs[k];
                     const float en = cell_energy32(es2, hc2, hc2b, p.twospeeds, xs[k], ys[k], es[k], ws[k], jn, js,
                                                    (int)((bits >> k) & 1u));
-                    if (j < jmid) kahan_add(kb, kbc, en);
-                    else kahan_add(kt, ktc, en);
-                }
-                if ((step & (ENERGY_RUN - 1)) == ENERGY_RUN - 1) {
-                    flush_run(nb, kb, kbc);
-                    flush_run(nt, kt, ktc);
+                    acc_add(j < jmid ? ab : at, en);
                 }
             }
         } else {
-            int step = 0;
 #pragma unroll 4
-            for (int j = lane; j < NY; j += 32, step++) {
+            for (int j = lane; j < NY; j += 32) {
                 const int jp = (j + 1 == NY) ? NY - 1 : j + 1, jm = (j == 0) ? 0 : j - 1;
                 int m;
                 if (MASK == 0) m = xy[row + j] != 0;
@@ -407,84 +428,56 @@ __global__ void __launch_bounds__(32 * ENERGY_COLS_PER_BLOCK)
                 if (sizeof(T) == 8) {
                     const double en = cell_energy(p, (double)rc[j], (double)ry[j], (double)re[j], (double)rw[j],
                                                   (double)rc[jp], (double)rc[jm], m);
-                    if (j < jmid) nb.add(en); else nt.add(en);
+                    acc_add(j < jmid ? ab : at, en);
                 } else {
                     const float en = cell_energy32(es2, hc2, hc2b, p.twospeeds, (float)rc[j], (float)ry[j],
                                                    (float)re[j], (float)rw[j], (float)rc[jp], (float)rc[jm], m);
-                    if (j < jmid) kahan_add(kb, kbc, en);
-                    else kahan_add(kt, ktc, en);
-                    if ((step & (4 * ENERGY_RUN - 1)) == 4 * ENERGY_RUN - 1) {
-                        flush_run(nb, kb, kbc);
-                        flush_run(nt, kt, ktc);
-                    }
+                    acc_add(j < jmid ? ab : at, en);
                 }
             }
         }
-        if (sizeof(T) == 4) {
-            flush_run(nb, kb, kbc);
-            flush_run(nt, kt, ktc);
-        }
     }
-    warp_merge(nb);
-    warp_merge(nt);
+    warp_merge(ab);
+    warp_merge(at);
     if (lane == 0) {
-        const double vb = nb.value(), vt = nt.value();
-        if (i < p.nx) cols[i] = make_double2(vb, vt);
-        sh[wid][0] = vb;
-        sh[wid][1] = vt;
+        if (i < p.nx) cols[i] = make_double2(ab.value(), at.value());
+        sh[wid][0] = ab;
+        sh[wid][1] = at;
         sbox[wid] = (i < ileft) ? 0 : (i < iright ? 1 : 2);
     }
     __syncthreads();
     if (threadIdx.x < 6) {
         const int k = threadIdx.x, box = k % 3, half = k < 3 ? 1 : 0;  // top boxes sum j >= ny/2
-        Neu acc;
+        Acc acc = {0, 0};
 #pragma unroll
         for (int w = 0; w < ENERGY_COLS_PER_BLOCK; w++)
-            if (sbox[w] == box) acc.add(sh[w][half]);
+            if (sbox[w] == box) acc_merge(acc, sh[w][half]);
         part[(size_t)blockIdx.x * 6 + k] = acc.value();
-    }
-}
-
-// out[0] = total, out[1..6] = boxes (top left/mid/right, bottom left/mid/right),
-// out[7..7+nx) = column sums over j < ny/2.  One block of 256 threads; every merge is an
-// FP64 Neumaier merge (value and compensation).
-__global__ void __launch_bounds__(256) k_energy_final(int nx, int nblocks, const double2 *__restrict__ cols,
-                                                      const double *__restrict__ part, double *__restrict__ out)
-{
-    __shared__ double sh[6][8][2];
-    __shared__ double box[6];
-    for (int i = threadIdx.x; i < nx; i += blockDim.x) out[7 + i] = cols[i].x;
-    Neu acc[6];
-    for (int b = threadIdx.x; b < nblocks; b += blockDim.x)
-#pragma unroll
-        for (int k = 0; k < 6; k++) acc[k].add(part[(size_t)b * 6 + k]);
-    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-#pragma unroll
-    for (int k = 0; k < 6; k++) {
-        warp_merge(acc[k]);
-        if (lane == 0) {
-            sh[k][wid][0] = acc[k].s;
-            sh[k][wid][1] = acc[k].c;
-        }
-    }
-    __syncthreads();
-    if (threadIdx.x < 6) {
-        Neu a;
-        for (int w = 0; w < (int)(blockDim.x >> 5); w++) {
-            Neu o;
-            o.s = sh[threadIdx.x][w][0];
-            o.c = sh[threadIdx.x][w][1];
-            a.merge(o);
-        }
-        out[1 + threadIdx.x] = a.value();
-        box[threadIdx.x] = a.value();
+        sbx[k] = acc;
     }
     __syncthreads();
     if (threadIdx.x == 0) {
-        Neu t;
-        for (int k = 0; k < 6; k++) t.add(box[k]);
-        out[0] = t.value();
+        Acc t = {0, 0};
+#pragma unroll
+        for (int k = 0; k < 6; k++) acc_merge(t, sbx[k]);
+        cols[(size_t)blockIdx.x * ENERGY_COLS_PER_BLOCK].y = t.value();
     }
+}
+
+// One warp per output: block k < 6 merges box k over the blocks of k_energy_cols into
+// out[1 + k] (top left/mid/right, bottom left/mid/right); block 6 merges the blocks'
+// totals into out[0]; all of them copy the column sums over j < ny/2 into out[7..7+nx).
+// FP64 Neumaier per lane, then merged across the warp.
+__global__ void __launch_bounds__(32) k_energy_final(int nx, int nblocks, const double2 *__restrict__ cols,
+                                                     const double *__restrict__ part, double *__restrict__ out)
+{
+    const int k = blockIdx.x, lane = threadIdx.x;
+    for (int i = k * 32 + lane; i < nx; i += 7 * 32) out[7 + i] = cols[i].x;
+    Neu acc = {0.0, 0.0};
+    for (int b = lane; b < nblocks; b += 32)
+        acc.add(k < 6 ? part[(size_t)b * 6 + k] : cols[(size_t)b * ENERGY_COLS_PER_BLOCK].y);
+    warp_merge(acc);
+    if (lane == 0) out[k < 6 ? 1 + k : 0] = acc.value();
 }
 
 // ---------------------------------------------------------------------------
@@ -642,7 +635,7 @@ void launch_energy(const DevParams &p, const T *phi, const T *psi, const int16_t
     double *part = reinterpret_cast<double *>(top);
     if (xy) k_energy_cols<T, 0><<<nblocks, 32 * ENERGY_COLS_PER_BLOCK, 0, st>>>(p, phi, psi, xy, nz, ileft, iright, bot, part);
     else k_energy_cols<T, 1><<<nblocks, 32 * ENERGY_COLS_PER_BLOCK, 0, st>>>(p, phi, psi, xy, nz, ileft, iright, bot, part);
-    k_energy_final<<<1, 256, 0, st>>>(p.nx, nblocks, bot, part, out);
+    k_energy_final<<<7, 32, 0, st>>>(p.nx, nblocks, bot, part, out);
 }
 template void launch_energy<float>(const DevParams &, const float *, const float *, const int16_t *, const uint32_t *, double2 *, double2 *, int, int, double *, cudaStream_t);
 template void launch_energy<double>(const DevParams &, const double *, const double *, const int16_t *, const uint32_t *, double2 *, double2 *, int, int, double *, cudaStream_t);

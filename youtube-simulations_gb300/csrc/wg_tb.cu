@@ -324,9 +324,62 @@ __device__ __forceinline__ float skew_cell(const DevParams &p, const TbArgs &a, 
 // rule; the source cell gets its increment.  Cells outside the domain keep whatever
 // they got: no cell inside reads them and none is stored.
 // ---------------------------------------------------------------------------
-__device__ __forceinline__ float pick4(float a0, float a1, float a2, float a3, int c)
+// Element c (0..3) of a lane's four columns held as two pairs.
+__device__ __forceinline__ float get4(const float2 (&r)[2], int c)
 {
-    return c == 0 ? a0 : (c == 1 ? a1 : (c == 2 ? a2 : a3));
+    return c == 0 ? r[0].x : (c == 1 ? r[0].y : (c == 2 ? r[1].x : r[1].y));
+}
+__device__ __forceinline__ void set4(float2 (&r)[2], int c, float v)
+{
+    if (c == 0) r[0].x = v;
+    else if (c == 1) r[0].y = v;
+    else if (c == 2) r[1].x = v;
+    else r[1].y = v;
+}
+
+// The inner rule of skew_cell<COEF, false, PLAIN, INL, KZ> for the lane's four columns,
+// as two pairs of packed FP32 instructions (add/sub/mul/fma .f32x2): every element is
+// rounded exactly as the scalar instruction on that element, in the same order
+// (the Laplacian as differences from the centre, then upd32 / upd32_k0), so the fields
+// equal the scalar forms' bit for bit.  X, N, S: level s-1 at rows r, r+1, r-1; Y: level
+// s-2 at row r; e3 / w0: the neighbours right of column 3 and left of column 0; T: tcc
+// (table scenes); act4: the cells' active bits.
+template <int COEF, bool PLAIN, bool KZ>
+__device__ __forceinline__ void inner4(const DevParams &p, const TbArgs &a, const float2 (&X)[2], const float2 (&Y)[2],
+                                       const float2 (&N)[2], const float2 (&S)[2], float e3, float w0,
+                                       const float2 (&T)[2], uint32_t act4, float2 (&out)[2])
+{
+    const float2 E[2] = {make_float2(X[0].y, X[1].x), make_float2(X[1].y, e3)};
+    const float2 Wv[2] = {make_float2(w0, X[0].x), make_float2(X[0].y, X[1].x)};
+#pragma unroll
+    for (int h = 0; h < 2; h++) {
+        const bool a0 = (act4 >> (2 * h)) & 1u, a1 = (act4 >> (2 * h + 1)) & 1u;
+        float2 cc, ng;
+        if (COEF == WG_COEF_TABLE) {
+            cc = T[h];
+            ng = make_float2(-a.gam, -a.gam);
+        } else {
+            cc = make_float2(a0 ? a.c2 : a.c2b, a1 ? a.c2 : a.c2b);
+            ng = make_float2(-(a0 ? a.gam : a.gamb), -(a1 ? a.gam : a.gamb));
+        }
+        const float2 d = add2(add2(sub2(N[h], X[h]), sub2(S[h], X[h])), add2(sub2(E[h], X[h]), sub2(Wv[h], X[h])));
+        const float2 w = sub2(X[h], Y[h]);
+        float2 t = fma2(ng, w, w);
+        if (!KZ) t = fma2(make_float2(-a.kappa, -a.kappa), X[h], t);
+        float2 v = add2(X[h], fma2(cc, d, t));
+        if (!PLAIN) {
+            // cells that are neither active nor in a two-speed scene keep psi (the
+            // reference writes nothing there); FLOOR clamps the active ones
+            const bool u0 = p.twospeeds || a0, u1 = p.twospeeds || a1;
+            if (p.floor_clamp) {
+                if (a0) v.x = fminf(fmaxf(v.x, -a.vmax), a.vmax);
+                if (a1) v.y = fminf(fmaxf(v.y, -a.vmax), a.vmax);
+            }
+            v.x = u0 ? v.x : Y[h].x;
+            v.y = u1 ? v.y : Y[h].y;
+        }
+        out[h] = v;
+    }
 }
 
 // Column 0 (right = false) or ny-1 (right = true) at a row 1..nx-2: the boundary rule of
@@ -411,8 +464,10 @@ __device__ __forceinline__ void skew_strip(const DevParams &p, const TbArgs &a, 
     const int ce = !edge ? -1 : (gj0 == 0 ? 0 : (cr >= 0 && cr <= 3 ? cr : -1));
     const bool src_lane = edge && p.src_on && p.src_j >= gj0 && p.src_j < gj0 + 4;
 
-    float W[K + 1][3][4];  // W[s][k][c] = level s at row m-s-2+k, column gj0+c
-    float Yp[4];           // psi(t-1) at row m-1
+    // The lane's four columns as two pairs (gj0, gj0+1), (gj0+2, gj0+3): the inner rule
+    // runs on the pairs with packed FP32 instructions.
+    float2 W[K + 1][3][2];  // W[s][k] = level s at row m-s-2+k
+    float2 Yp[2];           // psi(t-1) at row m-1
     // tcc at rows m, m-1, ..., m-K (table scenes): the warp's shared ring tring of K+1 rows
     // (slot ts holds row m), each lane writing and reading back only its own 16 bytes
     int ts = 0;
@@ -421,11 +476,10 @@ __device__ __forceinline__ void skew_strip(const DevParams &p, const TbArgs &a, 
 #pragma unroll
     for (int q = 0; q <= K; q++) {
 #pragma unroll
-        for (int c = 0; c < 4; c++) { W[q][0][c] = W[q][1][c] = W[q][2][c] = 0.f; }
+        for (int k = 0; k < 3; k++) W[q][k][0] = W[q][k][1] = make_float2(0.f, 0.f);
         TE[q] = 0.f;
     }
-#pragma unroll
-    for (int c = 0; c < 4; c++) Yp[c] = 0.f;
+    Yp[0] = Yp[1] = make_float2(0.f, 0.f);
 
     // row m goes to slot (m - m0) % D; each lane copies, and later reads, only its own bytes
     auto issue = [&](int m, int slot) {
@@ -465,85 +519,76 @@ __device__ __forceinline__ void skew_strip(const DevParams &p, const TbArgs &a, 
                                                       : make_float4(0.f, 0.f, 0.f, 0.f);
             const uint32_t aw = NEED_ACT ? reinterpret_cast<const uint32_t *>(b)[SL::ACT + lane] : 0u;
             const float tein = need_tce ? b[SL::TCE + lane] : 0.f;
-            const float xin[4] = {xq.x, xq.y, xq.z, xq.w};
-            const float yin[4] = {yq.x, yq.y, yq.z, yq.w};
             if (COEF == WG_COEF_TABLE) *reinterpret_cast<float4 *>(tring + ts * 128 + 4 * lane) = cq;
             if (NEED_ACT) aq = (aq << 4) | ((aw >> (gj0 & 31)) & 0xFu);
             // the slot of row m-1 (read in the previous row) takes row m+QD
             issue(m + QD, slot == 0 ? D - 1 : slot - 1);
             slot = (slot == D - 1) ? 0 : slot + 1;
-            float ylev1[4];
+            float2 ylev1[2];
 #pragma unroll
-            for (int c = 0; c < 4; c++) {
-                W[0][0][c] = W[0][1][c];
-                W[0][1][c] = W[0][2][c];
-                W[0][2][c] = xin[c];
-                ylev1[c] = Yp[c];
-                Yp[c] = yin[c];
+            for (int h = 0; h < 2; h++) {
+                W[0][0][h] = W[0][1][h];
+                W[0][1][h] = W[0][2][h];
+                ylev1[h] = Yp[h];
             }
+            W[0][2][0] = make_float2(xq.x, xq.y);
+            W[0][2][1] = make_float2(xq.z, xq.w);
+            Yp[0] = make_float2(yq.x, yq.y);
+            Yp[1] = make_float2(yq.z, yq.w);
 #pragma unroll
             for (int q = K; q > 0; q--) TE[q] = TE[q - 1];
             TE[0] = tein;
 #pragma unroll
             for (int lv = 1; lv <= K; lv++) {
                 const int r = m - lv;  // row of this level's new value
-                float v[4] = {0.f, 0.f, 0.f, 0.f};
+                float2 v[2] = {make_float2(0.f, 0.f), make_float2(0.f, 0.f)};
                 // Level lv at row r reaches the stored rows only from r >= i_s - K + lv on, i.e.
                 // from input row m0 + 2 lv + 1: in the pipeline fill the earlier levels are skipped
                 // (warp-uniform), and their window slots hold zeros that nothing reads.
                 if (m - m0 >= 2 * lv + 1) {
-                const float *Wc = W[lv - 1][1];
-                const float *Yl = (lv == 1) ? ylev1 : W[lv - 2 >= 0 ? lv - 2 : 0][0];
-                float Tl[4] = {0.f, 0.f, 0.f, 0.f};  // tcc at row r
+                const float2 (&Wc)[2] = W[lv - 1][1];
+                const float2 (&Wn)[2] = W[lv - 1][2];
+                const float2 (&Ws)[2] = W[lv - 1][0];
+                const float2 (&Yl)[2] = (lv == 1) ? ylev1 : W[lv - 2 >= 0 ? lv - 2 : 0][0];
+                float2 Tl[2] = {make_float2(0.f, 0.f), make_float2(0.f, 0.f)};  // tcc at row r
                 if (COEF == WG_COEF_TABLE) {
                     const int tsl = ts >= lv ? ts - lv : ts - lv + K + 1;
                     const float4 tq = *reinterpret_cast<const float4 *>(tring + tsl * 128 + 4 * lane);
-                    Tl[0] = tq.x;
-                    Tl[1] = tq.y;
-                    Tl[2] = tq.z;
-                    Tl[3] = tq.w;
+                    Tl[0] = make_float2(tq.x, tq.y);
+                    Tl[1] = make_float2(tq.z, tq.w);
                 }
-                const float e3 = __shfl_down_sync(0xffffffffu, Wc[0], 1);
-                const float w0 = __shfl_up_sync(0xffffffffu, Wc[3], 1);
-#pragma unroll
-                for (int c = 0; c < 4; c++) {
-                    const float e = (c < 3) ? Wc[c + 1 < 4 ? c + 1 : 3] : e3;
-                    const float w = (c > 0) ? Wc[c > 0 ? c - 1 : 0] : w0;
-                    const bool act = NEED_ACT ? ((aq >> (4 * lv + c)) & 1u) : true;
-                    v[c] = skew_cell<COEF, false, PLAIN, INL, KZ>(p, a, r, gj0 + c, lv, Wc[c], Yl[c], W[lv - 1][2][c],
-                                                         W[lv - 1][0][c], e, w, Tl[c], 0.f, act);
-                }
+                const float e3 = __shfl_down_sync(0xffffffffu, Wc[0].x, 1);
+                const float w0 = __shfl_up_sync(0xffffffffu, Wc[1].y, 1);
+                const uint32_t act4 = NEED_ACT ? ((aq >> (4 * lv)) & 0xFu) : 0xFu;
+                inner4<COEF, PLAIN, KZ>(p, a, Wc, Yl, Wn, Ws, e3, w0, Tl, act4, v);
                 if (!GEN && edge) {  // warp-uniform
                     if (ce >= 0 && r > 0 && r < p.nx - 1) {  // the lane holding column 0 (c = 0) or ny-1 (c = 3)
                         const bool lf = ce == 0;
                         const float res = col_edge_cell<COEF>(
-                            p, a, r, lf ? Wc[0] : Wc[3], lf ? Yl[0] : Yl[3], lf ? W[lv - 1][2][0] : W[lv - 1][2][3],
-                            lf ? W[lv - 1][0][0] : W[lv - 1][0][3], lf ? Wc[1] : e3, lf ? w0 : Wc[2],
-                            lf ? Tl[0] : Tl[3], TE[lv], NEED_ACT ? ((aq >> (4 * lv + ce)) & 1u) : true, !lf);
-                        v[0] = lf ? res : v[0];
-                        v[3] = lf ? v[3] : res;
+                            p, a, r, lf ? Wc[0].x : Wc[1].y, lf ? Yl[0].x : Yl[1].y, lf ? Wn[0].x : Wn[1].y,
+                            lf ? Ws[0].x : Ws[1].y, lf ? Wc[0].y : e3, lf ? w0 : Wc[1].x,
+                            lf ? Tl[0].x : Tl[1].y, TE[lv], NEED_ACT ? ((act4 >> ce) & 1u) : true, !lf);
+                        v[0].x = lf ? res : v[0].x;
+                        v[1].y = lf ? v[1].y : res;
                     }
                     if (src_lane && r == p.src_i) {
                         const double add = INL ? src_inl(p, a.t0 + lv) : a.src[lv - 1];
                         const int cs = p.src_j - gj0;
 #pragma unroll
-                        for (int c = 0; c < 4; c++) v[c] = (cs == c) ? (float)A_((double)v[c], add) : v[c];
+                        for (int c = 0; c < 4; c++)
+                            if (cs == c) set4(v, c, (float)A_((double)get4(v, c), add));
                     }
                 }
                 if (GEN) {
                     const bool row_edge = r == 0 || r == p.nx - 1;  // warp-uniform
                     if (ce >= 0 && r > 0 && r < p.nx - 1) {  // the lane holding column 0 or ny-1: picked by index
                         const float res = col_edge_cell<COEF>(
-                            p, a, r, pick4(Wc[0], Wc[1], Wc[2], Wc[3], ce), pick4(Yl[0], Yl[1], Yl[2], Yl[3], ce),
-                            pick4(W[lv - 1][2][0], W[lv - 1][2][1], W[lv - 1][2][2], W[lv - 1][2][3], ce),
-                            pick4(W[lv - 1][0][0], W[lv - 1][0][1], W[lv - 1][0][2], W[lv - 1][0][3], ce),
-                            pick4(Wc[1], Wc[2], Wc[3], e3, ce), pick4(w0, Wc[0], Wc[1], Wc[2], ce),
-                            pick4(Tl[0], Tl[1], Tl[2], Tl[3], ce), TE[lv],
-                            NEED_ACT ? ((aq >> (4 * lv + ce)) & 1u) : true, gj0 != 0);
-                        v[0] = (ce == 0) ? res : v[0];
-                        v[1] = (ce == 1) ? res : v[1];
-                        v[2] = (ce == 2) ? res : v[2];
-                        v[3] = (ce == 3) ? res : v[3];
+                            p, a, r, get4(Wc, ce), get4(Yl, ce), get4(Wn, ce), get4(Ws, ce),
+                            ce < 3 ? get4(Wc, ce + 1) : e3, ce > 0 ? get4(Wc, ce - 1) : w0, get4(Tl, ce), TE[lv],
+                            NEED_ACT ? ((act4 >> ce) & 1u) : true, gj0 != 0);
+#pragma unroll
+                        for (int c = 0; c < 4; c++)
+                            if (ce == c) set4(v, c, res);
                     }
                     if (row_edge) {  // rows 0 and nx-1 by the general rule, one cell at a time
 #pragma unroll 1
@@ -552,30 +597,25 @@ __device__ __forceinline__ void skew_strip(const DevParams &p, const TbArgs &a, 
                             if (gj < 0 || gj >= p.ny) continue;
                             const float tcv = (COEF == WG_COEF_TABLE && a.tc) ? a.tc[(size_t)r * p.pitch + gj] : 0.f;
                             const float res = skew_cell<COEF, true, false, INL>(
-                                p, a, r, gj, lv, pick4(Wc[0], Wc[1], Wc[2], Wc[3], c), pick4(Yl[0], Yl[1], Yl[2], Yl[3], c),
-                                pick4(W[lv - 1][2][0], W[lv - 1][2][1], W[lv - 1][2][2], W[lv - 1][2][3], c),
-                                pick4(W[lv - 1][0][0], W[lv - 1][0][1], W[lv - 1][0][2], W[lv - 1][0][3], c),
-                                pick4(Wc[1], Wc[2], Wc[3], e3, c), pick4(w0, Wc[0], Wc[1], Wc[2], c),
-                                pick4(Tl[0], Tl[1], Tl[2], Tl[3], c), tcv,
-                                NEED_ACT ? ((aq >> (4 * lv + c)) & 1u) : true);
-                            v[0] = (c == 0) ? res : v[0];
-                            v[1] = (c == 1) ? res : v[1];
-                            v[2] = (c == 2) ? res : v[2];
-                            v[3] = (c == 3) ? res : v[3];
+                                p, a, r, gj, lv, get4(Wc, c), get4(Yl, c), get4(Wn, c), get4(Ws, c),
+                                c < 3 ? get4(Wc, c + 1) : e3, c > 0 ? get4(Wc, c - 1) : w0, get4(Tl, c), tcv,
+                                NEED_ACT ? ((act4 >> c) & 1u) : true);
+                            set4(v, c, res);
                         }
                     } else if (src_lane && r == p.src_i) {  // the general rule adds it on rows 0 and nx-1
                         const double add = INL ? src_inl(p, a.t0 + lv) : a.src[lv - 1];
                         const int cs = p.src_j - gj0;
 #pragma unroll
-                        for (int c = 0; c < 4; c++) v[c] = (cs == c) ? (float)A_((double)v[c], add) : v[c];
+                        for (int c = 0; c < 4; c++)
+                            if (cs == c) set4(v, c, (float)A_((double)get4(v, c), add));
                     }
                 }
                 }  // levels in use
 #pragma unroll
-                for (int c = 0; c < 4; c++) {
-                    W[lv][0][c] = W[lv][1][c];
-                    W[lv][1][c] = W[lv][2][c];
-                    W[lv][2][c] = v[c];
+                for (int h = 0; h < 2; h++) {
+                    W[lv][0][h] = W[lv][1][h];
+                    W[lv][1][h] = W[lv][2][h];
+                    W[lv][2][h] = v[h];
                 }
             }
             ts = (ts == K) ? 0 : ts + 1;  // row m+1's tcc slot
@@ -584,16 +624,17 @@ __device__ __forceinline__ void skew_strip(const DevParams &p, const TbArgs &a, 
                 const size_t o = (size_t)r * p.pitch + gj0;
                 if (gj0 + 3 < p.ny) {
                     if (grp_ok) {
-                        *reinterpret_cast<float4 *>(a.phi_out + o) = make_float4(W[K][2][0], W[K][2][1], W[K][2][2], W[K][2][3]);
+                        *reinterpret_cast<float4 *>(a.phi_out + o) =
+                            make_float4(W[K][2][0].x, W[K][2][0].y, W[K][2][1].x, W[K][2][1].y);
                         *reinterpret_cast<float4 *>(a.psi_out + o) =
-                            make_float4(W[K - 1][1][0], W[K - 1][1][1], W[K - 1][1][2], W[K - 1][1][3]);
+                            make_float4(W[K - 1][1][0].x, W[K - 1][1][0].y, W[K - 1][1][1].x, W[K - 1][1][1].y);
                     }
                 } else if (grp_ok) {
 #pragma unroll
                     for (int c = 0; c < 4; c++)
                         if (gj0 + c < p.ny) {
-                            a.phi_out[o + c] = W[K][2][c];
-                            a.psi_out[o + c] = W[K - 1][1][c];
+                            a.phi_out[o + c] = get4(W[K][2], c);
+                            a.psi_out[o + c] = get4(W[K - 1][1], c);
                         }
                 }
             }
