@@ -372,7 +372,8 @@ typedef struct wg_server_config {
     int32_t precision;        /* WG_FP32 or WG_FP64 */
     int32_t steps_per_frame;  /* leapfrog updates per returned frame */
     int32_t max_scenes;       /* resident scenes at most */
-    int32_t reserved;
+    int32_t pipeline;         /* 0: a tick returns with its frames in host memory;
+                                 1: pipelined ticks (see wg_server_tick) */
     uint64_t hbm_budget;      /* device bytes the resident scenes may hold */
     wg_frame_params frame;    /* colour map of the returned frames */
     uint8_t lut[768];         /* 256x3 palette bytes (the reference's turbo_srgb_bytes) */
@@ -380,12 +381,18 @@ typedef struct wg_server_config {
 typedef struct wg_server_stats {
     int64_t submitted, admitted, completed, queued, resident, frames, ticks;
     double cell_updates;                  /* cell updates performed */
-    double busy_seconds;                  /* wall time inside wg_server_tick */
+    double busy_seconds;                  /* wall time inside wg_server_tick / wg_server_drain */
+    /* per frame: from the host's enqueue of the tick that renders it to the host seeing
+     * the frame in host memory (with pipelined ticks this includes waiting behind the
+     * previous tick's device work) */
     double frame_latency_p50_ms, frame_latency_p99_ms, frame_latency_max_ms;
     double first_frame_p50_ms, first_frame_p99_ms;  /* submit -> first frame on the host */
     uint64_t bytes_resident, bytes_peak;
+    /* per tick: device time from the tick's first kernel to its frames in host memory */
+    double tick_device_p50_ms, tick_device_p99_ms;
+    int64_t cancelled;
 } wg_server_stats;
-enum { WG_REQ_QUEUED = 0, WG_REQ_RESIDENT = 1, WG_REQ_DONE = 2 };
+enum { WG_REQ_QUEUED = 0, WG_REQ_RESIDENT = 1, WG_REQ_DONE = 2, WG_REQ_CANCELLED = 3 };
 
 wg_status wg_server_create(const wg_server_config *cfg, void *stream, wg_server **out);
 wg_status wg_server_destroy(wg_server *s);
@@ -393,12 +400,25 @@ wg_status wg_server_destroy(wg_server *s);
  * later tick, first come first served, as soon as its device bytes fit the budget. */
 wg_status wg_server_submit(wg_server *s, const wg_params *p, const double *phi, const double *psi,
                            const int16_t *xy, int32_t frames, int32_t keep_result, int64_t *request_id);
-/* One tick: admit what fits, advance every resident scene by one frame (one CUDA-graph
- * launch for all of them), render and copy every scene's frame to host memory, retire
- * finished requests.  *frames_out = frames produced. */
+/* One tick: retire requests whose frames are all rendered and cancelled ones, admit
+ * what fits, advance every resident scene by one frame (one CUDA-graph launch for all of
+ * them), render every scene's frame and copy them to host memory.
+ * pipeline = 0: the tick waits for its own frames; *frames_out = frames produced.
+ * pipeline = 1: the tick enqueues its work on the device, then waits only for the
+ * previous tick's frames (two frame buffers alternate), so the device works on tick t
+ * while the host handles tick t-1; *frames_out = frames of the previous tick that are
+ * now in host memory.  wg_server_drain completes the last enqueued tick. */
 wg_status wg_server_tick(wg_server *s, int32_t *frames_out);
-/* The latest frame of a request.  Valid until the next tick that renders frames; after
- * it the call returns WG_ERR_STATE (the host buffer holds that tick's frames). */
+/* Pipelined servers: waits for the enqueued tick and makes its frames readable
+ * (*frames_out = their number; 0 when no tick was pending).  No-op otherwise. */
+wg_status wg_server_drain(wg_server *s, int32_t *frames_out);
+/* Cancels a request: a queued one leaves the queue now; a resident one leaves the batch
+ * (and returns its bytes to the budget) at the next tick, before that tick's frame.
+ * Its state becomes WG_REQ_CANCELLED.  A finished request gives WG_ERR_STATE. */
+wg_status wg_server_cancel(wg_server *s, int64_t request_id);
+/* The latest frame of a request in host memory.  Valid until the next call that makes
+ * newer frames readable (the next tick, or drain); after it the call returns
+ * WG_ERR_STATE. */
 wg_status wg_server_frame(wg_server *s, int64_t request_id, uint8_t *rgb, int32_t *frame_index,
                           int32_t *width, int32_t *height);
 /* Final phi/psi of a finished request submitted with keep_result. */

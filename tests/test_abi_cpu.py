@@ -35,5 +35,5 @@ def test_library_exports_every_declared_symbol():
 def test_status_strings_without_gpu():
     from youtube_simulations_gb300 import wavegpu as W
     L = W.lib()
-    assert L.wg_abi_version() == 2
+    assert L.wg_abi_version() == 3
     assert L.wg_status_string(-4) == b"HBM budget exceeded"

@@ -103,3 +103,79 @@ def test_budget_refusal_and_queueing():
         z = np.zeros(2000 * 2000)
         with pytest.raises(W.WaveGpuError):
             srv.submit(p, z, z, np.zeros(2000 * 2000, np.int16), 1)
+
+
+def test_pipelined_ticks_give_the_same_frames_and_results():
+    """pipeline=1: tick t enqueues its device work and then completes tick t-1, whose
+    frames are then readable; drain() completes the last tick.  Every frame and every
+    final state equal those of the synchronous server and of the scene run alone."""
+    reqs = requests(6, 4)
+    steps = 3
+    with W.Server(LUT, precision=P.FP32, steps_per_frame=steps, pipeline=True) as srv:
+        ids = [srv.submit(p, f["phi"], f["psi"], xy, frames, keep=True) for (p, f, xy, frames) in reqs]
+        seen = {rid: [] for rid in ids}
+        ticks = 0
+        while any(srv.state(r)[0] != P.REQ_DONE for r in ids):
+            got = srv.tick() if ticks < 40 else srv.drain()
+            ticks += 1
+            assert ticks < 60
+            for rid in ids:
+                try:
+                    idx, img = srv.frame(rid)
+                except W.WaveGpuError:
+                    continue
+                if not seen[rid] or seen[rid][-1][0] != idx:
+                    seen[rid].append((idx, img))
+            if got == 0 and srv.stats()["resident"] == 0 and srv.stats()["queued"] == 0:
+                srv.drain()
+        st = srv.stats()
+        assert st["completed"] == len(reqs) and st["tick_device_p50_ms"] > 0
+        for rid, (p, f, xy, frames) in zip(ids, reqs):
+            assert [i for i, _ in seen[rid]] == list(range(frames)), rid
+            for idx, img in seen[rid]:
+                _, _, ref = solo(p, f, xy, P.FP32, (idx + 1) * steps, want_frame=True)
+                assert np.array_equal(img, ref), (rid, idx)
+            phi, psi = srv.result(rid)
+            phi1, psi1, _ = solo(p, f, xy, P.FP32, frames * steps)
+            assert np.array_equal(phi, phi1) and np.array_equal(psi, psi1), rid
+
+
+@pytest.mark.parametrize("pipeline", [False, True])
+def test_cancellation(pipeline):
+    """A queued request cancelled leaves the queue at once; a resident one leaves the
+    batch at the next tick and returns its bytes to the budget; a finished one cannot be
+    cancelled.  The other requests' results are unaffected."""
+    reqs = requests(8, 4)
+    with W.Server(LUT, precision=P.FP32, steps_per_frame=2) as probe:
+        order = sorted(range(len(reqs)), key=lambda k: -probe.request_bytes(reqs[k][0]))
+        reqs = [reqs[k] for k in order]  # the two largest first
+        sizes = [probe.request_bytes(p) for (p, _, _, _) in reqs]
+    budget = sizes[0] + sizes[1]  # the first two fit together, a third does not
+    with W.Server(LUT, precision=P.FP32, steps_per_frame=2, hbm_budget=budget, pipeline=pipeline) as srv:
+        ids = [srv.submit(p, f["phi"], f["psi"], xy, 6, keep=True) for (p, f, xy, _) in reqs]
+        srv.tick()
+        assert srv.state(ids[0])[0] == P.REQ_RESIDENT and srv.state(ids[3])[0] == P.REQ_QUEUED
+        srv.cancel(ids[3])                       # queued
+        assert srv.state(ids[3])[0] == P.REQ_CANCELLED
+        srv.tick()
+        srv.cancel(ids[1])                       # resident
+        with pytest.raises(W.WaveGpuError):
+            srv.cancel(ids[1])                   # already cancelled
+        srv.tick()
+        assert srv.state(ids[1])[0] == P.REQ_CANCELLED
+        ticks = 0
+        while srv.state(ids[0])[0] != P.REQ_DONE or srv.state(ids[2])[0] != P.REQ_DONE:
+            srv.tick()
+            ticks += 1
+            assert ticks < 40
+        srv.drain()
+        with pytest.raises(W.WaveGpuError):
+            srv.cancel(ids[0])                   # finished
+        st = srv.stats()
+        assert st["cancelled"] == 2 and st["completed"] == 2 and st["resident"] == 0
+        assert st["bytes_resident"] == 0
+        for k in (0, 2):
+            p, f, xy, _ = reqs[k]
+            phi, psi = srv.result(ids[k])
+            phi1, psi1, _ = solo(p, f, xy, P.FP32, 12)
+            assert np.array_equal(phi, phi1) and np.array_equal(psi, psi1), k

@@ -324,7 +324,7 @@ using namespace wg;
 
 extern "C" {
 
-int32_t wg_abi_version(void) { return 2; }
+int32_t wg_abi_version(void) { return 3; }
 
 const char *wg_last_error(void) { return g_err.c_str(); }
 

@@ -22,6 +22,7 @@
 #include <cmath>
 #include <cstring>
 #include <map>
+#include <mutex>
 #include <vector>
 #include "wg_internal.h"
 #include "wg_scene.h"
@@ -524,11 +525,41 @@ static void batch_enqueue_frame(wg_batch *b, int n, bool skewed)
 // the other pair, so the state does not change), best of three after one untimed pass;
 // the fastest per update is kept.  Nine candidates per class keep the tuning frame of a
 // server tick short.
+// Tuned classes are kept for the process (per device): a later batch or server whose
+// scenes fall in a class tuned before takes that depth and chunk without timing them
+// again, so a serving tick pays the tuning of a size class at most once per process.
+struct TuneCacheEntry {
+    int k = 0, rows = 0;
+    double ms[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+};
+static std::mutex g_tune_mu;
+static std::map<std::pair<int, int>, TuneCacheEntry> g_tune_cache;  // (device, class)
+
 static wg_status batch_autotune(wg_batch *b)
 {
     bool tuned = false, ghosts = false;
+    int devno = 0;
+    WG_CUDA(cudaGetDevice(&devno));
     for (int c = 0; c < BATCH_CLASSES; c++) {
         if (b->class_k[c]) continue;
+        {
+            std::lock_guard<std::mutex> lk(g_tune_mu);
+            auto it = g_tune_cache.find(std::make_pair(devno, c));
+            if (it != g_tune_cache.end()) {
+                bool present = false;
+                for (size_t e = 0; e < b->tab_slot.size() && !present; e++) {
+                    const BatchSlotHost &h = b->slots[b->tab_slot[e]];
+                    present = h.skew && h.cls == c;
+                }
+                if (!present) continue;
+                if (b->tune_ms.empty()) b->tune_ms.assign(BATCH_CLASSES * 8, 0.0);
+                b->class_k[c] = it->second.k;
+                b->class_rows[c] = it->second.rows;
+                for (int K = 0; K < 8; K++) b->tune_ms[c * 8 + K] = it->second.ms[K];
+                tuned = true;
+                continue;
+            }
+        }
         std::vector<const BatchSlotHost *> hs;
         std::vector<int> entries;
         for (size_t e = 0; e < b->tab_slot.size(); e++) {
@@ -592,6 +623,13 @@ static wg_status batch_autotune(wg_batch *b)
         if (err != cudaSuccess) return cuda_fail(err, "batch autotune");
         b->class_k[c] = best;
         b->class_rows[c] = best_rows;
+        {
+            std::lock_guard<std::mutex> lk(g_tune_mu);
+            TuneCacheEntry &ce = g_tune_cache[std::make_pair(devno, c)];
+            ce.k = best;
+            ce.rows = best_rows;
+            for (int K = 0; K < 8; K++) ce.ms[K] = b->tune_ms[c * 8 + K];
+        }
         tuned = true;
     }
     if (tuned) return batch_refresh_table(b);

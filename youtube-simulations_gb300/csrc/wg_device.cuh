@@ -74,8 +74,7 @@ __device__ __forceinline__ double absorb64(double x, double y, double tc, double
 // FP32 update in increment form: out = x + ((1-g)(x-y) - kappa*x + cc*delta) with the
 // Laplacian as differences from the centre.  Same mathematics as upd64.  Every rounding
 // is spelled out as an explicit operation or fused multiply-add (nothing is left for the
-// compiler to contract), so the packed-pair form of the skewed kernels rounds each
-// element exactly the same way.
+// compiler to contract), so every kernel that applies it rounds each cell the same way.
 __device__ __forceinline__ float upd32(float x, float y, float cc, float delta, float kappa, float g)
 {
     const float w = __fsub_rn(x, y);
@@ -90,36 +89,11 @@ __device__ __forceinline__ float upd32_k0(float x, float y, float cc, float delt
     return __fadd_rn(x, fmaf(cc, delta, fmaf(-g, w, w)));
 }
 
-// Packed FP32 pairs: one sm_100-family instruction (add/sub/fma .f32x2) works on
-// both elements of a float2, each rounded to nearest exactly as the scalar instruction.
-// Written as PTX with the explicit .rn modifier, which the code generator never fuses
-// with a neighbouring instruction (a product followed by a subtraction stays two
-// roundings, as in upd32).
-#define WG_F32X2_BINOP(name, op)                                                                      \
-    __device__ __forceinline__ float2 name(float2 a, float2 b)                                          \
-    {                                                                                                   \
-        float2 r;                                                                                       \
-        asm("{\n\t.reg .b64 ra, rb, rd;\n\tmov.b64 ra, {%2, %3};\n\tmov.b64 rb, {%4, %5};\n\t" op      \
-            " rd, ra, rb;\n\tmov.b64 {%0, %1}, rd;\n\t}"                                               \
-            : "=f"(r.x), "=f"(r.y)                                                                      \
-            : "f"(a.x), "f"(a.y), "f"(b.x), "f"(b.y));                                                  \
-        return r;                                                                                       \
-    }
-WG_F32X2_BINOP(add2, "add.rn.f32x2")
-WG_F32X2_BINOP(sub2, "sub.rn.f32x2")
-#undef WG_F32X2_BINOP
-__device__ __forceinline__ float2 fma2(float2 a, float2 b, float2 c)
-{
-    float2 r;
-    asm("{\n\t.reg .b64 ra, rb, rc, rd;\n\tmov.b64 ra, {%2, %3};\n\tmov.b64 rb, {%4, %5};\n\t"
-        "mov.b64 rc, {%6, %7};\n\tfma.rn.f32x2 rd, ra, rb, rc;\n\tmov.b64 {%0, %1}, rd;\n\t}"
-        : "=f"(r.x), "=f"(r.y)
-        : "f"(a.x), "f"(a.y), "f"(b.x), "f"(b.y), "f"(c.x), "f"(c.y));
-    return r;
-}
+// x - (tc*(x-nb) + k*x + g*(x-y)) with its roundings spelled out (as upd32).
 __device__ __forceinline__ float absorb32(float x, float y, float tc, float nb, float k, float g)
 {
-    return x - (tc * (x - nb) + k * x + g * (x - y));
+    const float t = fmaf(k, x, __fmul_rn(tc, __fsub_rn(x, nb)));
+    return __fsub_rn(x, fmaf(g, __fsub_rn(x, y), t));
 }
 
 // oscillating_bc (sub_wave.c:11965-12162) with the reference's constants.

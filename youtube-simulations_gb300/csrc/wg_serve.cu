@@ -2,7 +2,11 @@
 // running batch (continuous batching), one frame of steps_per_frame updates per tick
 // for every resident scene (the batch's CUDA graph), their RGB8 frames rendered in one
 // launch into a packed buffer and copied to pinned host memory, per-frame latency and
-// time to first frame recorded, finished scenes retired and their memory returned.
+// time to first frame recorded, finished and cancelled scenes retired and their memory
+// returned.  Two frame buffers (device and pinned host) alternate between ticks, each
+// with its own frame table and events: a pipelined server enqueues tick t and only then
+// waits for tick t-1, so the device never idles while the host does a tick's
+// bookkeeping, and the copy of tick t-1's frames overlaps tick t's updates.
 #include <algorithm>
 #include <chrono>
 #include <cstring>
@@ -84,18 +88,37 @@ static double percentile(std::vector<double> v, double q)
 
 using namespace wg;
 
+// Where a request's latest frame lies in host memory.
+struct FrameLoc {
+    int64_t tick = -1;
+    int buf = 0;
+    unsigned long long off = 0;
+    int index = -1;
+};
+
 struct ServeReq {
     int64_t id = 0;
     wg_params p;
     std::vector<double> phi, psi;
     std::vector<int16_t> xy;
-    int frames = 0, keep = 0, state = WG_REQ_QUEUED, slot = -1, frames_done = 0, last_index = -1;
-    int64_t frame_tick = -1;  // the tick that rendered last_index into the host buffer
+    int frames = 0, keep = 0, state = WG_REQ_QUEUED, slot = -1;
+    int frames_enqueued = 0, frames_done = 0;
+    bool cancel = false;                       // resident: leave the batch at the next tick
+    unsigned long long off[2] = {0, 0};        // its frame's offset in each frame buffer
+    FrameLoc last;                             // its latest frame in host memory
     double t_submit = 0.0, t_first = -1.0;
     uint64_t bytes = 0;
     int w = 0, h = 0;
-    unsigned long long frame_off = 0;
     std::vector<double> res_phi, res_psi;
+};
+
+// One enqueued tick: its frame buffer, when the host enqueued it, who takes part.
+struct TickRec {
+    bool pending = false;
+    int64_t tick = -1;
+    double t_enqueue = 0.0;
+    long long cells = 0;
+    std::vector<int64_t> ids;
 };
 
 struct wg_server {
@@ -108,13 +131,18 @@ struct wg_server {
     std::vector<int64_t> resident;
     int64_t next_id = 1;
     uint64_t used = 0, peak = 0;
-    uint8_t *d_lut = nullptr, *d_frames = nullptr, *h_frames = nullptr;
-    size_t frames_cap = 0, frames_bytes = 0;
-    FrameDev *d_ftab = nullptr;
-    int ftab_cap = 0, total_rows = 0;
-    bool layout_dirty = false;  // retirements since the last layout
-    std::vector<double> lat_ms, first_ms;
-    int64_t submitted = 0, admitted = 0, completed = 0, frames = 0, ticks = 0;
+    uint8_t *d_lut = nullptr;
+    // per frame buffer q: device and pinned host frames, frame table, layout state, events
+    uint8_t *d_frames[2] = {nullptr, nullptr}, *h_frames[2] = {nullptr, nullptr};
+    size_t frames_cap[2] = {0, 0}, frames_bytes[2] = {0, 0};
+    FrameDev *d_ftab[2] = {nullptr, nullptr};
+    int ftab_cap[2] = {0, 0}, total_rows[2] = {0, 0}, ntab[2] = {0, 0};
+    bool layout_dirty[2] = {true, true};  // membership changed since buffer q's layout
+    cudaEvent_t ev_start[2] = {nullptr, nullptr}, ev_done[2] = {nullptr, nullptr};
+    TickRec rec[2];
+    int64_t readable_tick = -1;           // the tick whose frames wg_server_frame returns
+    std::vector<double> lat_ms, first_ms, dev_ms;
+    int64_t submitted = 0, admitted = 0, completed = 0, cancelled = 0, frames = 0, ticks = 0;
     double cell_updates = 0.0, busy = 0.0;
 };
 
@@ -127,8 +155,9 @@ static uint64_t request_bytes(const wg_server *s, const wg_params &p)
     return fields + masks + frame + (size_t)p.nx * 40 + 4096;
 }
 
-// rebuild the frame table and the packed frame buffer after admissions/retirements
-static wg_status server_layout(wg_server *s)
+// Frame table and packed frame buffer q for the current resident scenes.  Buffer q was
+// last used by a tick that has completed, and its frames are no longer readable.
+static wg_status server_layout(wg_server *s, int q)
 {
     std::vector<FrameDev> tab;
     int rows = 0;
@@ -139,37 +168,124 @@ static wg_status server_layout(wg_server *s)
         FrameDev d;
         memset(&d, 0, sizeof d);
         d.p = h.dp;
-        for (int q = 0; q < 4; q++) d.f[q] = h.f[q];
+        for (int k = 0; k < 4; k++) d.f[k] = h.f[k];
         d.nz = h.nz;
         d.slot = r.slot;
         d.w = r.w;
         d.h = r.h;
         d.row_base = rows;
         d.out_off = off;
-        r.frame_off = off;
+        r.off[q] = off;
         rows += r.h;
         off += (unsigned long long)r.w * r.h * 3;
         tab.push_back(d);
     }
-    if ((int)tab.size() > s->ftab_cap) {
-        if (s->d_ftab) cudaFree(s->d_ftab);
-        s->d_ftab = nullptr;
+    if ((int)tab.size() > s->ftab_cap[q]) {
+        if (s->d_ftab[q]) cudaFree(s->d_ftab[q]);
+        s->d_ftab[q] = nullptr;
         const int cap = std::max(64, (int)tab.size() * 2);
-        WG_CUDA(cudaMalloc(&s->d_ftab, sizeof(FrameDev) * cap));
-        s->ftab_cap = cap;
+        WG_CUDA(cudaMalloc(&s->d_ftab[q], sizeof(FrameDev) * cap));
+        s->ftab_cap[q] = cap;
     }
-    if (!tab.empty()) WG_CUDA(cudaMemcpyAsync(s->d_ftab, tab.data(), sizeof(FrameDev) * tab.size(), cudaMemcpyHostToDevice, s->st));
-    if (off > s->frames_cap) {
-        if (s->d_frames) cudaFree(s->d_frames);
-        if (s->h_frames) cudaFreeHost(s->h_frames);
-        s->d_frames = s->h_frames = nullptr;
+    if (!tab.empty())
+        WG_CUDA(cudaMemcpyAsync(s->d_ftab[q], tab.data(), sizeof(FrameDev) * tab.size(), cudaMemcpyHostToDevice, s->st));
+    if (off > s->frames_cap[q]) {
+        if (s->d_frames[q]) cudaFree(s->d_frames[q]);
+        if (s->h_frames[q]) cudaFreeHost(s->h_frames[q]);
+        s->d_frames[q] = s->h_frames[q] = nullptr;
         const size_t cap = (size_t)off * 3 / 2 + 4096;
-        WG_CUDA(cudaMalloc(&s->d_frames, cap));
-        WG_CUDA(cudaHostAlloc(&s->h_frames, cap, cudaHostAllocDefault));
-        s->frames_cap = cap;
+        WG_CUDA(cudaMalloc(&s->d_frames[q], cap));
+        WG_CUDA(cudaHostAlloc(&s->h_frames[q], cap, cudaHostAllocDefault));
+        s->frames_cap[q] = cap;
     }
-    s->frames_bytes = off;
-    s->total_rows = rows;
+    // the table copy above reads `tab` from pageable memory: the copy is complete when
+    // cudaMemcpyAsync returns for pageable sources
+    s->frames_bytes[q] = off;
+    s->total_rows[q] = rows;
+    s->ntab[q] = (int)tab.size();
+    s->layout_dirty[q] = false;
+    return WG_OK;
+}
+
+// A request that has rendered all its frames, or was cancelled, leaves the batch: its
+// final state is downloaded first when it was submitted with keep_result (stream order
+// places the download after its last frame).
+static wg_status server_retire(wg_server *s, ServeReq &r)
+{
+    wg_status st;
+    if (r.slot < 0) return WG_OK;
+    if (r.keep && !r.cancel) {
+        r.res_phi.resize((size_t)r.p.nx * r.p.ny);
+        r.res_psi.resize((size_t)r.p.nx * r.p.ny);
+        if ((st = wg_batch_download(s->batch, r.slot, r.res_phi.data(), r.res_psi.data()))) return st;
+    }
+    if ((st = wg_batch_remove(s->batch, r.slot))) return st;
+    s->used -= r.bytes;
+    r.slot = -1;
+    if (r.cancel) {
+        r.state = WG_REQ_CANCELLED;
+        s->cancelled++;
+    } else if (r.frames_done >= r.frames) {
+        r.state = WG_REQ_DONE;
+        s->completed++;
+    }
+    s->layout_dirty[0] = s->layout_dirty[1] = true;
+    return WG_OK;
+}
+
+static wg_status server_retire_finished(wg_server *s)
+{
+    std::vector<int64_t> keep;
+    bool any = false;
+    for (int64_t id : s->resident) {
+        ServeReq &r = s->reqs[id];
+        if (r.cancel || r.frames_enqueued >= r.frames) {
+            wg_status st = server_retire(s, r);
+            if (st) return st;
+            any = true;
+        } else {
+            keep.push_back(id);
+        }
+    }
+    if (any) s->resident.swap(keep);
+    return WG_OK;
+}
+
+// Waits for the tick enqueued on buffer q and makes its frames readable.
+static wg_status server_complete(wg_server *s, int q, int32_t *nframes)
+{
+    TickRec &t = s->rec[q];
+    if (nframes) *nframes = 0;
+    if (!t.pending) return WG_OK;
+    WG_CUDA(cudaEventSynchronize(s->ev_done[q]));
+    const double t_obs = now_s();
+    float dev = 0.f;
+    WG_CUDA(cudaEventElapsedTime(&dev, s->ev_start[q], s->ev_done[q]));
+    s->dev_ms.push_back(dev);
+    const double lat = 1e3 * (t_obs - t.t_enqueue);
+    for (int64_t id : t.ids) {
+        ServeReq &r = s->reqs[id];
+        r.frames_done++;
+        r.last.tick = t.tick;
+        r.last.buf = q;
+        r.last.off = r.off[q];
+        r.last.index = r.frames_done - 1;
+        s->lat_ms.push_back(lat);
+        if (r.t_first < 0.0) {
+            r.t_first = t_obs;
+            s->first_ms.push_back(1e3 * (t_obs - r.t_submit));
+        }
+        s->frames++;
+        if (r.frames_done >= r.frames && r.slot < 0 && r.state == WG_REQ_RESIDENT) {  // retired already
+            r.state = WG_REQ_DONE;
+            s->completed++;
+        }
+    }
+    s->cell_updates += (double)t.cells * s->cfg.steps_per_frame;
+    s->readable_tick = t.tick;
+    if (nframes) *nframes = (int32_t)t.ids.size();
+    t.pending = false;
+    t.ids.clear();
     return WG_OK;
 }
 
@@ -179,7 +295,8 @@ wg_status wg_server_create(const wg_server_config *cfg, void *stream, wg_server 
 {
     if (!cfg || !out) { set_error("NULL argument"); return WG_ERR_INVALID; }
     if (cfg->frame.plot != WG_P_AMPLITUDE) { set_error("server frames are P_AMPLITUDE frames"); return WG_ERR_INVALID; }
-    if (cfg->steps_per_frame < 1 || cfg->max_scenes < 1 || cfg->frame.size < 1 || !(cfg->frame.scale != 0.0)) {
+    if (cfg->steps_per_frame < 1 || cfg->max_scenes < 1 || cfg->frame.size < 1 || !(cfg->frame.scale != 0.0) ||
+        cfg->pipeline < 0 || cfg->pipeline > 1) {
         set_error("bad server configuration");
         return WG_ERR_INVALID;
     }
@@ -194,6 +311,10 @@ wg_status wg_server_create(const wg_server_config *cfg, void *stream, wg_server 
     wg_status st = wg_batch_create(cfg->precision, s->st, &s->batch);
     if (st) { wg_server_destroy(s); return st; }
     cudaError_t e = cudaMalloc(&s->d_lut, 768);
+    for (int q = 0; q < 2 && e == cudaSuccess; q++) {
+        e = cudaEventCreate(&s->ev_start[q]);
+        if (e == cudaSuccess) e = cudaEventCreate(&s->ev_done[q]);
+    }
     if (e == cudaSuccess) e = cudaMemcpyAsync(s->d_lut, cfg->lut, 768, cudaMemcpyHostToDevice, s->st);
     if (e == cudaSuccess) e = cudaStreamSynchronize(s->st);
     if (e != cudaSuccess) { wg_server_destroy(s); return cuda_fail(e, "wg_server_create"); }
@@ -207,9 +328,13 @@ wg_status wg_server_destroy(wg_server *s)
     if (s->st) cudaStreamSynchronize(s->st);
     if (s->batch) wg_batch_destroy(s->batch);
     if (s->d_lut) cudaFree(s->d_lut);
-    if (s->d_frames) cudaFree(s->d_frames);
-    if (s->h_frames) cudaFreeHost(s->h_frames);
-    if (s->d_ftab) cudaFree(s->d_ftab);
+    for (int q = 0; q < 2; q++) {
+        if (s->d_frames[q]) cudaFree(s->d_frames[q]);
+        if (s->h_frames[q]) cudaFreeHost(s->h_frames[q]);
+        if (s->d_ftab[q]) cudaFree(s->d_ftab[q]);
+        if (s->ev_start[q]) cudaEventDestroy(s->ev_start[q]);
+        if (s->ev_done[q]) cudaEventDestroy(s->ev_done[q]);
+    }
     if (s->own_stream && s->st) cudaStreamDestroy(s->st);
     delete s;
     return WG_OK;
@@ -248,8 +373,11 @@ wg_status wg_server_tick(wg_server *s, int32_t *frames_out)
     if (!s) { set_error("NULL server"); return WG_ERR_INVALID; }
     const double t0 = now_s();
     wg_status st;
-    // 1. admission, first come first served, while the budget and the slots allow
-    bool changed = false;
+    if (frames_out) *frames_out = 0;
+    const int q = (int)(s->ticks & 1), prev = q ^ 1;
+    // 1. finished and cancelled requests leave the batch (their last frames stay readable)
+    if ((st = server_retire_finished(s))) return st;
+    // 2. admission, first come first served, while the budget and the slots allow
     while (!s->queue.empty() && (int)s->resident.size() < s->cfg.max_scenes) {
         ServeReq &r = s->reqs[s->queue.front()];
         if (s->used + r.bytes > s->cfg.hbm_budget) break;
@@ -265,76 +393,88 @@ wg_status wg_server_tick(wg_server *s, int32_t *frames_out)
         s->resident.push_back(r.id);
         s->queue.pop_front();
         s->admitted++;
-        changed = true;
+        s->layout_dirty[0] = s->layout_dirty[1] = true;
     }
-    // the frame table is rebuilt before this tick's frame launch whenever scenes were
-    // admitted now or retired at the end of the previous tick
-    if ((changed || s->layout_dirty) && (st = server_layout(s))) return st;
-    s->layout_dirty = false;
-    if (s->resident.empty()) {
-        if (frames_out) *frames_out = 0;
-        return WG_OK;
-    }
-    // 2. one frame for every resident scene (one graph launch)
-    const double t_step = now_s();
-    if ((st = wg_batch_step(s->batch, s->cfg.steps_per_frame))) return st;
-    // 3. all frames in one launch, one copy to pinned host memory
-    if (s->cfg.precision == WG_FP32)
-        k_server_frames<float><<<s->total_rows, 128, 0, s->st>>>(s->d_ftab, (int)s->resident.size(), s->batch->d_dyn, s->d_lut, s->cfg.frame, s->d_frames);
-    else
-        k_server_frames<double><<<s->total_rows, 128, 0, s->st>>>(s->d_ftab, (int)s->resident.size(), s->batch->d_dyn, s->d_lut, s->cfg.frame, s->d_frames);
-    WG_CUDA(cudaGetLastError());
-    s->batch->launches++;
-    WG_CUDA(cudaMemcpyAsync(s->h_frames, s->d_frames, s->frames_bytes, cudaMemcpyDeviceToHost, s->st));
-    WG_CUDA(cudaStreamSynchronize(s->st));
-    const double t1 = now_s();
-    const double lat = 1e3 * (t1 - t_step);
-    // 4. bookkeeping; retire finished requests
-    std::vector<int64_t> keep_resident;
-    long long cells = 0;
-    for (int64_t id : s->resident) {
-        ServeReq &r = s->reqs[id];
-        cells += (long long)r.p.nx * r.p.ny;
-        r.frames_done++;
-        r.last_index = r.frames_done - 1;
-        r.frame_tick = s->ticks;
-        s->lat_ms.push_back(lat);
-        if (r.t_first < 0.0) {
-            r.t_first = t1;
-            s->first_ms.push_back(1e3 * (t1 - r.t_submit));
-        }
-        s->frames++;
-        if (r.frames_done >= r.frames) {
-            if (r.keep) {
-                r.res_phi.resize((size_t)r.p.nx * r.p.ny);
-                r.res_psi.resize((size_t)r.p.nx * r.p.ny);
-                if ((st = wg_batch_download(s->batch, r.slot, r.res_phi.data(), r.res_psi.data()))) return st;
-            }
-            r.state = WG_REQ_DONE;
-            s->completed++;
-        } else {
-            keep_resident.push_back(id);
-        }
-    }
-    s->cell_updates += (double)cells * s->cfg.steps_per_frame;
-    if (frames_out) *frames_out = (int32_t)s->resident.size();
-    if (keep_resident.size() != s->resident.size()) {
-        // the retired scenes' frames stay readable in the host buffer until the next
-        // layout change; their device memory returns to the pool now
+    int32_t done_prev = 0;
+    if (!s->resident.empty()) {
+        // 3. buffer q's frame table follows the membership (buffer q was last used two
+        // ticks ago, and that tick has completed)
+        if (s->layout_dirty[q] && (st = server_layout(s, q))) return st;
+        // 4. one frame for every resident scene (one graph launch), all frames in one
+        // launch, one copy to pinned host memory, bracketed by the buffer's events
+        TickRec &t = s->rec[q];
+        t.tick = s->ticks;
+        t.t_enqueue = now_s();
+        t.cells = 0;
+        t.ids = s->resident;
         for (int64_t id : s->resident) {
             ServeReq &r = s->reqs[id];
-            if (r.state == WG_REQ_DONE && r.slot >= 0) {
-                if ((st = wg_batch_remove(s->batch, r.slot))) return st;
-                s->used -= r.bytes;
-                r.slot = -1;
-            }
+            t.cells += (long long)r.p.nx * r.p.ny;
+            r.frames_enqueued++;
         }
-        s->resident.swap(keep_resident);
-        s->layout_dirty = true;
+        WG_CUDA(cudaEventRecord(s->ev_start[q], s->st));
+        if ((st = wg_batch_step(s->batch, s->cfg.steps_per_frame))) return st;
+        if (s->cfg.precision == WG_FP32)
+            k_server_frames<float><<<s->total_rows[q], 128, 0, s->st>>>(s->d_ftab[q], s->ntab[q], s->batch->d_dyn,
+                                                                        s->d_lut, s->cfg.frame, s->d_frames[q]);
+        else
+            k_server_frames<double><<<s->total_rows[q], 128, 0, s->st>>>(s->d_ftab[q], s->ntab[q], s->batch->d_dyn,
+                                                                         s->d_lut, s->cfg.frame, s->d_frames[q]);
+        WG_CUDA(cudaGetLastError());
+        s->batch->launches++;
+        WG_CUDA(cudaMemcpyAsync(s->h_frames[q], s->d_frames[q], s->frames_bytes[q], cudaMemcpyDeviceToHost, s->st));
+        WG_CUDA(cudaEventRecord(s->ev_done[q], s->st));
+        t.pending = true;
+        s->ticks++;
     }
-    s->ticks++;
+    // 5. pipelined: the previous tick's frames (its work ran ahead of this tick's);
+    // otherwise this tick's own frames, and the requests they finished leave now
+    if (s->cfg.pipeline) {
+        if ((st = server_complete(s, prev, &done_prev))) return st;
+    } else {
+        if ((st = server_complete(s, q, &done_prev))) return st;
+        if ((st = server_retire_finished(s))) return st;
+    }
+    if (frames_out) *frames_out = done_prev;
     s->busy += now_s() - t0;
     return WG_OK;
+}
+
+wg_status wg_server_drain(wg_server *s, int32_t *frames_out)
+{
+    if (!s) { set_error("NULL server"); return WG_ERR_INVALID; }
+    const double t0 = now_s();
+    if (frames_out) *frames_out = 0;
+    for (int q = 0; q < 2; q++)
+        if (s->rec[q].pending) {
+            wg_status st = server_complete(s, q, frames_out);
+            if (st) return st;
+        }
+    s->busy += now_s() - t0;
+    return WG_OK;
+}
+
+wg_status wg_server_cancel(wg_server *s, int64_t id)
+{
+    if (!s) { set_error("NULL server"); return WG_ERR_INVALID; }
+    auto it = s->reqs.find(id);
+    if (it == s->reqs.end()) { set_error("unknown request %lld", (long long)id); return WG_ERR_NOTFOUND; }
+    ServeReq &r = it->second;
+    if (r.state == WG_REQ_QUEUED) {
+        s->queue.erase(std::find(s->queue.begin(), s->queue.end(), id));
+        r.state = WG_REQ_CANCELLED;
+        r.phi.clear(); r.phi.shrink_to_fit();
+        r.psi.clear(); r.psi.shrink_to_fit();
+        r.xy.clear(); r.xy.shrink_to_fit();
+        s->cancelled++;
+        return WG_OK;
+    }
+    if (r.state == WG_REQ_RESIDENT && !r.cancel && r.slot >= 0) {
+        r.cancel = true;  // leaves the batch at the next tick, before that tick's frame
+        return WG_OK;
+    }
+    set_error("request %lld is finished or already cancelled", (long long)id);
+    return WG_ERR_STATE;
 }
 
 wg_status wg_server_frame(wg_server *s, int64_t id, uint8_t *rgb, int32_t *frame_index, int32_t *width, int32_t *height)
@@ -343,16 +483,16 @@ wg_status wg_server_frame(wg_server *s, int64_t id, uint8_t *rgb, int32_t *frame
     auto it = s->reqs.find(id);
     if (it == s->reqs.end()) { set_error("unknown request %lld", (long long)id); return WG_ERR_NOTFOUND; }
     const ServeReq &r = it->second;
-    if (r.last_index < 0) { set_error("request %lld has no frame yet", (long long)id); return WG_ERR_STATE; }
-    if (r.frame_tick != s->ticks - 1) {  // a later tick has rendered over the host buffer
-        set_error("the last frame of request %lld (tick %lld) was overwritten by tick %lld: read frames before the "
-                  "next tick", (long long)id, (long long)r.frame_tick, (long long)(s->ticks - 1));
+    if (r.last.index < 0) { set_error("request %lld has no frame yet", (long long)id); return WG_ERR_STATE; }
+    if (r.last.tick != s->readable_tick) {  // newer frames have been made readable since
+        set_error("the last frame of request %lld (tick %lld) is no longer in host memory (tick %lld is): read "
+                  "frames before the next tick", (long long)id, (long long)r.last.tick, (long long)s->readable_tick);
         return WG_ERR_STATE;
     }
     if (width) *width = r.w;
     if (height) *height = r.h;
-    if (frame_index) *frame_index = r.last_index;
-    if (rgb) memcpy(rgb, s->h_frames + r.frame_off, (size_t)r.w * r.h * 3);
+    if (frame_index) *frame_index = r.last.index;
+    if (rgb) memcpy(rgb, s->h_frames[r.last.buf] + r.last.off, (size_t)r.w * r.h * 3);
     return WG_OK;
 }
 
@@ -398,6 +538,9 @@ wg_status wg_server_get_stats(wg_server *s, wg_server_stats *o)
     o->first_frame_p99_ms = percentile(s->first_ms, 0.99);
     o->bytes_resident = s->used;
     o->bytes_peak = s->peak;
+    o->tick_device_p50_ms = percentile(s->dev_ms, 0.50);
+    o->tick_device_p99_ms = percentile(s->dev_ms, 0.99);
+    o->cancelled = s->cancelled;
     return WG_OK;
 }
 

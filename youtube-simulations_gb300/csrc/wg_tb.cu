@@ -305,6 +305,27 @@ __device__ __forceinline__ float skew_cell(const DevParams &p, const TbArgs &a, 
 }
 
 
+// skew_cell's inner rule (GEN = false) with the horizontal part of the Laplacian given
+// as he = e - x and hw = x - w: (e - x) + (w - x) == he - hw exactly (round to nearest is
+// symmetric, so w - x == -(x - w)), and a lane's four cells share the five differences
+// of its row, 5 subtractions instead of 8.
+template <int COEF, bool PLAIN, bool KZ = false>
+__device__ __forceinline__ float skew_inner(const DevParams &p, const TbArgs &a, float x, float y, float n, float sv,
+                                            float he, float hw, float cc, bool act)
+{
+    const float ccv = (COEF == WG_COEF_TABLE) ? cc : (act ? a.c2 : a.c2b);
+    const float g = (COEF == WG_COEF_TABLE) ? a.gam : (act ? a.gam : a.gamb);
+    const float lap = ((n - x) + (sv - x)) + (he - hw);
+    if (PLAIN && KZ) return upd32_k0(x, y, ccv, lap, g);
+    if (PLAIN) return upd32(x, y, ccv, lap, a.kappa, g);
+    float v = y;
+    if (p.twospeeds || act) {
+        v = upd32(x, y, ccv, lap, a.kappa, g);
+        if (p.floor_clamp && act) v = fminf(fmaxf(v, -a.vmax), a.vmax);
+    }
+    return v;
+}
+
 // ---------------------------------------------------------------------------
 // Time-skewed streaming (k_step_skew): every warp owns a tile of 128 columns (four
 // adjacent columns j per lane, loaded as float4; a column halo of H = K rounded up to 4
@@ -324,62 +345,9 @@ __device__ __forceinline__ float skew_cell(const DevParams &p, const TbArgs &a, 
 // rule; the source cell gets its increment.  Cells outside the domain keep whatever
 // they got: no cell inside reads them and none is stored.
 // ---------------------------------------------------------------------------
-// Element c (0..3) of a lane's four columns held as two pairs.
-__device__ __forceinline__ float get4(const float2 (&r)[2], int c)
+__device__ __forceinline__ float pick4(float a0, float a1, float a2, float a3, int c)
 {
-    return c == 0 ? r[0].x : (c == 1 ? r[0].y : (c == 2 ? r[1].x : r[1].y));
-}
-__device__ __forceinline__ void set4(float2 (&r)[2], int c, float v)
-{
-    if (c == 0) r[0].x = v;
-    else if (c == 1) r[0].y = v;
-    else if (c == 2) r[1].x = v;
-    else r[1].y = v;
-}
-
-// The inner rule of skew_cell<COEF, false, PLAIN, INL, KZ> for the lane's four columns,
-// as two pairs of packed FP32 instructions (add/sub/mul/fma .f32x2): every element is
-// rounded exactly as the scalar instruction on that element, in the same order
-// (the Laplacian as differences from the centre, then upd32 / upd32_k0), so the fields
-// equal the scalar forms' bit for bit.  X, N, S: level s-1 at rows r, r+1, r-1; Y: level
-// s-2 at row r; e3 / w0: the neighbours right of column 3 and left of column 0; T: tcc
-// (table scenes); act4: the cells' active bits.
-template <int COEF, bool PLAIN, bool KZ>
-__device__ __forceinline__ void inner4(const DevParams &p, const TbArgs &a, const float2 (&X)[2], const float2 (&Y)[2],
-                                       const float2 (&N)[2], const float2 (&S)[2], float e3, float w0,
-                                       const float2 (&T)[2], uint32_t act4, float2 (&out)[2])
-{
-    const float2 E[2] = {make_float2(X[0].y, X[1].x), make_float2(X[1].y, e3)};
-    const float2 Wv[2] = {make_float2(w0, X[0].x), make_float2(X[0].y, X[1].x)};
-#pragma unroll
-    for (int h = 0; h < 2; h++) {
-        const bool a0 = (act4 >> (2 * h)) & 1u, a1 = (act4 >> (2 * h + 1)) & 1u;
-        float2 cc, ng;
-        if (COEF == WG_COEF_TABLE) {
-            cc = T[h];
-            ng = make_float2(-a.gam, -a.gam);
-        } else {
-            cc = make_float2(a0 ? a.c2 : a.c2b, a1 ? a.c2 : a.c2b);
-            ng = make_float2(-(a0 ? a.gam : a.gamb), -(a1 ? a.gam : a.gamb));
-        }
-        const float2 d = add2(add2(sub2(N[h], X[h]), sub2(S[h], X[h])), add2(sub2(E[h], X[h]), sub2(Wv[h], X[h])));
-        const float2 w = sub2(X[h], Y[h]);
-        float2 t = fma2(ng, w, w);
-        if (!KZ) t = fma2(make_float2(-a.kappa, -a.kappa), X[h], t);
-        float2 v = add2(X[h], fma2(cc, d, t));
-        if (!PLAIN) {
-            // cells that are neither active nor in a two-speed scene keep psi (the
-            // reference writes nothing there); FLOOR clamps the active ones
-            const bool u0 = p.twospeeds || a0, u1 = p.twospeeds || a1;
-            if (p.floor_clamp) {
-                if (a0) v.x = fminf(fmaxf(v.x, -a.vmax), a.vmax);
-                if (a1) v.y = fminf(fmaxf(v.y, -a.vmax), a.vmax);
-            }
-            v.x = u0 ? v.x : Y[h].x;
-            v.y = u1 ? v.y : Y[h].y;
-        }
-        out[h] = v;
-    }
+    return c == 0 ? a0 : (c == 1 ? a1 : (c == 2 ? a2 : a3));
 }
 
 // Column 0 (right = false) or ny-1 (right = true) at a row 1..nx-2: the boundary rule of
@@ -464,10 +432,8 @@ __device__ __forceinline__ void skew_strip(const DevParams &p, const TbArgs &a, 
     const int ce = !edge ? -1 : (gj0 == 0 ? 0 : (cr >= 0 && cr <= 3 ? cr : -1));
     const bool src_lane = edge && p.src_on && p.src_j >= gj0 && p.src_j < gj0 + 4;
 
-    // The lane's four columns as two pairs (gj0, gj0+1), (gj0+2, gj0+3): the inner rule
-    // runs on the pairs with packed FP32 instructions.
-    float2 W[K + 1][3][2];  // W[s][k] = level s at row m-s-2+k
-    float2 Yp[2];           // psi(t-1) at row m-1
+    float W[K + 1][3][4];  // W[s][k][c] = level s at row m-s-2+k, column gj0+c
+    float Yp[4];           // psi(t-1) at row m-1
     // tcc at rows m, m-1, ..., m-K (table scenes): the warp's shared ring tring of K+1 rows
     // (slot ts holds row m), each lane writing and reading back only its own 16 bytes
     int ts = 0;
@@ -476,10 +442,11 @@ __device__ __forceinline__ void skew_strip(const DevParams &p, const TbArgs &a, 
 #pragma unroll
     for (int q = 0; q <= K; q++) {
 #pragma unroll
-        for (int k = 0; k < 3; k++) W[q][k][0] = W[q][k][1] = make_float2(0.f, 0.f);
+        for (int c = 0; c < 4; c++) { W[q][0][c] = W[q][1][c] = W[q][2][c] = 0.f; }
         TE[q] = 0.f;
     }
-    Yp[0] = Yp[1] = make_float2(0.f, 0.f);
+#pragma unroll
+    for (int c = 0; c < 4; c++) Yp[c] = 0.f;
 
     // row m goes to slot (m - m0) % D; each lane copies, and later reads, only its own bytes
     auto issue = [&](int m, int slot) {
@@ -519,76 +486,87 @@ __device__ __forceinline__ void skew_strip(const DevParams &p, const TbArgs &a, 
                                                       : make_float4(0.f, 0.f, 0.f, 0.f);
             const uint32_t aw = NEED_ACT ? reinterpret_cast<const uint32_t *>(b)[SL::ACT + lane] : 0u;
             const float tein = need_tce ? b[SL::TCE + lane] : 0.f;
+            const float xin[4] = {xq.x, xq.y, xq.z, xq.w};
+            const float yin[4] = {yq.x, yq.y, yq.z, yq.w};
             if (COEF == WG_COEF_TABLE) *reinterpret_cast<float4 *>(tring + ts * 128 + 4 * lane) = cq;
             if (NEED_ACT) aq = (aq << 4) | ((aw >> (gj0 & 31)) & 0xFu);
             // the slot of row m-1 (read in the previous row) takes row m+QD
             issue(m + QD, slot == 0 ? D - 1 : slot - 1);
             slot = (slot == D - 1) ? 0 : slot + 1;
-            float2 ylev1[2];
+            float ylev1[4];
 #pragma unroll
-            for (int h = 0; h < 2; h++) {
-                W[0][0][h] = W[0][1][h];
-                W[0][1][h] = W[0][2][h];
-                ylev1[h] = Yp[h];
+            for (int c = 0; c < 4; c++) {
+                W[0][0][c] = W[0][1][c];
+                W[0][1][c] = W[0][2][c];
+                W[0][2][c] = xin[c];
+                ylev1[c] = Yp[c];
+                Yp[c] = yin[c];
             }
-            W[0][2][0] = make_float2(xq.x, xq.y);
-            W[0][2][1] = make_float2(xq.z, xq.w);
-            Yp[0] = make_float2(yq.x, yq.y);
-            Yp[1] = make_float2(yq.z, yq.w);
+            if (need_tce) {  // warp-uniform: only tiles that hold a boundary column read TE
 #pragma unroll
-            for (int q = K; q > 0; q--) TE[q] = TE[q - 1];
-            TE[0] = tein;
+                for (int q = K; q > 0; q--) TE[q] = TE[q - 1];
+                TE[0] = tein;
+            }
 #pragma unroll
             for (int lv = 1; lv <= K; lv++) {
                 const int r = m - lv;  // row of this level's new value
-                float2 v[2] = {make_float2(0.f, 0.f), make_float2(0.f, 0.f)};
+                float v[4] = {0.f, 0.f, 0.f, 0.f};
                 // Level lv at row r reaches the stored rows only from r >= i_s - K + lv on, i.e.
                 // from input row m0 + 2 lv + 1: in the pipeline fill the earlier levels are skipped
                 // (warp-uniform), and their window slots hold zeros that nothing reads.
                 if (m - m0 >= 2 * lv + 1) {
-                const float2 (&Wc)[2] = W[lv - 1][1];
-                const float2 (&Wn)[2] = W[lv - 1][2];
-                const float2 (&Ws)[2] = W[lv - 1][0];
-                const float2 (&Yl)[2] = (lv == 1) ? ylev1 : W[lv - 2 >= 0 ? lv - 2 : 0][0];
-                float2 Tl[2] = {make_float2(0.f, 0.f), make_float2(0.f, 0.f)};  // tcc at row r
+                const float *Wc = W[lv - 1][1];
+                const float *Yl = (lv == 1) ? ylev1 : W[lv - 2 >= 0 ? lv - 2 : 0][0];
+                float Tl[4] = {0.f, 0.f, 0.f, 0.f};  // tcc at row r
                 if (COEF == WG_COEF_TABLE) {
                     const int tsl = ts >= lv ? ts - lv : ts - lv + K + 1;
                     const float4 tq = *reinterpret_cast<const float4 *>(tring + tsl * 128 + 4 * lane);
-                    Tl[0] = make_float2(tq.x, tq.y);
-                    Tl[1] = make_float2(tq.z, tq.w);
+                    Tl[0] = tq.x;
+                    Tl[1] = tq.y;
+                    Tl[2] = tq.z;
+                    Tl[3] = tq.w;
                 }
-                const float e3 = __shfl_down_sync(0xffffffffu, Wc[0].x, 1);
-                const float w0 = __shfl_up_sync(0xffffffffu, Wc[1].y, 1);
-                const uint32_t act4 = NEED_ACT ? ((aq >> (4 * lv)) & 0xFu) : 0xFu;
-                inner4<COEF, PLAIN, KZ>(p, a, Wc, Yl, Wn, Ws, e3, w0, Tl, act4, v);
+                const float e3 = __shfl_down_sync(0xffffffffu, Wc[0], 1);
+                const float w0 = __shfl_up_sync(0xffffffffu, Wc[3], 1);
+                // hd[c] = x(gj0+c) - x(gj0+c-1): cell c's e - x is hd[c+1], its x - w is hd[c]
+                const float hd[5] = {Wc[0] - w0, Wc[1] - Wc[0], Wc[2] - Wc[1], Wc[3] - Wc[2], e3 - Wc[3]};
+#pragma unroll
+                for (int c = 0; c < 4; c++) {
+                    const bool act = NEED_ACT ? ((aq >> (4 * lv + c)) & 1u) : true;
+                    v[c] = skew_inner<COEF, PLAIN, KZ>(p, a, Wc[c], Yl[c], W[lv - 1][2][c], W[lv - 1][0][c], hd[c + 1],
+                                                       hd[c], Tl[c], act);
+                }
                 if (!GEN && edge) {  // warp-uniform
                     if (ce >= 0 && r > 0 && r < p.nx - 1) {  // the lane holding column 0 (c = 0) or ny-1 (c = 3)
                         const bool lf = ce == 0;
                         const float res = col_edge_cell<COEF>(
-                            p, a, r, lf ? Wc[0].x : Wc[1].y, lf ? Yl[0].x : Yl[1].y, lf ? Wn[0].x : Wn[1].y,
-                            lf ? Ws[0].x : Ws[1].y, lf ? Wc[0].y : e3, lf ? w0 : Wc[1].x,
-                            lf ? Tl[0].x : Tl[1].y, TE[lv], NEED_ACT ? ((act4 >> ce) & 1u) : true, !lf);
-                        v[0].x = lf ? res : v[0].x;
-                        v[1].y = lf ? v[1].y : res;
+                            p, a, r, lf ? Wc[0] : Wc[3], lf ? Yl[0] : Yl[3], lf ? W[lv - 1][2][0] : W[lv - 1][2][3],
+                            lf ? W[lv - 1][0][0] : W[lv - 1][0][3], lf ? Wc[1] : e3, lf ? w0 : Wc[2],
+                            lf ? Tl[0] : Tl[3], TE[lv], NEED_ACT ? ((aq >> (4 * lv + ce)) & 1u) : true, !lf);
+                        v[0] = lf ? res : v[0];
+                        v[3] = lf ? v[3] : res;
                     }
                     if (src_lane && r == p.src_i) {
                         const double add = INL ? src_inl(p, a.t0 + lv) : a.src[lv - 1];
                         const int cs = p.src_j - gj0;
 #pragma unroll
-                        for (int c = 0; c < 4; c++)
-                            if (cs == c) set4(v, c, (float)A_((double)get4(v, c), add));
+                        for (int c = 0; c < 4; c++) v[c] = (cs == c) ? (float)A_((double)v[c], add) : v[c];
                     }
                 }
                 if (GEN) {
                     const bool row_edge = r == 0 || r == p.nx - 1;  // warp-uniform
                     if (ce >= 0 && r > 0 && r < p.nx - 1) {  // the lane holding column 0 or ny-1: picked by index
                         const float res = col_edge_cell<COEF>(
-                            p, a, r, get4(Wc, ce), get4(Yl, ce), get4(Wn, ce), get4(Ws, ce),
-                            ce < 3 ? get4(Wc, ce + 1) : e3, ce > 0 ? get4(Wc, ce - 1) : w0, get4(Tl, ce), TE[lv],
-                            NEED_ACT ? ((act4 >> ce) & 1u) : true, gj0 != 0);
-#pragma unroll
-                        for (int c = 0; c < 4; c++)
-                            if (ce == c) set4(v, c, res);
+                            p, a, r, pick4(Wc[0], Wc[1], Wc[2], Wc[3], ce), pick4(Yl[0], Yl[1], Yl[2], Yl[3], ce),
+                            pick4(W[lv - 1][2][0], W[lv - 1][2][1], W[lv - 1][2][2], W[lv - 1][2][3], ce),
+                            pick4(W[lv - 1][0][0], W[lv - 1][0][1], W[lv - 1][0][2], W[lv - 1][0][3], ce),
+                            pick4(Wc[1], Wc[2], Wc[3], e3, ce), pick4(w0, Wc[0], Wc[1], Wc[2], ce),
+                            pick4(Tl[0], Tl[1], Tl[2], Tl[3], ce), TE[lv],
+                            NEED_ACT ? ((aq >> (4 * lv + ce)) & 1u) : true, gj0 != 0);
+                        v[0] = (ce == 0) ? res : v[0];
+                        v[1] = (ce == 1) ? res : v[1];
+                        v[2] = (ce == 2) ? res : v[2];
+                        v[3] = (ce == 3) ? res : v[3];
                     }
                     if (row_edge) {  // rows 0 and nx-1 by the general rule, one cell at a time
 #pragma unroll 1
@@ -597,25 +575,30 @@ __device__ __forceinline__ void skew_strip(const DevParams &p, const TbArgs &a, 
                             if (gj < 0 || gj >= p.ny) continue;
                             const float tcv = (COEF == WG_COEF_TABLE && a.tc) ? a.tc[(size_t)r * p.pitch + gj] : 0.f;
                             const float res = skew_cell<COEF, true, false, INL>(
-                                p, a, r, gj, lv, get4(Wc, c), get4(Yl, c), get4(Wn, c), get4(Ws, c),
-                                c < 3 ? get4(Wc, c + 1) : e3, c > 0 ? get4(Wc, c - 1) : w0, get4(Tl, c), tcv,
-                                NEED_ACT ? ((act4 >> c) & 1u) : true);
-                            set4(v, c, res);
+                                p, a, r, gj, lv, pick4(Wc[0], Wc[1], Wc[2], Wc[3], c), pick4(Yl[0], Yl[1], Yl[2], Yl[3], c),
+                                pick4(W[lv - 1][2][0], W[lv - 1][2][1], W[lv - 1][2][2], W[lv - 1][2][3], c),
+                                pick4(W[lv - 1][0][0], W[lv - 1][0][1], W[lv - 1][0][2], W[lv - 1][0][3], c),
+                                pick4(Wc[1], Wc[2], Wc[3], e3, c), pick4(w0, Wc[0], Wc[1], Wc[2], c),
+                                pick4(Tl[0], Tl[1], Tl[2], Tl[3], c), tcv,
+                                NEED_ACT ? ((aq >> (4 * lv + c)) & 1u) : true);
+                            v[0] = (c == 0) ? res : v[0];
+                            v[1] = (c == 1) ? res : v[1];
+                            v[2] = (c == 2) ? res : v[2];
+                            v[3] = (c == 3) ? res : v[3];
                         }
                     } else if (src_lane && r == p.src_i) {  // the general rule adds it on rows 0 and nx-1
                         const double add = INL ? src_inl(p, a.t0 + lv) : a.src[lv - 1];
                         const int cs = p.src_j - gj0;
 #pragma unroll
-                        for (int c = 0; c < 4; c++)
-                            if (cs == c) set4(v, c, (float)A_((double)get4(v, c), add));
+                        for (int c = 0; c < 4; c++) v[c] = (cs == c) ? (float)A_((double)v[c], add) : v[c];
                     }
                 }
                 }  // levels in use
 #pragma unroll
-                for (int h = 0; h < 2; h++) {
-                    W[lv][0][h] = W[lv][1][h];
-                    W[lv][1][h] = W[lv][2][h];
-                    W[lv][2][h] = v[h];
+                for (int c = 0; c < 4; c++) {
+                    W[lv][0][c] = W[lv][1][c];
+                    W[lv][1][c] = W[lv][2][c];
+                    W[lv][2][c] = v[c];
                 }
             }
             ts = (ts == K) ? 0 : ts + 1;  // row m+1's tcc slot
@@ -624,17 +607,16 @@ __device__ __forceinline__ void skew_strip(const DevParams &p, const TbArgs &a, 
                 const size_t o = (size_t)r * p.pitch + gj0;
                 if (gj0 + 3 < p.ny) {
                     if (grp_ok) {
-                        *reinterpret_cast<float4 *>(a.phi_out + o) =
-                            make_float4(W[K][2][0].x, W[K][2][0].y, W[K][2][1].x, W[K][2][1].y);
+                        *reinterpret_cast<float4 *>(a.phi_out + o) = make_float4(W[K][2][0], W[K][2][1], W[K][2][2], W[K][2][3]);
                         *reinterpret_cast<float4 *>(a.psi_out + o) =
-                            make_float4(W[K - 1][1][0].x, W[K - 1][1][0].y, W[K - 1][1][1].x, W[K - 1][1][1].y);
+                            make_float4(W[K - 1][1][0], W[K - 1][1][1], W[K - 1][1][2], W[K - 1][1][3]);
                     }
                 } else if (grp_ok) {
 #pragma unroll
                     for (int c = 0; c < 4; c++)
                         if (gj0 + c < p.ny) {
-                            a.phi_out[o + c] = get4(W[K][2], c);
-                            a.psi_out[o + c] = get4(W[K - 1][1], c);
+                            a.phi_out[o + c] = W[K][2][c];
+                            a.psi_out[o + c] = W[K - 1][1][c];
                         }
                 }
             }

@@ -107,10 +107,13 @@ class WgFrameParams(ctypes.Structure):
 class WgServerConfig(ctypes.Structure):
     _fields_ = [
         ("precision", ctypes.c_int32), ("steps_per_frame", ctypes.c_int32),
-        ("max_scenes", ctypes.c_int32), ("reserved", ctypes.c_int32),
+        ("max_scenes", ctypes.c_int32), ("pipeline", ctypes.c_int32),
         ("hbm_budget", ctypes.c_uint64), ("frame", WgFrameParams),
         ("lut", ctypes.c_uint8 * 768),
     ]
+
+
+REQ_QUEUED, REQ_RESIDENT, REQ_DONE, REQ_CANCELLED = 0, 1, 2, 3
 
 
 class WgServerStats(ctypes.Structure):
@@ -121,5 +124,6 @@ class WgServerStats(ctypes.Structure):
         ("frame_latency_p50_ms", ctypes.c_double), ("frame_latency_p99_ms", ctypes.c_double),
         ("frame_latency_max_ms", ctypes.c_double), ("first_frame_p50_ms", ctypes.c_double),
         ("first_frame_p99_ms", ctypes.c_double), ("bytes_resident", ctypes.c_uint64),
-        ("bytes_peak", ctypes.c_uint64),
+        ("bytes_peak", ctypes.c_uint64), ("tick_device_p50_ms", ctypes.c_double),
+        ("tick_device_p99_ms", ctypes.c_double), ("cancelled", ctypes.c_int64),
     ]

@@ -102,6 +102,8 @@ SIGNATURES = {
     "wg_server_destroy": (_I32, [_V]),
     "wg_server_submit": (_I32, [_V, _V, _V, _V, _V, _I32, _I32, ctypes.POINTER(_I64)]),
     "wg_server_tick": (_I32, [_V, ctypes.POINTER(_I32)]),
+    "wg_server_drain": (_I32, [_V, ctypes.POINTER(_I32)]),
+    "wg_server_cancel": (_I32, [_V, _I64]),
     "wg_server_frame": (_I32, [_V, _I64, _V, ctypes.POINTER(_I32), ctypes.POINTER(_I32), ctypes.POINTER(_I32)]),
     "wg_server_result": (_I32, [_V, _I64, _V, _V]),
     "wg_server_request_state": (_I32, [_V, _I64, ctypes.POINTER(_I32), ctypes.POINTER(_I32)]),
@@ -507,13 +509,16 @@ class Batch:
 
 class Server:
     """Serving loop (wg_server_*): requests admitted under an HBM budget into a running
-    batch, one frame per tick for every resident scene, RGB8 frames to host memory."""
+    batch, one frame per tick for every resident scene, RGB8 frames to host memory.
+    pipeline=True: a tick enqueues its device work and then waits for the previous
+    tick's frames (drain() waits for the last one)."""
 
     def __init__(self, lut, precision=P.FP32, steps_per_frame=10, max_scenes=512, hbm_budget=150 << 30,
                  size=2, vshift=-0.2, vscale=1.0, slope=1.0, color_range=0.8, scale=1.0, stream=None,
-                 plot=P.P_AMPLITUDE):
+                 plot=P.P_AMPLITUDE, pipeline=False):
         cfg = P.WgServerConfig()
         cfg.precision, cfg.steps_per_frame, cfg.max_scenes, cfg.hbm_budget = precision, steps_per_frame, max_scenes, hbm_budget
+        cfg.pipeline = 1 if pipeline else 0
         cfg.frame = P.WgFrameParams(size, 0, vshift, vscale, slope, color_range, scale, 1.0, 0, int(plot))
         lut = np.ascontiguousarray(lut, np.uint8).reshape(-1)
         ctypes.memmove(cfg.lut, lut.ctypes.data, 768)
@@ -553,6 +558,14 @@ class Server:
         n = _I32()
         check(lib().wg_server_tick(self.h, ctypes.byref(n)))
         return n.value
+
+    def drain(self):
+        n = _I32()
+        check(lib().wg_server_drain(self.h, ctypes.byref(n)))
+        return n.value
+
+    def cancel(self, rid):
+        check(lib().wg_server_cancel(self.h, int(rid)))
 
     def state(self, rid):
         st, fd = _I32(), _I32()
