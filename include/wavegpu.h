@@ -301,13 +301,21 @@ wg_status wg_scene_frame_reset(wg_scene *s);
  * 0 rectangle, 1 ellipse, 2 stadium, 8 polygon (npoly, apoly), 20 discs, 201 discs in a
  * rectangle (circles: ncircles x (xc, yc, radius), the reference's circles[]), and for
  * WG_COEF_TABLE scenes the tables of init_ior_2d (sub_wave.c:12983-13002).  Then
- * wg_scene_upload_state sets phi and psi.  Masks are 0/1; Neumann scenes are refused
- * (their ghost cells and records come from the host).  The polygon's cos/sin are
+ * wg_scene_upload_state sets phi and psi.  Masks are 0/1.  A Neumann scene (BC_NEUMANN,
+ * WG_COEF_TABLE, domain 1 or 8) also gets the set-up of init_neumann_bc
+ * (sub_wave.c:13720-13947) on the device after its tables: ghost cells (outside, a
+ * 4-neighbour inside) marked -1, one record each in the reference's row-major order, with
+ * test_neumann_data's deactivation.  The polygon's cos/sin (and its normal's atan) are
  * CUDA's: a cell within rounding of an edge may fall on the other side. */
 wg_status wg_scene_build_domain(wg_scene *s, int32_t domain, double lambda, int32_t npoly, double apoly,
                                 const double *circles, int32_t ncircles);
-/* The scene's mask as 0/1 (1 where xy != 0), [nx][ny]. */
+/* The scene's mask, [nx][ny]: 1 inside, 0 outside, -1 for Neumann ghost cells. */
 wg_status wg_scene_download_mask(wg_scene *s, int16_t *xy);
+/* The Neumann records wg_scene_build_domain made on the device (the reference's
+ * t_neumann_bc, global_pdes.c:518-528): *count = their number; out (room for capacity
+ * records) may be NULL to ask the count only.  WG_ERR_STATE for records set from the
+ * host. */
+wg_status wg_scene_neumann_records(wg_scene *s, wg_neumann_bc *out, int32_t capacity, int32_t *count);
 /* RGB8 frame (row 0 at the bottom, width x height pixels) to a file: the uncompressed
  * baseline TIFF of writetiff (sub_wave.c:62-122: 8-bit RGB, one row per strip,
  * ORIENTATION_BOTLEFT, `description` as ImageDescription, scanline s = row

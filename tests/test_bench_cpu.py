@@ -28,3 +28,46 @@ def test_active_cells_counts_the_inside_of_the_mask():
 def test_active_rate_scales_the_all_cell_rate():
     res = bench.with_active_rate({"value": 100.0}, active=300, cells=400)
     assert res["active_cell_rate"] == 75.0 and res["value"] == 100.0
+
+
+class FakeServer:
+    """Host-only stand-in for W.Server: a request needs `frames` ticks once submitted."""
+
+    def __init__(self):
+        self.left, self.submit_times, self.t0, self.done = [], [], None, 0
+
+    def submit(self, params, phi, psi, xy, frames):
+        import time
+        self.submit_times.append(time.perf_counter())
+        self.left.append(frames)
+
+    def stats(self):
+        return {"resident": sum(1 for f in self.left if f > 0), "queued": 0, "completed": self.done,
+                "cancelled": 0}
+
+    def tick(self):
+        for k, f in enumerate(self.left):
+            if f > 0:
+                self.left[k] = f - 1
+                if f == 1:
+                    self.done += 1
+        return 0
+
+    def drain(self):
+        return 0
+
+
+def test_serve_stream_submits_on_the_wall_clock():
+    import time
+
+    class M:
+        params = phi = psi = xy = None
+    reqs = [(M(), 3), (M(), 1), (M(), 2)]
+    arrivals = np.array([0.0, 0.05, 0.12])
+    srv = FakeServer()
+    t0 = time.perf_counter()
+    wall, max_q, max_res = bench.serve_stream(None, srv, reqs, arrivals)
+    assert srv.done == 3 and len(srv.submit_times) == 3
+    for t, a in zip(srv.submit_times, arrivals):
+        assert t - t0 >= a - 1e-3  # never submitted before its arrival time
+    assert wall >= 0.12 and max_q == 0 and max_res >= 1

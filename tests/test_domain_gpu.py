@@ -96,3 +96,70 @@ def test_build_domain_refusals():
             s.upload_state(np.zeros(p.nx * p.ny), np.zeros(p.nx * p.ny))   # no mask yet
         with pytest.raises(W.WaveGpuError):
             s.build_domain(5)
+
+
+NEU = [("full_neu_ellipse", 301, 221), ("full_neu_polygon", 301, 221), ("full_neu_ellipse", 67, 45)]
+
+
+@pytest.mark.parametrize("variant,nx,ny", NEU)
+def test_device_neumann_setup_matches_oracle(variant, nx, ny):
+    """init_neumann_bc on the device: the ghost marks (-1), and every record (cell,
+    normal weights, neighbours, active flag) in the reference's order, against the
+    oracle's restatement (pinned bit for bit to the reference's SETUP).  Ellipse: equal
+    in every bit.  Polygon: its normal uses CUDA's atan/cos/sin, so weights agree to
+    1e-12 and a cell within rounding of a side may take the neighbouring side's normal."""
+    import ref_variants
+    m = ref_variants.VARIANTS[variant]["macros"]
+    p = params_of(variant, nx=nx, ny=ny)
+    dom, lam, npoly, apoly = m["B_DOMAIN"], m["LAMBDA"], m["NPOLY"], m["APOLY"]
+    mask = oracle.mask(p, dom, lam, npoly, apoly)
+    ref_xy, ref = oracle.init_neumann(p, dom, lam, mask, npoly=npoly, apoly=apoly)
+    with W.Scene(p, P.FP64, P.COEF_TABLE) as s:
+        s.build_domain(dom, lam=lam, npoly=npoly, apoly=apoly)
+        got_xy = s.download_mask()
+        got = s.neumann_records()
+    assert len(ref) > 0 and np.count_nonzero(ref_xy == -1) == len(ref)
+    assert np.array_equal(got_xy, ref_xy)
+    assert len(got) == len(ref)
+    assert np.array_equal(got["i"], ref["i"]) and np.array_equal(got["j"], ref["j"])
+    ints = ["signx1", "signy1", "signx2", "signy2", "nbi1", "nbj1", "nbi2", "nbj2", "top", "active"]
+    if dom == scenes.D_ELLIPSE:
+        for k in ints + ["nx", "ny"]:
+            assert np.array_equal(got[k], ref[k]), k
+    else:
+        same = np.ones(len(ref), bool)
+        for k in ints:
+            same &= got[k] == ref[k]
+        assert np.mean(same) >= 0.98
+        assert np.max(np.abs(got["nx"][same] - ref["nx"][same])) <= 1e-12
+        assert np.max(np.abs(got["ny"][same] - ref["ny"][same])) <= 1e-12
+
+
+@pytest.mark.parametrize("prec", [P.FP64, P.FP32])
+def test_device_neumann_scene_steps_like_host_setup(prec):
+    """A Neumann ellipse scene built on the device steps bit for bit like the same scene
+    uploaded from the host with the oracle's ghost marks, tables and records (tables from
+    the mask before the ghost marks, as the reference calls init_ior_2d before
+    init_neumann_bc)."""
+    variant = "full_neu_ellipse"
+    p = params_of(variant, nx=161, ny=121)
+    mask = oracle.mask(p, scenes.D_ELLIPSE, 1.8)
+    tcc, tc, tg = scenes.tables(p, mask)
+    xy, nbc = oracle.init_neumann(p, scenes.D_ELLIPSE, 1.8, mask)
+    rng = np.random.default_rng(3)
+    x, y = scenes.grid_xy(p)
+    phi = scenes.pulse(p, np.ones(p.nx * p.ny, np.int16), x[70], y[60], variance=0.05 ** 2)
+    phi = np.where(xy != 0, phi + 0.01 * rng.standard_normal(p.nx * p.ny), 0.0)
+    psi = phi * 0.99
+    out = []
+    for device in (False, True):
+        with W.Scene(p, prec, P.COEF_TABLE) as s:
+            if device:
+                s.build_domain(scenes.D_ELLIPSE, lam=1.8)
+                s.upload_state(phi, psi)
+            else:
+                s.upload(phi, psi, xy, tcc, tc, tg)
+                s.set_neumann(nbc)
+            s.step(40)
+            out.append(s.download())
+    assert np.array_equal(out[0][0], out[1][0]) and np.array_equal(out[0][1], out[1][1])

@@ -32,23 +32,13 @@
 namespace wg {
 
 // A boundary-line cell (reference rules) plus the point source; out of line so that
-// the tile loop below stays small.
+// the tile loop below stays small.  Its arguments are plain pointers and values: the
+// rule's argument block is built here, in registers of this call, not passed by address
+// (an address taken across the call would put the block in local memory).
 template <class T>
-__device__ __noinline__ T batch_edge(const DevParams &p, const FastArgs<T> &a, int i, int j, long long time, T y)
+__device__ __noinline__ T batch_edge(const DevParams &p, const T *phi, T *out, const uint32_t *act, const uint32_t *nz,
+                                     int i, int j, long long time, T y)
 {
-    T v = fast_edge<T, WG_COEF_MASK>(p, a, i, j, time, y);
-    if (p.src_on && i == p.src_i && j == p.src_j) v = (T)A_((double)v, point_source(p, time));
-    return v;
-}
-
-// Z (FP64 scenes): upd64's flags for KAPPA = 0 and GAMMA = GAMMAB = 0, the bulk update
-// without those zero terms (values unchanged).
-template <class T, int Z = 0>
-__device__ __forceinline__ void batch_tile(const DevParams &p, const T *__restrict__ phi, T *__restrict__ out,
-                                           const uint32_t *__restrict__ act, const uint32_t *__restrict__ nz,
-                                           int i0, int jt, long long time)
-{
-    constexpr int V = Vec<T>::n;
     FastArgs<T> a;
     a.phi = phi;
     a.psi = out;
@@ -63,55 +53,89 @@ __device__ __forceinline__ void batch_tile(const DevParams &p, const T *__restri
     a.kappaf = (float)p.kappa;
     a.has_ghosts = 0;
     a.do_source = 1;
+    T v = fast_edge<T, WG_COEF_MASK>(p, a, i, j, time, y);
+    if (p.src_on && i == p.src_i && j == p.src_j) v = (T)A_((double)v, point_source(p, time));
+    return v;
+}
+
+// The scene values the bulk update reads, held in registers for a work item (the
+// descriptor lives in global memory, which the tile's stores could alias); the
+// coefficients in the field precision only.
+template <class T>
+struct TileCoef {
+    int nx, ny, pitch, wpitch, twospeeds, floor_clamp;
+    T c2, c2b, gam, gamb, kappa;
+};
+
+// Z (FP64 scenes): upd64's flags for KAPPA = 0 and GAMMA = GAMMAB = 0, the bulk update
+// without those zero terms (values unchanged).
+template <class T, int Z = 0>
+__device__ __forceinline__ void batch_tile(const DevParams &p, const T *__restrict__ phi, T *__restrict__ out,
+                                           const uint32_t *__restrict__ act, const uint32_t *__restrict__ nz,
+                                           int i0, int jt, long long time)
+{
+    constexpr int V = Vec<T>::n;
+    const TileCoef<T> k{p.nx, p.ny, p.pitch, p.wpitch, p.twospeeds, p.floor_clamp,
+                        (T)p.c2, (T)p.c2b, (T)p.gam, (T)p.gamb, (T)p.kappa};
     const int j0 = (jt * BT_THREADS + (int)threadIdx.x) * V;
+    // interior rows: the bulk rule (boundary columns and padding keep psi for now)
     for (int rr = threadIdx.y; rr < BT_ROWS; rr += blockDim.y) {
         const int i = i0 + rr;
-        if (i >= p.nx || j0 >= p.pitch) continue;
-        const size_t row = (size_t)i * p.pitch;
-        if (i == 0 || i == p.nx - 1) {
-            for (int k = 0; k < V; k++) {
-                const int j = j0 + k;
-                if (j >= p.ny) break;
-                out[row + j] = batch_edge<T>(p, a, i, j, time, out[row + j]);
-            }
-            continue;
-        }
+        if (i >= k.nx - 1 || i == 0 || j0 >= k.pitch) continue;
+        const size_t row = (size_t)i * k.pitch;
         T c[V], y[V], n[V], s[V];
         vload(phi + row + j0, c);
         vload(out + row + j0, y);
-        vload(phi + row + p.pitch + j0, n);
-        vload(phi + row - p.pitch + j0, s);
+        vload(phi + row + k.pitch + j0, n);
+        vload(phi + row - k.pitch + j0, s);
         const T wl = (j0 > 0) ? phi[row + j0 - 1] : (T)0;
-        const T er = (j0 + V < p.pitch) ? phi[row + j0 + V] : (T)0;
-        const uint32_t word = act[(size_t)i * p.wpitch + (j0 >> 5)] >> (j0 & 31);
+        const T er = (j0 + V < k.pitch) ? phi[row + j0 + V] : (T)0;
+        const uint32_t word = act[(size_t)i * k.wpitch + (j0 >> 5)] >> (j0 & 31);
         T o[V];
 #pragma unroll
-        for (int k = 0; k < V; k++) {
-            const int j = j0 + k;
-            T v = y[k];
-            const bool ac = (word >> k) & 1u;
-            if (j >= 1 && j < p.ny - 1 && (p.twospeeds || ac)) {
-                const T x = c[k];
-                const T w = (k == 0) ? wl : c[k - 1];
-                const T e = (k == V - 1) ? er : c[k + 1];
+        for (int q = 0; q < V; q++) {
+            const int j = j0 + q;
+            T v = y[q];
+            const bool ac = (word >> q) & 1u;
+            if (j >= 1 && j < k.ny - 1 && (k.twospeeds || ac)) {
+                const T x = c[q];
+                const T w = (q == 0) ? wl : c[q - 1];
+                const T e = (q == V - 1) ? er : c[q + 1];
                 if (sizeof(T) == 8) {
-                    const double delta = L4_(A_(A_(A_((double)n[k], (double)s[k]), (double)e), (double)w), (double)x);
-                    v = (T)upd64<Z>((double)x, (double)y[k], ac ? p.c2 : p.c2b, delta, p.kappa, ac ? p.gam : p.gamb);
+                    const double delta = L4_(A_(A_(A_((double)n[q], (double)s[q]), (double)e), (double)w), (double)x);
+                    v = (T)upd64<Z>((double)x, (double)y[q], ac ? (double)k.c2 : (double)k.c2b, delta, (double)k.kappa,
+                                    ac ? (double)k.gam : (double)k.gamb);
                 } else {
                     const float xf = (float)x;
-                    const float delta = (((float)n[k] - xf) + ((float)s[k] - xf)) + (((float)e - xf) + ((float)w - xf));
-                    v = (T)upd32(xf, (float)y[k], ac ? a.c2f : a.c2bf, delta, a.kappaf, ac ? a.gamf : a.gambf);
+                    const float delta = (((float)n[q] - xf) + ((float)s[q] - xf)) + (((float)e - xf) + ((float)w - xf));
+                    v = (T)upd32(xf, (float)y[q], ac ? (float)k.c2 : (float)k.c2b, delta, (float)k.kappa,
+                                 ac ? (float)k.gam : (float)k.gamb);
                 }
-                if (p.floor_clamp && ac) v = (T)floor_clamp(p, (double)v);
+                if (k.floor_clamp && ac) v = (T)floor_clamp(p, (double)v);
             }
-            o[k] = v;
+            o[q] = v;
         }
         vstore(out + row + j0, o);
-        // this thread's boundary-line cells and an interior point source, after the store
-        if (j0 == 0) out[row] = batch_edge<T>(p, a, i, 0, time, y[0]);
-        if (p.ny - 1 >= j0 && p.ny - 1 < j0 + V) out[row + p.ny - 1] = batch_edge<T>(p, a, i, p.ny - 1, time, out[row + p.ny - 1]);
-        if (p.src_on && i == p.src_i && p.src_j >= j0 && p.src_j < j0 + V && p.src_j > 0 && p.src_j < p.ny - 1)
-            out[row + p.src_j] = (T)A_((double)out[row + p.src_j], point_source(p, time));
+    }
+    // then the boundary lines and the point source, by the threads that stored those
+    // cells above (each reads phi and its own cell's psi, which the loop above left)
+    const bool col0 = j0 == 0, colr = k.ny - 1 >= j0 && k.ny - 1 < j0 + V;
+    const bool srcj = p.src_on && p.src_j >= j0 && p.src_j < j0 + V && p.src_j > 0 && p.src_j < k.ny - 1;
+    for (int rr = threadIdx.y; rr < BT_ROWS; rr += blockDim.y) {
+        const int i = i0 + rr;
+        if (i >= k.nx || j0 >= k.pitch) continue;
+        const size_t row = (size_t)i * k.pitch;
+        if (i == 0 || i == k.nx - 1) {
+            for (int q = 0; q < V; q++) {
+                const int j = j0 + q;
+                if (j >= k.ny) break;
+                out[row + j] = batch_edge<T>(p, phi, out, act, nz, i, j, time, out[row + j]);
+            }
+            continue;
+        }
+        if (col0) out[row] = batch_edge<T>(p, phi, out, act, nz, i, 0, time, out[row]);
+        if (colr) out[row + k.ny - 1] = batch_edge<T>(p, phi, out, act, nz, i, k.ny - 1, time, out[row + k.ny - 1]);
+        if (srcj && i == p.src_i) out[row + p.src_j] = (T)A_((double)out[row + p.src_j], point_source(p, time));
     }
 }
 
@@ -522,7 +546,7 @@ static void batch_enqueue_frame(wg_batch *b, int n, bool skewed)
 // Depth and row chunk per size class, in two stages: depths 2..6 with the list-wide
 // chunk, then chunks of 32, 64, 128 and 256 rows at the best depth.  Each candidate
 // times one skewed pass over the class's scenes (reading their current fields, writing
-// the other pair, so the state does not change), best of three after one untimed pass;
+// the other pair, so the state does not change), best of five after one untimed pass;
 // the fastest per update is kept.  Nine candidates per class keep the tuning frame of a
 // server tick short.
 // Tuned classes are kept for the process (per device): a later batch or server whose
@@ -576,8 +600,8 @@ static wg_status batch_autotune(wg_batch *b)
             b->launches++;
             ghosts = true;
         }
-        cudaEvent_t ev[4];
-        for (int q = 0; q < 4; q++) WG_CUDA(cudaEventCreate(&ev[q]));
+        cudaEvent_t ev[6];
+        for (int q = 0; q < 6; q++) WG_CUDA(cudaEventCreate(&ev[q]));
         int best = 0, best_rows = 0;
         double best_ms = 1e30;
         int4 *dev = nullptr;
@@ -593,7 +617,7 @@ static wg_status batch_autotune(wg_batch *b)
             if (err == cudaSuccess && nt) err = cudaMemcpyAsync(dev, tasks.data(), sizeof(int4) * nt, cudaMemcpyHostToDevice, b->st);
             const int idx = b->skew_n_cap - 1;  // the count slot kept for tuning
             if (err == cudaSuccess) err = cudaMemcpyAsync(b->d_skew_n + idx, &nt, sizeof(int), cudaMemcpyHostToDevice, b->st);
-            const int reps = 3;  // one untimed pass, then the best of three
+            const int reps = 5;  // one untimed pass, then the best of five
             for (int r = 0; r <= reps && err == cudaSuccess; r++) {
                 cudaMemsetAsync(b->d_tune_ticket + r, 0, sizeof(int), b->st);
                 launch_batch_skew(K, b->d_tab, b->d_dyn, dev, b->d_skew_n + idx, b->d_tune_ticket + r, 0, 0, b->st);
@@ -619,7 +643,7 @@ static wg_status batch_autotune(wg_batch *b)
                 best_rows = R;
             }
         }
-        for (int q = 0; q < 4; q++) cudaEventDestroy(ev[q]);
+        for (int q = 0; q < 6; q++) cudaEventDestroy(ev[q]);
         if (err != cudaSuccess) return cuda_fail(err, "batch autotune");
         b->class_k[c] = best;
         b->class_rows[c] = best_rows;
@@ -666,7 +690,7 @@ wg_status wg_batch_create(int32_t precision, void *stream, wg_batch **out)
     b->skew_n_cap = 32;
     if (e == cudaSuccess) e = cudaMalloc(&b->d_skew_n, sizeof(int) * b->skew_n_cap);
     if (e == cudaSuccess) e = cudaMemsetAsync(b->d_skew_n, 0, sizeof(int) * b->skew_n_cap, b->st);
-    if (e == cudaSuccess) e = cudaMalloc(&b->d_tune_ticket, sizeof(int) * 4);
+    if (e == cudaSuccess) e = cudaMalloc(&b->d_tune_ticket, sizeof(int) * 8);
     if (e != cudaSuccess) {
         wg_status r = cuda_fail(e, "wg_batch_create");
         wg_batch_destroy(b);

@@ -278,7 +278,8 @@ __global__ void k_neumann_fast(DevParams p, const T *__restrict__ phi, T *__rest
 {
     const int q = blockIdx.x * blockDim.x + threadIdx.x;
     if (q >= n) return;
-    const int4 r = idx[q];       // cell, nb1, nb2 (element offsets), flags (bit0 floor)
+    const int4 r = idx[q];       // cell, nb1, nb2 (element offsets), flags (bit0 floor, bit1 inactive)
+    if (r.w & 2) return;
     const double2 cw = w[q];
     double v = M_(cw.x, (double)phi[r.y]);
     v = A_(v, M_(cw.y, (double)phi[r.z]));

@@ -230,7 +230,8 @@ wg_status wg_scene_destroy(wg_scene *s)
     for (auto &f : s->f) if (f) cudaFree(f);
     for (auto &g : s->g) if (g) cudaFree(g);
     void *dev[] = {s->act, s->nz, s->tcc, s->tc, s->tg, s->nidx, s->nw, s->ebot, s->etop, s->eout, s->dcount,
-                   s->dstage, s->rgb, s->lut, s->bv_osc, s->bv_src, s->dflag, s->facc, s->probe_cells, s->probe_buf};
+                   s->dstage, s->rgb, s->lut, s->bv_osc, s->bv_src, s->dflag, s->facc, s->probe_cells, s->probe_buf,
+                   s->nrec_dev};
     for (void *d : dev) if (d) cudaFree(d);
     for (auto &c : s->skew) if (c.dev) cudaFree(c.dev);
     if (s->hout) cudaFreeHost(s->hout);
@@ -380,8 +381,11 @@ wg_status wg_scene_set_neumann(wg_scene *s, const wg_neumann_bc *r, int32_t n)
     }
     if (s->nidx) cudaFree(s->nidx);
     if (s->nw) cudaFree(s->nw);
+    if (s->nrec_dev) cudaFree(s->nrec_dev);
     s->nidx = nullptr;
     s->nw = nullptr;
+    s->nrec_dev = nullptr;
+    s->nrec_all = n;
     s->nrec = (int)idx.size();
     if (s->nrec) {
         WG_CUDA(cudaMalloc(&s->nidx, sizeof(int4) * idx.size()));

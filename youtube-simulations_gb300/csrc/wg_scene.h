@@ -28,7 +28,9 @@ struct wg_scene {
     void *tcc = nullptr, *tc = nullptr, *tg = nullptr;
     int4 *nidx = nullptr;
     double2 *nw = nullptr;
-    int nrec = 0;
+    int nrec = 0;                          // gather entries (flag bit 1: an inactive record)
+    wg_neumann_bc *nrec_dev = nullptr;     // records built on the device (wg_scene_build_domain)
+    int nrec_all = 0;
     long long time = 0, launches = 0;
     double2 *ebot = nullptr, *etop = nullptr;
     double *eout = nullptr, *hout = nullptr;

@@ -82,6 +82,7 @@ SIGNATURES = {
     "wg_scene_frame_reset": (_I32, [_V]),
     "wg_scene_build_domain": (_I32, [_V, _I32, _D, _I32, _D, _V, _I32]),
     "wg_scene_download_mask": (_I32, [_V, _V]),
+    "wg_scene_neumann_records": (_I32, [_V, _V, _I32, ctypes.POINTER(_I32)]),
     "wg_write_tiff": (_I32, [ctypes.c_char_p, ctypes.c_char_p, _V, _I32, _I32]),
     "wg_write_ppm": (_I32, [ctypes.c_char_p, _V, _I32, _I32]),
     "wg_scene_set_probes": (_I32, [_V, _I32, _V, _V, _I32]),
@@ -370,6 +371,15 @@ class Scene:
         c = np.zeros((0, 3)) if circles is None else np.ascontiguousarray(np.asarray(circles, np.float64)[:, :3])
         check(lib().wg_scene_build_domain(self.h, int(domain), float(lam), int(npoly), float(apoly),
                                           c.ctypes.data if len(c) else None, len(c)))
+
+    def neumann_records(self):
+        """The Neumann records built on the device by build_domain (NEUMANN_DTYPE array)."""
+        n = _I32()
+        check(lib().wg_scene_neumann_records(self.h, None, 0, ctypes.byref(n)))
+        out = np.zeros(n.value, dtype=P.NEUMANN_DTYPE)
+        if n.value:
+            check(lib().wg_scene_neumann_records(self.h, out.ctypes.data, n.value, ctypes.byref(n)))
+        return out
 
     def download_mask(self):
         xy = np.zeros(self.params.nx * self.params.ny, np.int16)
