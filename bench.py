@@ -702,22 +702,24 @@ def frame_palette():
 def run_probe(args):
     """Small, fixed cases for kernel captures (ncu): the config-2 scene with a given
     precision and temporal blocking, stepped `--probe-updates` times, a 64-instance
-    batch stepped 4 frames of 10 updates, or 512 parameter-sweep instances (FP32,
-    skewed passes of depth `--probe-block` K) stepped 4 frames of 10 updates."""
+    batch (FP32 or FP64 with batch64, single updates only) stepped 4 frames of 10
+    updates, or 512 parameter-sweep instances (FP32, skewed passes of depth
+    `--probe-block` K) stepped 4 frames of 10 updates."""
     import numpy as np
     _package()
     from youtube_simulations_gb300 import params as P
     from youtube_simulations_gb300 import scenes
     from youtube_simulations_gb300 import wavegpu as W
-    if args.probe == "batch":
+    if args.probe in ("batch", "batch64"):
         rng = np.random.default_rng(1000)
-        b = W.Batch(P.FP32)
+        b = W.Batch(P.FP32 if args.probe == "batch" else P.FP64)
+        b.set_skew(0)  # single updates only: the persistent k_batch_step
         for _ in range(64):
             m = scenes.batch_member(rng)
             b.add(m.params, m.phi, m.psi, m.xy)
         for _ in range(4):
             b.step(10)
-        print(json.dumps({"probe": "batch", "instances": b.count()[0], "energy0": b.energy(0)}))
+        print(json.dumps({"probe": args.probe, "instances": b.count()[0], "energy0": b.energy(0)}))
         b.close()
         return 0
     if args.probe == "sweep":
@@ -757,7 +759,8 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--ref-updates", type=int, default=20, help="updates per reference step")
     ap.add_argument("--e2e-steps", type=int, default=20)
-    ap.add_argument("--probe", choices=["fp32", "fp64", "batch", "sweep"], help="run a small fixed case for kernel captures")
+    ap.add_argument("--probe", choices=["fp32", "fp64", "batch", "batch64", "sweep"],
+                    help="run a small fixed case for kernel captures")
     ap.add_argument("--probe-block", type=int, nargs=3, default=[3, 16, 256], metavar=("K", "L", "W"))
     ap.add_argument("--probe-updates", type=int, default=24)
     ap.add_argument("--no-batch", action="store_true")
