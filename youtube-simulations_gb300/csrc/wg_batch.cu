@@ -70,13 +70,31 @@ struct TileCoef {
 // Z (FP64 scenes): upd64's flags for KAPPA = 0 and GAMMA = GAMMAB = 0, the bulk update
 // without those zero terms (values unchanged).
 template <class T, int Z = 0>
-__device__ __forceinline__ void batch_tile(const DevParams &p, const T *__restrict__ phi, T *__restrict__ out,
-                                           const uint32_t *__restrict__ act, const uint32_t *__restrict__ nz,
-                                           int i0, int jt, long long time)
+__device__ __forceinline__ void batch_tile(const DevParams &p, const float *cf, const T *__restrict__ phi,
+                                           T *__restrict__ out, const uint32_t *__restrict__ act,
+                                           const uint32_t *__restrict__ nz, int i0, int jt, long long time)
 {
     constexpr int V = Vec<T>::n;
-    const TileCoef<T> k{p.nx, p.ny, p.pitch, p.wpitch, p.twospeeds, p.floor_clamp,
-                        (T)p.c2, (T)p.c2b, (T)p.gam, (T)p.gamb, (T)p.kappa};
+    TileCoef<T> k;
+    k.nx = p.nx;
+    k.ny = p.ny;
+    k.pitch = p.pitch;
+    k.wpitch = p.wpitch;
+    k.twospeeds = p.twospeeds;
+    k.floor_clamp = p.floor_clamp;
+    if constexpr (sizeof(T) == 4) {
+        k.c2 = cf[CF_C2];
+        k.c2b = cf[CF_C2B];
+        k.gam = cf[CF_GAM];
+        k.gamb = cf[CF_GAMB];
+        k.kappa = cf[CF_KAPPA];
+    } else {
+        k.c2 = p.c2;
+        k.c2b = p.c2b;
+        k.gam = p.gam;
+        k.gamb = p.gamb;
+        k.kappa = p.kappa;
+    }
     const int j0 = (jt * BT_THREADS + (int)threadIdx.x) * V;
     // interior rows: the bulk rule (boundary columns and padding keep psi for now)
     for (int rr = threadIdx.y; rr < BT_ROWS; rr += blockDim.y) {
@@ -169,11 +187,11 @@ __global__ void __launch_bounds__(256, 4) k_batch_step(const BatchHdr *__restric
         if constexpr (sizeof(T) == 8)
             z = (sd.p.kappa == 0.0 ? Z_KAPPA : 0) | (sd.p.gam == 0.0 && sd.p.gamb == 0.0 ? Z_GAMMA : 0);
         if (z == (Z_KAPPA | Z_GAMMA))
-            batch_tile<T, Z_KAPPA | Z_GAMMA>(sd.p, in, out, sd.act, sd.nz, w.y, w.z, d.time + u + 1);
+            batch_tile<T, Z_KAPPA | Z_GAMMA>(sd.p, sd.cf, in, out, sd.act, sd.nz, w.y, w.z, d.time + u + 1);
         else if (z == Z_KAPPA)
-            batch_tile<T, Z_KAPPA>(sd.p, in, out, sd.act, sd.nz, w.y, w.z, d.time + u + 1);
+            batch_tile<T, Z_KAPPA>(sd.p, sd.cf, in, out, sd.act, sd.nz, w.y, w.z, d.time + u + 1);
         else
-            batch_tile<T>(sd.p, in, out, sd.act, sd.nz, w.y, w.z, d.time + u + 1);
+            batch_tile<T>(sd.p, sd.cf, in, out, sd.act, sd.nz, w.y, w.z, d.time + u + 1);
         if (tid == 0) s_next[buf ^ 1] = next;
         __syncthreads();  // the next ticket is visible; s_next[buf] is free again
     }
@@ -382,6 +400,12 @@ wg_status batch_refresh_table(wg_batch *b)
             d.act = h.act;
             d.nz = h.nz;
             d.slot = k;
+            {
+                const double c[12] = {h.dp.c2, h.dp.c2b, h.dp.gam, h.dp.gamb, h.dp.kappa, h.dp.kappa_sides,
+                                      h.dp.kappa_topbot, h.dp.gamma_sides, h.dp.gamma_topbot, h.dp.vmax,
+                                      h.dp.courant, h.dp.courantb};
+                for (int q = 0; q < 12; q++) d.cf[q] = (float)c[q];
+            }
             d.skew_k = sk;
             d.wrap = h.wrap ? 1 : 0;
             d.tiles_j = (h.dp.pitch / V + BT_THREADS - 1) / BT_THREADS;

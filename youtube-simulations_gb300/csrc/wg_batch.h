@@ -19,7 +19,12 @@ struct __align__(16) SlotDev {   // one entry of the compact table of active sce
     int skew_k;                  // depth class of the scene's skewed passes; 0: single updates only
     int wrap;                    // periodic scene in the ghost layout (skewed passes read wrapped halos)
     int pad_[2];
+    // the coefficients rounded to FP32 once on the host (a conversion from FP64 costs the
+    // FP64 pipe on the device): c2, c2b, gam, gamb, kappa, kappa_sides, kappa_topbot,
+    // gamma_sides, gamma_topbot, vmax, courant, courantb
+    float cf[12];
 };
+enum { CF_C2, CF_C2B, CF_GAM, CF_GAMB, CF_KAPPA, CF_KS, CF_KT, CF_GS, CF_GT, CF_VMAX, CF_COURANT, CF_COURANTB };
 struct SlotDyn {
     long long time;
     int cur;                     // phi = f[2 pair + cur], psi = f[2 pair + 1 - cur]

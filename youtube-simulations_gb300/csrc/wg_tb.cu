@@ -861,18 +861,18 @@ __global__ void __launch_bounds__(128, 4) k_batch_skew(const SlotDev *__restrict
         a.psi_out = (float *)sd.f[2 * pout + 1];
         a.act = sd.act;
         a.tcc = a.tc = nullptr;
-        a.c2 = (float)sd.p.c2;
-        a.c2b = (float)sd.p.c2b;
-        a.gam = (float)sd.p.gam;
-        a.gamb = (float)sd.p.gamb;
-        a.kappa = (float)sd.p.kappa;
-        a.ks = (float)sd.p.kappa_sides;
-        a.kt = (float)sd.p.kappa_topbot;
-        a.gs = (float)sd.p.gamma_sides;
-        a.gt = (float)sd.p.gamma_topbot;
-        a.vmax = (float)sd.p.vmax;
-        a.courant = (float)sd.p.courant;
-        a.courantb = (float)sd.p.courantb;
+        a.c2 = sd.cf[CF_C2];
+        a.c2b = sd.cf[CF_C2B];
+        a.gam = sd.cf[CF_GAM];
+        a.gamb = sd.cf[CF_GAMB];
+        a.kappa = sd.cf[CF_KAPPA];
+        a.ks = sd.cf[CF_KS];
+        a.kt = sd.cf[CF_KT];
+        a.gs = sd.cf[CF_GS];
+        a.gt = sd.cf[CF_GT];
+        a.vmax = sd.cf[CF_VMAX];
+        a.courant = sd.cf[CF_COURANT];
+        a.courantb = sd.cf[CF_COURANTB];
         a.t0 = dy.time + toff;
         a.osc = nullptr;
         a.src = nullptr;
