@@ -23,6 +23,7 @@
 #include <cstring>
 #include <map>
 #include <mutex>
+#include <tuple>
 #include <vector>
 #include "wg_internal.h"
 #include "wg_scene.h"
@@ -36,8 +37,8 @@ namespace wg {
 // rule's argument block is built here, in registers of this call, not passed by address
 // (an address taken across the call would put the block in local memory).
 template <class T>
-__device__ __noinline__ T batch_edge(const DevParams &p, const T *phi, T *out, const uint32_t *act, const uint32_t *nz,
-                                     int i, int j, long long time, T y)
+__device__ __noinline__ T batch_edge(const DevParams &p, const float *cf, const T *phi, T *out, const uint32_t *act,
+                                     const uint32_t *nz, int i, int j, long long time, T y)
 {
     FastArgs<T> a;
     a.phi = phi;
@@ -46,11 +47,18 @@ __device__ __noinline__ T batch_edge(const DevParams &p, const T *phi, T *out, c
     a.act = act;
     a.nz = nz;
     a.tcc = a.tc = a.tg = nullptr;
-    a.c2f = (float)p.c2;
-    a.c2bf = (float)p.c2b;
-    a.gamf = (float)p.gam;
-    a.gambf = (float)p.gamb;
-    a.kappaf = (float)p.kappa;
+    a.c2f = cf[CF_C2];  // rounded on the host (a conversion here would run on the FP64 pipe)
+    a.c2bf = cf[CF_C2B];
+    a.gamf = cf[CF_GAM];
+    a.gambf = cf[CF_GAMB];
+    a.kappaf = cf[CF_KAPPA];
+    a.courantf = cf[CF_COURANT];
+    a.courantbf = cf[CF_COURANTB];
+    a.ksf = cf[CF_KS];
+    a.ktf = cf[CF_KT];
+    a.gsf = cf[CF_GS];
+    a.gtf = cf[CF_GT];
+    a.vmaxf = cf[CF_VMAX];
     a.has_ghosts = 0;
     a.do_source = 1;
     T v = fast_edge<T, WG_COEF_MASK>(p, a, i, j, time, y);
@@ -147,12 +155,12 @@ __device__ __forceinline__ void batch_tile(const DevParams &p, const float *cf, 
             for (int q = 0; q < V; q++) {
                 const int j = j0 + q;
                 if (j >= k.ny) break;
-                out[row + j] = batch_edge<T>(p, phi, out, act, nz, i, j, time, out[row + j]);
+                out[row + j] = batch_edge<T>(p, cf, phi, out, act, nz, i, j, time, out[row + j]);
             }
             continue;
         }
-        if (col0) out[row] = batch_edge<T>(p, phi, out, act, nz, i, 0, time, out[row]);
-        if (colr) out[row + k.ny - 1] = batch_edge<T>(p, phi, out, act, nz, i, k.ny - 1, time, out[row + k.ny - 1]);
+        if (col0) out[row] = batch_edge<T>(p, cf, phi, out, act, nz, i, 0, time, out[row]);
+        if (colr) out[row + k.ny - 1] = batch_edge<T>(p, cf, phi, out, act, nz, i, k.ny - 1, time, out[row + k.ny - 1]);
         if (srcj && i == p.src_i) out[row + p.src_j] = (T)A_((double)out[row + p.src_j], point_source(p, time));
     }
 }
@@ -573,15 +581,33 @@ static void batch_enqueue_frame(wg_batch *b, int n, bool skewed)
 // the other pair, so the state does not change), best of five after one untimed pass;
 // the fastest per update is kept.  Nine candidates per class keep the tuning frame of a
 // server tick short.
-// Tuned classes are kept for the process (per device): a later batch or server whose
-// scenes fall in a class tuned before takes that depth and chunk without timing them
-// again, so a serving tick pays the tuning of a size class at most once per process.
+// Tuned classes are kept for the process, keyed by device, size class and the kinds of
+// scene in the class (their boundary conditions, the ghost layout, two speeds): a later
+// batch or server whose class holds the same kinds takes that depth and chunk without
+// timing them again, so a serving tick pays the tuning of a size class at most once per
+// process.  (Keyed by size class alone, the sweep's absorbing scenes took the depth tuned
+// for the uneven batch's mirror and periodic ones: 309 against 351 Gcell/s.)
 struct TuneCacheEntry {
     int k = 0, rows = 0;
     double ms[8] = {0, 0, 0, 0, 0, 0, 0, 0};
 };
 static std::mutex g_tune_mu;
-static std::map<std::pair<int, int>, TuneCacheEntry> g_tune_cache;  // (device, class)
+static std::map<std::tuple<int, int, unsigned>, TuneCacheEntry> g_tune_cache;  // (device, class, kinds)
+
+static unsigned class_kinds(const wg_batch *b, int c)
+{
+    unsigned sig = 0;
+    for (size_t e = 0; e < b->tab_slot.size(); e++) {
+        const BatchSlotHost &h = b->slots[b->tab_slot[e]];
+        if (!(h.skew && h.cls == c)) continue;
+        sig |= 1u << (h.prm.b_cond & 7);
+        if (h.wrap) sig |= 1u << 8;
+        if (h.prm.twospeeds) sig |= 1u << 9;
+        if (h.prm.oscillate_left || h.prm.oscillate_topbot) sig |= 1u << 10;
+        if (h.prm.src_on) sig |= 1u << 11;
+    }
+    return sig;
+}
 
 static wg_status batch_autotune(wg_batch *b)
 {
@@ -592,14 +618,10 @@ static wg_status batch_autotune(wg_batch *b)
         if (b->class_k[c]) continue;
         {
             std::lock_guard<std::mutex> lk(g_tune_mu);
-            auto it = g_tune_cache.find(std::make_pair(devno, c));
+            const unsigned kinds = class_kinds(b, c);
+            if (!kinds) continue;  // no scene of this class takes skewed passes
+            auto it = g_tune_cache.find(std::make_tuple(devno, c, kinds));
             if (it != g_tune_cache.end()) {
-                bool present = false;
-                for (size_t e = 0; e < b->tab_slot.size() && !present; e++) {
-                    const BatchSlotHost &h = b->slots[b->tab_slot[e]];
-                    present = h.skew && h.cls == c;
-                }
-                if (!present) continue;
                 if (b->tune_ms.empty()) b->tune_ms.assign(BATCH_CLASSES * 8, 0.0);
                 b->class_k[c] = it->second.k;
                 b->class_rows[c] = it->second.rows;
@@ -673,7 +695,7 @@ static wg_status batch_autotune(wg_batch *b)
         b->class_rows[c] = best_rows;
         {
             std::lock_guard<std::mutex> lk(g_tune_mu);
-            TuneCacheEntry &ce = g_tune_cache[std::make_pair(devno, c)];
+            TuneCacheEntry &ce = g_tune_cache[std::make_tuple(devno, c, class_kinds(b, c))];
             ce.k = best;
             ce.rows = best_rows;
             for (int K = 0; K < 8; K++) ce.ms[K] = b->tune_ms[c * 8 + K];

@@ -90,11 +90,10 @@ __device__ inline float fast_edge32(const DevParams &p, const FastArgs<float> &a
         g = a.tg ? a.tg[o] : a.gamf;
     } else {
         ccv = act ? a.c2f : a.c2bf;
-        tcv = act ? (float)p.courant : (float)p.courantb;
+        tcv = act ? a.courantf : a.courantbf;
         g = act ? a.gamf : a.gambf;
     }
-    const Edge32K k{a.kappaf, (float)p.kappa_sides, (float)p.kappa_topbot, (float)p.gamma_sides,
-                    (float)p.gamma_topbot, (float)p.vmax};
+    const Edge32K k{a.kappaf, a.ksf, a.ktf, a.gsf, a.gtf, a.vmaxf};
     float v = edge32<false>(p, i, j, x, y, n, sv, e, w, ccv, tcv, g, act, k,
                             [&] { return (float)osc_bc(p, (int)time, j); });
     if (p.floor_clamp && ActBits{a.nz, p.wpitch}(i, j)) v = (float)floor_clamp(p, (double)v);

@@ -16,6 +16,9 @@ struct FastArgs {
     const uint32_t *nz;  // "nonzero" plane: xy != 0
     const T *tcc, *tc, *tg;  // WG_COEF_TABLE tables (tg may be null: uniform)
     float c2f, c2bf, gamf, gambf, kappaf;
+    // the boundary rules' coefficients in FP32, rounded on the host (a conversion from
+    // FP64 on the device runs on this GPU's slow FP64 pipe)
+    float courantf, courantbf, ksf, ktf, gsf, gtf, vmaxf;
     int has_ghosts;      // the mask has cells < 0 (Neumann ghosts)
     int do_source;       // add the point source in this kernel
 };

@@ -83,6 +83,13 @@ static FastArgs<T> fast_args(wg_scene *s, int do_source)
     a.gamf = (float)s->dp.gam;
     a.gambf = (float)s->dp.gamb;
     a.kappaf = (float)s->dp.kappa;
+    a.courantf = (float)s->dp.courant;
+    a.courantbf = (float)s->dp.courantb;
+    a.ksf = (float)s->dp.kappa_sides;
+    a.ktf = (float)s->dp.kappa_topbot;
+    a.gsf = (float)s->dp.gamma_sides;
+    a.gtf = (float)s->dp.gamma_topbot;
+    a.vmaxf = (float)s->dp.vmax;
     a.has_ghosts = s->has_ghosts;
     a.do_source = do_source;
     return a;
