@@ -4,7 +4,7 @@
 Workload (one GPU): 3840x2160 grid, 64 seeded discs of refractive index 1.5
 (TWOSPEEDS, COURANTB = COURANT/1.5) through the tcc table, absorbing boundary,
 GAMMA = 1e-4, an oscillating point source of amplitude 0.05 and seeded period in
-[20, 60] updates, energy reported every 100 updates with FP64 compensated sums.
+[20, 60] updates, energy reported every 100 updates (compensated sums merged in FP64).
 One bench step = 100 leapfrog updates + one energy report; 100 steps = the full 10^4
 updates.  `value` is the FP32 form in Gcell-updates/s (all cells count), with inputs
 resident in HBM; `e2e` is the same metric through the C ABI with host buffers (the

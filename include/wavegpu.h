@@ -235,7 +235,10 @@ wg_status wg_scene_step(wg_scene *s, int32_t nsteps);
 /* Copies phi (time t) and psi (time t-1) to flat host arrays in FP64 or the scene's
  * precision.  Either pointer may be NULL. */
 wg_status wg_scene_download(wg_scene *s, void *phi, void *psi, int32_t host_precision);
-/* Energy diagnostics with FP64 compensated (Neumaier) sums.
+/* Energy diagnostics (compute_energy per cell, wave_common.c:453-472) with compensated
+ * sums: FP64 Neumaier accumulators for FP64 fields; for FP32 fields (cell energies in
+ * FP32) an error-free FP32 double-word accumulator converted exactly to FP64 per column;
+ * columns, boxes and the total merged in FP64 Neumaier sums.
  *  total   : sum of compute_energy over all cells (may be NULL)
  *  columns : nx values, sum over j < ny/2 (compute_energy_x), may be NULL
  *  boxes   : 6 values (compute_energy_tblr) for ileft/iright, may be NULL */
