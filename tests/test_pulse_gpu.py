@@ -43,8 +43,11 @@ def test_scene_add_circular_wave(variant, factor, x, y, prec):
         assert outside.any()
         assert np.array_equal(got_phi[outside], phi[outside])
     else:
+        # FP32 scenes hold phi and the velocity phi - psi, which takes the same increment:
+        # psi = phi - v comes back within FP32 roundings of the values involved
         assert np.max(np.abs(got_phi - ref)) <= 4 * np.finfo(np.float32).eps * np.max(np.abs(ref))
-        assert np.array_equal(got_psi, psi.astype(np.float32).astype(np.float64))
+        scale = max(np.max(np.abs(ref)), np.max(np.abs(psi)))
+        assert np.max(np.abs(got_psi - psi)) <= 8 * np.finfo(np.float32).eps * scale
 
 
 def test_scene_add_circular_wave_rejects_bad_variance():

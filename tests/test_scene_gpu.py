@@ -109,6 +109,9 @@ def test_scene_energy_matches_oracle(prec):
 
 
 def test_state_roundtrip_and_time():
+    """An FP32 scene stores phi and the velocity v = phi - psi (each rounded once from the
+    FP64 difference); psi comes back as phi - v, within an FP32 rounding of |v| of the
+    uploaded psi, and phi exactly."""
     p, f, xy, _ = variant_inputs("s_per", seed=9)
     with W.Scene(p, P.FP32, P.COEF_MASK) as s:
         s.upload(f["phi"], f["psi"], xy)
@@ -116,7 +119,13 @@ def test_state_roundtrip_and_time():
         b = np.random.default_rng(1).standard_normal(p.nx * p.ny).astype(np.float32)
         s.upload_state(a, b)
         x, y = s.download(native=True)
-        assert np.array_equal(x, a) and np.array_equal(y, b)
+        v = (a.astype(np.float64) - b.astype(np.float64)).astype(np.float32)
+        assert np.array_equal(x, a)
+        assert np.array_equal(y, (a.astype(np.float64) - v.astype(np.float64)).astype(np.float32))
+        assert np.max(np.abs(y.astype(np.float64) - b)) <= 2 * np.finfo(np.float32).eps * np.max(np.abs(v))
+        x64, y64 = s.download()
+        assert np.array_equal(x64, a.astype(np.float64))
+        assert np.array_equal(y64, a.astype(np.float64) - v.astype(np.float64))
         s.time = 100
         s.step(3)
         assert s.time == 103

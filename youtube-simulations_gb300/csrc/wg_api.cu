@@ -312,7 +312,7 @@ static wg_status di_one_update(int in, int prev, int out)
                       g_di.time, recs ? 0 : 1, g_di.st);
     if (recs) {
         launch_neumann_exact(g_di.dp, g_di.buf[in], g_di.buf[out], g_di.xy, g_di.rec, g_di.nrec, g_di.st);
-        if (g_di.prm.src_on) launch_point_source<double>(g_di.dp, g_di.buf[out], g_di.time, g_di.st);
+        if (g_di.prm.src_on) launch_point_source<double>(g_di.dp, g_di.buf[out], nullptr, g_di.time, g_di.st);
     }
     WG_CUDA(cudaGetLastError());
     return WG_OK;
@@ -432,7 +432,7 @@ wg_status wg_dropin_add_circular_wave(double init_amp, double factor, double x, 
     const int k = di_slot(phi, 0, &fresh);
     if (k < 0) { set_error("too many field arrays"); return WG_ERR_STATE; }
     if (fresh && (s = di_upload_rows<double>(phi, g_di.buf[k]))) return s;
-    launch_add_circular_wave<double>(pa, g_di.buf[k], g_di.xy, nullptr, g_di.st);
+    launch_add_circular_wave<double>(pa, g_di.buf[k], nullptr, g_di.xy, nullptr, g_di.st);
     WG_CUDA(cudaGetLastError());
     if (g_di.mode == WG_DROPIN_STRICT) return di_download_rows(g_di.buf[k], phi);
     return WG_OK;

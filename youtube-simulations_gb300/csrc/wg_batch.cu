@@ -9,7 +9,9 @@
 // admitting or removing scenes changes data, not the graph.
 //
 // The per-cell arithmetic is the single-scene kernels' (k_step_bulk / fast_edge), so a
-// scene advanced in a batch is bit-identical to the same scene advanced alone.
+// scene advanced in a batch is bit-identical to the same scene advanced alone.  FP64
+// scenes update in place (the new level overwrites psi); FP32 scenes (phi and the
+// velocity) write each update into their other pair of fields.
 //
 // FP32 scenes with mirror ("Dirichlet"), absorbing or periodic boundaries (periodic ones
 // in the ghost layout of wg_batch.h) take skewed passes instead (k_batch_skew, wg_tb.cu):
@@ -36,14 +38,17 @@ namespace wg {
 // the tile loop below stays small.  Its arguments are plain pointers and values: the
 // rule's argument block is built here, in registers of this call, not passed by address
 // (an address taken across the call would put the block in local memory).
+// FP64 fields: phi and psi (y = the cell's psi); returns the new value.
+// FP32 fields: phi and the velocity vel; returns the new phi and velocity.
 template <class T>
-__device__ __noinline__ T batch_edge(const DevParams &p, const float *cf, const T *phi, T *out, const uint32_t *act,
-                                     const uint32_t *nz, int i, int j, long long time, T y)
+__device__ __forceinline__ FastArgs<T> batch_args(const float *cf, const T *phi, const T *psi, const uint32_t *act,
+                                                  const uint32_t *nz)
 {
     FastArgs<T> a;
     a.phi = phi;
-    a.psi = out;
-    a.out = out;
+    a.psi = psi;
+    a.out = nullptr;
+    a.vout = nullptr;
     a.act = act;
     a.nz = nz;
     a.tcc = a.tc = a.tg = nullptr;
@@ -61,9 +66,24 @@ __device__ __noinline__ T batch_edge(const DevParams &p, const float *cf, const 
     a.vmaxf = cf[CF_VMAX];
     a.has_ghosts = 0;
     a.do_source = 1;
-    T v = fast_edge<T, WG_COEF_MASK>(p, a, i, j, time, y);
-    if (p.src_on && i == p.src_i && j == p.src_j) v = (T)A_((double)v, point_source(p, time));
+    return a;
+}
+__device__ __noinline__ double batch_edge(const DevParams &p, const float *cf, const double *phi, const double *psi,
+                                          const uint32_t *act, const uint32_t *nz, int i, int j, long long time,
+                                          double y)
+{
+    const FastArgs<double> a = batch_args<double>(cf, phi, psi, act, nz);
+    double v = fast_edge<double, WG_COEF_MASK>(p, a, i, j, time, y);
+    if (p.src_on && i == p.src_i && j == p.src_j) v = A_(v, point_source(p, time));
     return v;
+}
+__device__ __noinline__ XV batch_edge_v(const DevParams &p, const float *cf, const float *phi, const float *vel,
+                                        const uint32_t *act, const uint32_t *nz, int i, int j, long long time)
+{
+    const FastArgs<float> a = batch_args<float>(cf, phi, vel, act, nz);
+    XV r = fast_edge_v<WG_COEF_MASK>(p, a, i, j, time);
+    if (p.src_on && i == p.src_i && j == p.src_j) r = source32(r, point_source(p, time));
+    return r;
 }
 
 // The scene values the bulk update reads, held in registers for a work item (the
@@ -75,14 +95,18 @@ struct TileCoef {
     T c2, c2b, gam, gamb, kappa;
 };
 
+// One work item.  FP64 (in place): phi, and psi = out, overwritten by the new level.
+// FP32: phi and the velocity vin; the new phi and velocity go to out and vout.
 // Z (FP64 scenes): upd64's flags for KAPPA = 0 and GAMMA = GAMMAB = 0, the bulk update
 // without those zero terms (values unchanged).
 template <class T, int Z = 0>
 __device__ __forceinline__ void batch_tile(const DevParams &p, const float *cf, const T *__restrict__ phi,
-                                           T *__restrict__ out, const uint32_t *__restrict__ act,
-                                           const uint32_t *__restrict__ nz, int i0, int jt, long long time)
+                                           const T *__restrict__ vin, T *__restrict__ out, T *__restrict__ vout,
+                                           const uint32_t *__restrict__ act, const uint32_t *__restrict__ nz, int i0,
+                                           int jt, long long time)
 {
     constexpr int V = Vec<T>::n;
+    constexpr bool F32 = sizeof(T) == 4;
     TileCoef<T> k;
     k.nx = p.nx;
     k.ny = p.ny;
@@ -90,7 +114,7 @@ __device__ __forceinline__ void batch_tile(const DevParams &p, const float *cf, 
     k.wpitch = p.wpitch;
     k.twospeeds = p.twospeeds;
     k.floor_clamp = p.floor_clamp;
-    if constexpr (sizeof(T) == 4) {
+    if constexpr (F32) {
         k.c2 = cf[CF_C2];
         k.c2b = cf[CF_C2B];
         k.gam = cf[CF_GAM];
@@ -103,50 +127,66 @@ __device__ __forceinline__ void batch_tile(const DevParams &p, const float *cf, 
         k.gamb = p.gamb;
         k.kappa = p.kappa;
     }
+    const float vmaxf = cf[CF_VMAX];
     const int j0 = (jt * BT_THREADS + (int)threadIdx.x) * V;
-    // interior rows: the bulk rule (boundary columns and padding keep psi for now)
+    // interior rows: the bulk rule (boundary columns and padding take the unwritten-cell
+    // rule for now)
     for (int rr = threadIdx.y; rr < BT_ROWS; rr += blockDim.y) {
         const int i = i0 + rr;
         if (i >= k.nx - 1 || i == 0 || j0 >= k.pitch) continue;
         const size_t row = (size_t)i * k.pitch;
         T c[V], y[V], n[V], s[V];
         vload(phi + row + j0, c);
-        vload(out + row + j0, y);
+        vload(vin + row + j0, y);
         vload(phi + row + k.pitch + j0, n);
         vload(phi + row - k.pitch + j0, s);
         const T wl = (j0 > 0) ? phi[row + j0 - 1] : (T)0;
         const T er = (j0 + V < k.pitch) ? phi[row + j0 + V] : (T)0;
         const uint32_t word = act[(size_t)i * k.wpitch + (j0 >> 5)] >> (j0 & 31);
-        T o[V];
+        T o[V], ov[V];
 #pragma unroll
         for (int q = 0; q < V; q++) {
             const int j = j0 + q;
-            T v = y[q];
             const bool ac = (word >> q) & 1u;
-            if (j >= 1 && j < k.ny - 1 && (k.twospeeds || ac)) {
-                const T x = c[q];
-                const T w = (q == 0) ? wl : c[q - 1];
-                const T e = (q == V - 1) ? er : c[q + 1];
-                if (sizeof(T) == 8) {
-                    const double delta = L4_(A_(A_(A_((double)n[q], (double)s[q]), (double)e), (double)w), (double)x);
-                    v = (T)upd64<Z>((double)x, (double)y[q], ac ? (double)k.c2 : (double)k.c2b, delta, (double)k.kappa,
-                                    ac ? (double)k.gam : (double)k.gamb);
-                } else {
-                    const float xf = (float)x;
-                    const float delta = (((float)n[q] - xf) + ((float)s[q] - xf)) + (((float)e - xf) + ((float)w - xf));
-                    v = (T)upd32(xf, (float)y[q], ac ? (float)k.c2 : (float)k.c2b, delta, (float)k.kappa,
-                                 ac ? (float)k.gam : (float)k.gamb);
+            const bool upd = j >= 1 && j < k.ny - 1 && (k.twospeeds || ac);
+            const T x = c[q];
+            const T w = (q == 0) ? wl : c[q - 1];
+            const T e = (q == V - 1) ? er : c[q + 1];
+            if constexpr (!F32) {
+                double v = y[q];
+                if (upd) {
+                    const double delta = L4_(A_(A_(A_(n[q], s[q]), e), w), x);
+                    v = upd64<Z>(x, y[q], ac ? k.c2 : k.c2b, delta, k.kappa, ac ? k.gam : k.gamb);
+                    if (k.floor_clamp && ac) v = floor_clamp(p, v);
                 }
-                if (k.floor_clamp && ac) v = (T)floor_clamp(p, (double)v);
+                o[q] = (T)v;
+            } else {
+                XV r = keep32(x, y[q]);
+                if (upd) {
+                    const float delta = ((n[q] - x) + (s[q] - x)) + ((e - x) + (w - x));
+                    r = upd32(x, y[q], ac ? k.c2 : k.c2b, delta, k.kappa, ac ? k.gam : k.gamb);
+                    if (k.floor_clamp && ac) r = clamp32(x, r, vmaxf);
+                }
+                o[q] = r.x;
+                ov[q] = r.v;
             }
-            o[q] = v;
         }
         vstore(out + row + j0, o);
+        if constexpr (F32) vstore(vout + row + j0, ov);
     }
     // then the boundary lines and the point source, by the threads that stored those
-    // cells above (each reads phi and its own cell's psi, which the loop above left)
+    // cells above (each reads phi and its own cell's psi or velocity)
     const bool col0 = j0 == 0, colr = k.ny - 1 >= j0 && k.ny - 1 < j0 + V;
     const bool srcj = p.src_on && p.src_j >= j0 && p.src_j < j0 + V && p.src_j > 0 && p.src_j < k.ny - 1;
+    auto edge = [&](size_t row, int i, int j) {
+        if constexpr (F32) {
+            const XV r = batch_edge_v(p, cf, phi, vin, act, nz, i, j, time);
+            out[row + j] = r.x;
+            vout[row + j] = r.v;
+        } else {
+            out[row + j] = batch_edge(p, cf, phi, out, act, nz, i, j, time, out[row + j]);
+        }
+    };
     for (int rr = threadIdx.y; rr < BT_ROWS; rr += blockDim.y) {
         const int i = i0 + rr;
         if (i >= k.nx || j0 >= k.pitch) continue;
@@ -155,13 +195,17 @@ __device__ __forceinline__ void batch_tile(const DevParams &p, const float *cf, 
             for (int q = 0; q < V; q++) {
                 const int j = j0 + q;
                 if (j >= k.ny) break;
-                out[row + j] = batch_edge<T>(p, cf, phi, out, act, nz, i, j, time, out[row + j]);
+                edge(row, i, j);
             }
             continue;
         }
-        if (col0) out[row] = batch_edge<T>(p, cf, phi, out, act, nz, i, 0, time, out[row]);
-        if (colr) out[row + k.ny - 1] = batch_edge<T>(p, cf, phi, out, act, nz, i, k.ny - 1, time, out[row + k.ny - 1]);
-        if (srcj && i == p.src_i) out[row + p.src_j] = (T)A_((double)out[row + p.src_j], point_source(p, time));
+        if (col0) edge(row, i, 0);
+        if (colr) edge(row, i, k.ny - 1);
+        if (srcj && i == p.src_i) {
+            const double add = point_source(p, time);
+            out[row + p.src_j] = (T)A_((double)out[row + p.src_j], add);
+            if constexpr (F32) vout[row + p.src_j] = (T)A_((double)vout[row + p.src_j], add);
+        }
     }
 }
 
@@ -188,18 +232,30 @@ __global__ void __launch_bounds__(256, 4) k_batch_step(const BatchHdr *__restric
         const int4 w = items[it];
         const SlotDev &sd = tab[w.x];
         const SlotDyn d = dyn[w.w];
-        const int phase = (d.cur + u) & 1, base = 2 * d.pair;
-        const T *in = (const T *)sd.f[base + phase];
-        T *out = (T *)sd.f[base + 1 - phase];
+        const T *in, *vin;
+        T *out, *vout;
+        if constexpr (sizeof(T) == 4) {  // pair (pair ^ u) -> the other pair
+            const int pin = d.pair ^ (u & 1);
+            in = (const T *)sd.f[2 * pin];
+            vin = (const T *)sd.f[2 * pin + 1];
+            out = (T *)sd.f[2 * (pin ^ 1)];
+            vout = (T *)sd.f[2 * (pin ^ 1) + 1];
+        } else {  // in place within pair 0
+            const int phase = (d.cur + u) & 1;
+            in = (const T *)sd.f[phase];
+            out = (T *)sd.f[1 - phase];
+            vin = out;
+            vout = nullptr;
+        }
         int z = 0;  // block-uniform
         if constexpr (sizeof(T) == 8)
             z = (sd.p.kappa == 0.0 ? Z_KAPPA : 0) | (sd.p.gam == 0.0 && sd.p.gamb == 0.0 ? Z_GAMMA : 0);
         if (z == (Z_KAPPA | Z_GAMMA))
-            batch_tile<T, Z_KAPPA | Z_GAMMA>(sd.p, sd.cf, in, out, sd.act, sd.nz, w.y, w.z, d.time + u + 1);
+            batch_tile<T, Z_KAPPA | Z_GAMMA>(sd.p, sd.cf, in, vin, out, vout, sd.act, sd.nz, w.y, w.z, d.time + u + 1);
         else if (z == Z_KAPPA)
-            batch_tile<T, Z_KAPPA>(sd.p, sd.cf, in, out, sd.act, sd.nz, w.y, w.z, d.time + u + 1);
+            batch_tile<T, Z_KAPPA>(sd.p, sd.cf, in, vin, out, vout, sd.act, sd.nz, w.y, w.z, d.time + u + 1);
         else
-            batch_tile<T>(sd.p, sd.cf, in, out, sd.act, sd.nz, w.y, w.z, d.time + u + 1);
+            batch_tile<T>(sd.p, sd.cf, in, vin, out, vout, sd.act, sd.nz, w.y, w.z, d.time + u + 1);
         if (tid == 0) s_next[buf ^ 1] = next;
         __syncthreads();  // the next ticket is visible; s_next[buf] is free again
     }
@@ -269,21 +325,19 @@ __global__ void k_act_ghosts(uint32_t *act, int wpitch, int nx, int ny)
     act[base] = v;
 }
 
-// skewed: the frame ran the skewed passes of the scenes with a depth class
+// skewed: the frame ran the skewed passes of the scenes with a depth class.  pairs: FP32
+// scenes, whose single updates also alternate between the pairs.
 __global__ void k_batch_advance(const BatchHdr *__restrict__ hdr, const SlotDev *__restrict__ tab,
-                                SlotDyn *__restrict__ dyn, int n, int skewed)
+                                SlotDyn *__restrict__ dyn, int n, int skewed, int pairs)
 {
     const int k = blockIdx.x * blockDim.x + threadIdx.x;
     if (k >= hdr->nactive) return;
     SlotDyn &d = dyn[tab[k].slot];
     d.time += n;
     const int P = skewed ? batch_passes(n, tab[k].skew_k) : 0;
-    if (P > 0) {
-        d.pair ^= P & 1;
-        d.cur = 0;
-    } else {
-        d.cur = (d.cur + n) & 1;
-    }
+    if (P > 0) d.pair ^= P & 1;
+    else if (pairs) d.pair ^= n & 1;
+    else d.cur = (d.cur + n) & 1;
 }
 
 }  // namespace wg
@@ -572,7 +626,8 @@ static void batch_enqueue_frame(wg_batch *b, int n, bool skewed)
     }
     for (int K : groups) cudaStreamWaitEvent(b->st, b->ev_join[K], 0);
     const int cap = std::max(b->tab_cap, 1);
-    k_batch_advance<<<(cap + 255) / 256, 256, 0, b->st>>>(b->d_hdr, b->d_tab, b->d_dyn, n, skewed ? 1 : 0);
+    k_batch_advance<<<(cap + 255) / 256, 256, 0, b->st>>>(b->d_hdr, b->d_tab, b->d_dyn, n, skewed ? 1 : 0,
+                                                          sizeof(T) == 4 ? 1 : 0);
 }
 
 // Depth and row chunk per size class, in two stages: depths 2..6 with the list-wide
@@ -798,7 +853,7 @@ wg_status wg_batch_add(wg_batch *b, const wg_params *p, const double *phi, const
     }
     const size_t fb = L.field_bytes, mb = L.mask_bytes;
     cudaError_t e = cudaSuccess;
-    const int nf = h.skew ? 4 : 2;  // the second pair takes the skewed passes' output
+    const int nf = b->prec == WG_FP32 ? 4 : 2;  // FP32: the second pair takes every update's output
     for (int q = 0; q < nf && e == cudaSuccess; q++) e = cudaMallocAsync(&h.mem[q], fb, b->st);
     for (int q = (h.wrap ? 0 : 2); q < nf && e == cudaSuccess; q++) e = cudaMemsetAsync(h.mem[q], 0, fb, b->st);
     if (e == cudaSuccess) e = cudaMallocAsync((void **)&h.act_mem, mb, b->st);
@@ -811,7 +866,7 @@ wg_status wg_batch_add(wg_batch *b, const wg_params *p, const double *phi, const
     if (e == cudaSuccess) e = cudaMallocAsync((void **)&h.etop, p->nx * sizeof(double2), b->st);
     if (e == cudaSuccess) e = cudaMallocAsync((void **)&h.eout, (p->nx + 8) * sizeof(double), b->st);
     void *stage = nullptr;
-    if (e == cudaSuccess) e = cudaMallocAsync(&stage, n * sizeof(double), b->st);
+    if (e == cudaSuccess) e = cudaMallocAsync(&stage, 2 * n * sizeof(double), b->st);
     if (e != cudaSuccess) {
         void *ptrs[] = {h.mem[0], h.mem[1], h.mem[2], h.mem[3], h.act_mem, h.nz_mem, h.ebot, h.etop, h.eout, stage};
         for (void *q : ptrs) if (q) cudaFreeAsync(q, b->st);
@@ -827,11 +882,14 @@ wg_status wg_batch_add(wg_batch *b, const wg_params *p, const double *phi, const
         k_act_ghosts<<<dim3((words + 63) / 64, rows), 64, 0, b->st>>>(h.act, h.dp.wpitch, p->nx, p->ny);
         b->launches++;
     }
-    const double *src[2] = {phi, psi};
-    for (int q = 0; q < 2; q++) {
-        WG_CUDA(cudaMemcpyAsync(stage, src[q], n * sizeof(double), cudaMemcpyHostToDevice, b->st));
-        if (b->prec == WG_FP32) launch_convert_in<float>(p->nx, p->ny, pitch, (const double *)stage, (float *)h.f[q], b->st);
-        else launch_convert_in<double>(p->nx, p->ny, pitch, (const double *)stage, (double *)h.f[q], b->st);
+    double *dstage = (double *)stage;
+    WG_CUDA(cudaMemcpyAsync(dstage, phi, n * sizeof(double), cudaMemcpyHostToDevice, b->st));
+    WG_CUDA(cudaMemcpyAsync(dstage + n, psi, n * sizeof(double), cudaMemcpyHostToDevice, b->st));
+    if (b->prec == WG_FP32) {  // phi and the velocity phi - psi
+        launch_state_in32<double>(p->nx, p->ny, pitch, dstage, dstage + n, (float *)h.f[0], (float *)h.f[1], b->st);
+    } else {
+        launch_convert_in<double>(p->nx, p->ny, pitch, dstage, (double *)h.f[0], b->st);
+        launch_convert_in<double>(p->nx, p->ny, pitch, dstage + n, (double *)h.f[1], b->st);
     }
     WG_CUDA(cudaFreeAsync(stage, b->st));
     WG_CUDA(cudaGetLastError());
@@ -943,15 +1001,17 @@ wg_status wg_batch_download(wg_batch *b, int32_t slot, double *phi, double *psi)
     WG_CUDA(cudaStreamSynchronize(b->st));
     const size_t n = (size_t)h.prm.nx * h.prm.ny;
     double *stage = nullptr;
-    WG_CUDA(cudaMallocAsync((void **)&stage, n * sizeof(double), b->st));
-    double *dst[2] = {phi, psi};
-    for (int q = 0; q < 2; q++) {
-        if (!dst[q]) continue;
-        const void *src = h.f[2 * d.pair + (q == 0 ? d.cur : 1 - d.cur)];
-        if (b->prec == WG_FP32) launch_convert_out<float>(h.prm.nx, h.prm.ny, h.dp.pitch, (const float *)src, stage, b->st);
-        else launch_convert_out<double>(h.prm.nx, h.prm.ny, h.dp.pitch, (const double *)src, stage, b->st);
-        WG_CUDA(cudaMemcpyAsync(dst[q], stage, n * sizeof(double), cudaMemcpyDeviceToHost, b->st));
+    WG_CUDA(cudaMallocAsync((void **)&stage, 2 * n * sizeof(double), b->st));
+    if (b->prec == WG_FP32) {  // phi, and psi = phi - v
+        launch_state_out32<double>(h.prm.nx, h.prm.ny, h.dp.pitch, (const float *)h.f[2 * d.pair],
+                                   (const float *)h.f[2 * d.pair + 1], phi ? stage : nullptr, psi ? stage + n : nullptr,
+                                   b->st);
+    } else {
+        if (phi) launch_convert_out<double>(h.prm.nx, h.prm.ny, h.dp.pitch, (const double *)h.f[d.cur], stage, b->st);
+        if (psi) launch_convert_out<double>(h.prm.nx, h.prm.ny, h.dp.pitch, (const double *)h.f[1 - d.cur], stage + n, b->st);
     }
+    if (phi) WG_CUDA(cudaMemcpyAsync(phi, stage, n * sizeof(double), cudaMemcpyDeviceToHost, b->st));
+    if (psi) WG_CUDA(cudaMemcpyAsync(psi, stage + n, n * sizeof(double), cudaMemcpyDeviceToHost, b->st));
     WG_CUDA(cudaFreeAsync(stage, b->st));
     WG_CUDA(cudaStreamSynchronize(b->st));
     return WG_OK;
@@ -967,6 +1027,7 @@ wg_status wg_batch_energy(wg_batch *b, int32_t slot, double *total)
     SlotDyn d;
     WG_CUDA(cudaMemcpyAsync(&d, b->d_dyn + slot, sizeof d, cudaMemcpyDeviceToHost, b->st));
     WG_CUDA(cudaStreamSynchronize(b->st));
+    // FP32: phi and the velocity of the current pair; FP64: phi and psi of pair 0
     const void *phi = h.f[2 * d.pair + d.cur], *psi = h.f[2 * d.pair + 1 - d.cur];
     if (b->prec == WG_FP32)
         launch_energy<float>(h.dp, (const float *)phi, (const float *)psi, nullptr, h.nz, h.ebot, h.etop, 0, 0, h.eout, b->st);

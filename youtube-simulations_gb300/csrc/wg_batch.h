@@ -12,7 +12,7 @@ constexpr int BT_THREADS = 64;   // threads along j per tile row (x V cells)
 
 struct __align__(16) SlotDev {   // one entry of the compact table of active scenes
     DevParams p;
-    void *f[4];                  // pair 0: f[0], f[1]; pair 1 (skewed scenes): f[2], f[3]
+    void *f[4];                  // pair 0: f[0], f[1]; pair 1 (FP32 scenes): f[2], f[3]
     uint32_t *act, *nz;
     int slot;                    // index into the per-slot dynamic state
     int tiles_j, tile_base, ntiles;
@@ -27,8 +27,8 @@ struct __align__(16) SlotDev {   // one entry of the compact table of active sce
 enum { CF_C2, CF_C2B, CF_GAM, CF_GAMB, CF_KAPPA, CF_KS, CF_KT, CF_GS, CF_GT, CF_VMAX, CF_COURANT, CF_COURANTB };
 struct SlotDyn {
     long long time;
-    int cur;                     // phi = f[2 pair + cur], psi = f[2 pair + 1 - cur]
-    int pair;
+    int cur;                     // FP64: phi = f[cur], psi = f[1 - cur]
+    int pair;                    // FP32: phi = f[2 pair], velocity = f[2 pair + 1]
 };
 struct BatchHdr {
     int nactive, total_tiles;    // all work items
@@ -85,7 +85,7 @@ struct BatchSlotHost {
     bool used = false;
     wg_params prm;
     wg::DevParams dp;
-    void *f[4] = {nullptr, nullptr, nullptr, nullptr};  // f[2], f[3]: second pair of skewed scenes
+    void *f[4] = {nullptr, nullptr, nullptr, nullptr};  // f[2], f[3]: second pair of FP32 scenes
     void *mem[4] = {nullptr, nullptr, nullptr, nullptr};  // the allocations behind f (ghost layout: f is inside)
     uint32_t *act_mem = nullptr, *nz_mem = nullptr;
     uint32_t *act = nullptr, *nz = nullptr;

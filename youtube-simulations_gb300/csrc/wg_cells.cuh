@@ -1,6 +1,6 @@
 // wg_cells.cuh — per-cell building blocks shared by the stepping kernels: field and
 // mask accessors, coefficient sources, 16-byte vector loads, and the boundary-line
-// rule of the native form.
+// rules of the native forms.
 #pragma once
 #include "wg_internal.h"
 
@@ -14,6 +14,16 @@ struct Field {
     const T *a;
     int pitch;
     __device__ __forceinline__ T operator()(int i, int j) const { return a[(size_t)i * pitch + j]; }
+};
+// psi of an FP32 scene: phi - v in FP64
+struct PsiOfVel {
+    const float *x, *v;
+    int pitch;
+    __device__ __forceinline__ double operator()(int i, int j) const
+    {
+        const size_t o = (size_t)i * pitch + j;
+        return S_((double)x[o], (double)v[o]);
+    }
 };
 struct ActI16 {
     const int16_t *a;
@@ -67,62 +77,63 @@ __device__ __forceinline__ void vstore(T *ptr, const T (&v)[Vec<T>::n])
     *reinterpret_cast<typename Vec<T>::type *>(ptr) = t;
 }
 
-// FP32 boundary-line cell of a mirror, periodic or absorbing scene by edge32 (the rule of
+// FP32 boundary-line cell: mirror, periodic and absorbing scenes by edge32 (the rule of
 // the tiled and skewed FP32 steppers), neighbours read from the current level (wrapped
-// around the grid for periodic scenes).
+// around the grid for periodic scenes); the other boundary conditions by the reference
+// rule of edge_cell in FP64 on psi = phi - v, the velocity being the FP64 change rounded
+// once.  FLOOR on cells whose mask is nonzero.
 template <int COEF>
-__device__ inline float fast_edge32(const DevParams &p, const FastArgs<float> &a, int i, int j, long long time, float y)
+__device__ inline XV fast_edge_v(const DevParams &p, const FastArgs<float> &a, int i, int j, long long time)
 {
     const size_t o = (size_t)i * p.pitch + j;
-    const bool per = p.b_cond == WG_BC_PERIODIC;
-    const int ip = (i + 1 < p.nx) ? i + 1 : (per ? 0 : i), im = (i > 0) ? i - 1 : (per ? p.nx - 1 : i);
-    const int jp = (j + 1 < p.ny) ? j + 1 : (per ? 0 : j), jm = (j > 0) ? j - 1 : (per ? p.ny - 1 : j);
-    const float x = a.phi[o];
-    const float n = a.phi[(size_t)ip * p.pitch + j];
-    const float sv = a.phi[(size_t)im * p.pitch + j];
-    const float e = a.phi[(size_t)i * p.pitch + jp];
-    const float w = a.phi[(size_t)i * p.pitch + jm];
-    const bool act = ActBits{a.act, p.wpitch}(i, j);
-    float ccv, tcv, g;
-    if (COEF == WG_COEF_TABLE) {
-        ccv = a.tcc[o];
-        tcv = a.tc ? a.tc[o] : 0.f;
-        g = a.tg ? a.tg[o] : a.gamf;
+    const float x = a.phi[o], y = a.psi[o];
+    XV r;
+    if (p.b_cond == WG_BC_DIRICHLET || p.b_cond == WG_BC_ABSORBING || p.b_cond == WG_BC_PERIODIC) {
+        const bool per = p.b_cond == WG_BC_PERIODIC;
+        const int ip = (i + 1 < p.nx) ? i + 1 : (per ? 0 : i), im = (i > 0) ? i - 1 : (per ? p.nx - 1 : i);
+        const int jp = (j + 1 < p.ny) ? j + 1 : (per ? 0 : j), jm = (j > 0) ? j - 1 : (per ? p.ny - 1 : j);
+        const float n = a.phi[(size_t)ip * p.pitch + j];
+        const float sv = a.phi[(size_t)im * p.pitch + j];
+        const float e = a.phi[(size_t)i * p.pitch + jp];
+        const float w = a.phi[(size_t)i * p.pitch + jm];
+        const bool act = ActBits{a.act, p.wpitch}(i, j);
+        float ccv, tcv, g;
+        if (COEF == WG_COEF_TABLE) {
+            ccv = a.tcc[o];
+            tcv = a.tc ? a.tc[o] : 0.f;
+            g = a.tg ? a.tg[o] : a.gamf;
+        } else {
+            ccv = act ? a.c2f : a.c2bf;
+            tcv = act ? a.courantf : a.courantbf;
+            g = act ? a.gamf : a.gambf;
+        }
+        const Edge32K k{a.kappaf, a.ksf, a.ktf, a.gsf, a.gtf, a.vmaxf};
+        r = edge32<false>(p, i, j, x, y, n, sv, e, w, ccv, tcv, g, act, k,
+                          [&] { return (float)osc_bc(p, (int)time, j); });
     } else {
-        ccv = act ? a.c2f : a.c2bf;
-        tcv = act ? a.courantf : a.courantbf;
-        g = act ? a.gamf : a.gambf;
+        Field<float> PHI{a.phi, p.pitch};
+        PsiOfVel PSI{a.phi, a.psi, p.pitch};
+        ActBits ACT{a.act, p.wpitch};
+        double v;
+        bool w;
+        if (COEF == WG_COEF_MASK) {
+            CoefMask CF{ACT, p.c2, p.c2b, p.gam, p.gamb, p.courant, p.courantb};
+            w = edge_cell<float>(p, time, i, j, PHI, PSI, ACT, CF, &v);
+        } else {
+            CoefTab<float> CF{a.tcc, a.tc, a.tg, p.pitch, p.gam};
+            w = edge_cell<float>(p, time, i, j, PHI, PSI, ACT, CF, &v);
+        }
+        r = w ? XV{(float)v, (float)S_(v, (double)x)} : keep32(x, y);
     }
-    const Edge32K k{a.kappaf, a.ksf, a.ktf, a.gsf, a.gtf, a.vmaxf};
-    float v = edge32<false>(p, i, j, x, y, n, sv, e, w, ccv, tcv, g, act, k,
-                            [&] { return (float)osc_bc(p, (int)time, j); });
-    if (p.floor_clamp && ActBits{a.nz, p.wpitch}(i, j)) v = (float)floor_clamp(p, (double)v);
-    return v;
+    if (p.floor_clamp && ActBits{a.nz, p.wpitch}(i, j)) r = clamp32(x, r, a.vmaxf);
+    return r;
 }
 
-template <class T, int COEF> struct Edge32Path {
-    static __device__ __forceinline__ bool run(const DevParams &, const FastArgs<T> &, int, int, long long, T, T *)
-    {
-        return false;
-    }
-};
-template <int COEF> struct Edge32Path<float, COEF> {
-    static __device__ __forceinline__ bool run(const DevParams &p, const FastArgs<float> &a, int i, int j, long long time,
-                                               float y, float *out)
-    {
-        if (p.b_cond != WG_BC_DIRICHLET && p.b_cond != WG_BC_ABSORBING && p.b_cond != WG_BC_PERIODIC) return false;
-        *out = fast_edge32<COEF>(p, a, i, j, time, y);
-        return true;
-    }
-};
-
-// Boundary-line cell of the native form, reference rules.  Returns the value to
+// Boundary-line cell of the native FP64 form, reference rules.  Returns the value to
 // store (the old psi value y when the reference writes nothing).
 template <class T, int COEF>
 __device__ inline T fast_edge(const DevParams &p, const FastArgs<T> &a, int i, int j, long long time, T y)
 {
-    T r;  // FP32 mirror, periodic and absorbing scenes: the FP32 rule
-    if (Edge32Path<T, COEF>::run(p, a, i, j, time, y, &r)) return r;
     Field<T> PHI{a.phi, p.pitch}, PSI{a.psi, p.pitch};
     ActBits ACT{a.act, p.wpitch}, NZ{a.nz, p.wpitch};
     double v;

@@ -71,29 +71,57 @@ __device__ __forceinline__ double absorb64(double x, double y, double tc, double
     return S_(r, M_(g, S_(x, y)));
 }
 
-// FP32 update in increment form: out = x + ((1-g)(x-y) - kappa*x + cc*delta) with the
+// FP32 state: phi and the velocity v = phi(t) - phi(t-1), each stored in FP32 (psi is
+// phi - v; conversions in and out are done in FP64).  v kept as its own array carries
+// the increment each update applied, to FP32 precision of v itself; recovered from two
+// stored levels it would carry the rounding of phi, magnified by |phi|/|v| (16-80 times
+// less accurate energies in measurements, more so for small COURANT numbers).  A rule
+// returns the cell's new (phi, v).
+struct XV {
+    float x, v;
+};
+
+// Bulk update in increment form: v' = (1-g) v - kappa x + cc delta, x' = x + v', with the
 // Laplacian as differences from the centre.  Same mathematics as upd64.  Every rounding
-// is spelled out as an explicit operation or fused multiply-add (nothing is left for the
-// compiler to contract), so every kernel that applies it rounds each cell the same way.
-__device__ __forceinline__ float upd32(float x, float y, float cc, float delta, float kappa, float g)
+// is spelled out as an operation or a fused multiply-add (nothing left for the compiler
+// to contract), so every kernel that applies it rounds each cell the same way.
+__device__ __forceinline__ XV upd32(float x, float v, float cc, float delta, float kappa, float g)
 {
-    const float w = __fsub_rn(x, y);
-    const float inc = fmaf(cc, delta, fmaf(-kappa, x, fmaf(-g, w, w)));
-    return __fadd_rn(x, inc);
+    const float vn = fmaf(cc, delta, fmaf(-kappa, x, fmaf(-g, v, v)));
+    return XV{__fadd_rn(x, vn), vn};
 }
 // upd32 with KAPPA = 0: the kappa*x term is then an exact zero, so leaving it out changes
 // at most the sign of a zero result, never a value.
-__device__ __forceinline__ float upd32_k0(float x, float y, float cc, float delta, float g)
+__device__ __forceinline__ XV upd32_k0(float x, float v, float cc, float delta, float g)
 {
-    const float w = __fsub_rn(x, y);
-    return __fadd_rn(x, fmaf(cc, delta, fmaf(-g, w, w)));
+    const float vn = fmaf(cc, delta, fmaf(-g, v, v));
+    return XV{__fadd_rn(x, vn), vn};
 }
-
-// x - (tc*(x-nb) + k*x + g*(x-y)) with its roundings spelled out (as upd32).
-__device__ __forceinline__ float absorb32(float x, float y, float tc, float nb, float k, float g)
+// Absorbing edge: x' = x - (tc (x - nb) + k x + g v).
+__device__ __forceinline__ XV absorb32(float x, float v, float tc, float nb, float k, float g)
 {
     const float t = fmaf(k, x, __fmul_rn(tc, __fsub_rn(x, nb)));
-    return __fsub_rn(x, fmaf(g, __fsub_rn(x, y), t));
+    const float vn = -fmaf(g, v, t);
+    return XV{__fadd_rn(x, vn), vn};
+}
+// A value a rule sets (oscillating edge, FLOOR): the velocity is the change it makes.
+__device__ __forceinline__ XV set32(float x, float xn) { return XV{xn, __fsub_rn(xn, x)}; }
+// A cell the reference does not write: the in-place two-level form swaps phi and psi
+// there, so phi' = psi = x - v and v' = -v.
+__device__ __forceinline__ XV keep32(float x, float v) { return XV{__fsub_rn(x, v), -v}; }
+// FLOOR: phi clamped to [-vmax, vmax] by the reference's two comparisons (a NaN passes,
+// as there); an unchanged value keeps its velocity.
+__device__ __forceinline__ XV clamp32(float x, XV r, float vmax)
+{
+    if (r.x > vmax) return set32(x, vmax);
+    if (r.x < -vmax) return set32(x, -vmax);
+    return r;
+}
+// The point source: its FP64 increment added to the new value and to the velocity (psi
+// is not touched), each rounded once.
+__device__ __forceinline__ XV source32(XV r, double add)
+{
+    return XV{(float)A_((double)r.x, add), (float)A_((double)r.v, add)};
 }
 
 // oscillating_bc (sub_wave.c:11965-12162) with the reference's constants.
@@ -206,18 +234,17 @@ __device__ __forceinline__ bool left_bc(const DevParams &p, int j)
 // FP32 boundary-line cell (rows 0 and nx-1, columns 0 and ny-1) for mirror ("Dirichlet"),
 // periodic and absorbing boundaries: edge_cell's rules (below) in the FP32 increment form
 // of upd32 / absorb32, the neighbours the reference mirrors replaced by the cell itself.
-// x, y: phi and psi of the cell; n, sv, e, w: phi at i+1, i-1, j+1, j-1 (wrapped around
-// the grid for periodic scenes; any value where outside the grid otherwise); ccv, tcv, g:
-// the cell's tcc, tc and tgamma; osc(): the oscillating value.  Returns y where the
+// x, v: phi and velocity of the cell; n, sv, e, w: phi at i+1, i-1, j+1, j-1 (wrapped
+// around the grid for periodic scenes; any value where outside the grid otherwise); ccv,
+// tcv, g: the cell's tcc, tc and tgamma; osc(): the oscillating value.  keep32 where the
 // reference writes nothing.  CLAMP: FLOOR on written cells with act.  Every FP32 stepper
 // (single updates, tiles, skewed passes) uses this rule.
 struct Edge32K {
     float kappa, ks, kt, gs, gt, vmax;
 };
 template <bool CLAMP, class OscF>
-__device__ __forceinline__ float edge32(const DevParams &p, int gi, int gj, float x, float y, float n, float sv,
-                                        float e, float w, float ccv, float tcv, float g, bool act, const Edge32K &k,
-                                        const OscF &osc)
+__device__ __forceinline__ XV edge32(const DevParams &p, int gi, int gj, float x, float v, float n, float sv, float e,
+                                     float w, float ccv, float tcv, float g, bool act, const Edge32K &k, const OscF &osc)
 {
     const int NX = p.nx, NY = p.ny;
     const bool bi0 = gi == 0, bi1 = gi == NX - 1, bj0 = gj == 0, bj1 = gj == NY - 1;
@@ -254,23 +281,23 @@ __device__ __forceinline__ float edge32(const DevParams &p, int gi, int gj, floa
         }
     }
     if (p.osc_left && !p.beam && bi0 && (bj0 || (p.corner2_on && gj == NX - 1))) mode = 2;
-    float v = y;
+    XV r = keep32(x, v);
     if (mode == 2 || p.twospeeds || act) {
-        if (mode == 0) v = upd32(x, y, ccv, ((n - x) + (sv - x)) + ((e - x) + (w - x)), k.kappa, g);
-        else if (mode == 1) v = absorb32(x, y, tcv, nb, kk, gg);
-        else v = osc();
-        if (CLAMP && p.floor_clamp && act) v = fminf(fmaxf(v, -k.vmax), k.vmax);
+        if (mode == 0) r = upd32(x, v, ccv, ((n - x) + (sv - x)) + ((e - x) + (w - x)), k.kappa, g);
+        else if (mode == 1) r = absorb32(x, v, tcv, nb, kk, gg);
+        else r = set32(x, osc());
+        if (CLAMP && p.floor_clamp && act) r = clamp32(x, r, k.vmax);
     }
-    return v;
+    return r;
 }
 
 // Any boundary-line cell of the reference (left/right columns, top/bottom rows),
 // computed with the reference's rules.  Returns true when the reference writes the
 // cell; *out then holds the value (corner oscillation included, FLOOR not).
 // Accessors: PHI(i,j), PSI(i,j) field reads; ACT(i,j) -> "xy != 0"; TCC/TC/TG tables.
-template <class T, class Phi, class Act, class Coef>
+template <class T, class Phi, class Psi, class Act, class Coef>
 __device__ inline bool edge_cell(const DevParams &p, long long time, int i, int j,
-                                 const Phi &PHI, const Phi &PSI, const Act &ACT, const Coef &CF,
+                                 const Phi &PHI, const Psi &PSI, const Act &ACT, const Coef &CF,
                                  double *out)
 {
     const int NX = p.nx, NY = p.ny;

@@ -53,7 +53,8 @@ __global__ void k_frame_rgb8(const __grid_constant__ DevParams p, const T *__res
         const int jp = (j + 1 == p.ny) ? p.ny - 1 : j + 1, jm = (j == 0) ? 0 : j - 1;
         const double e = (double)phi[(size_t)ip * p.pitch + j], wv = (double)phi[(size_t)im * p.pitch + j];
         const double n = (double)phi[(size_t)i * p.pitch + jp], sv = (double)phi[(size_t)i * p.pitch + jm];
-        const double y = (double)psi[c];
+        // psi of FP64 fields; FP32 fields hold the velocity: psi = phi - v (exact in FP64)
+        const double y = sizeof(T) == 4 ? S_(x, (double)psi[c]) : (double)psi[c];
         if (plot == WG_P_ENERGY_FLUX || plot == WG_P_TOTAL_ENERGY_FLUX) {
             vel = fabs(S_(x, y));
             gx = S_(e, wv);

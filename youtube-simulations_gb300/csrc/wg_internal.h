@@ -7,11 +7,15 @@
 
 namespace wg {
 
+// FP64 fields: phi (level t), psi (level t-1, read at the cell itself only) and out
+// (level t+1, == psi: in place).  FP32 fields: phi and the velocity v = phi - psi in psi;
+// the update writes the new phi to out and the new velocity to vout (another pair).
 template <class T>
 struct FastArgs {
-    const T *phi;        // level t
-    const T *psi;        // level t-1 (read at the cell itself only)
-    T *out;              // level t+1 (== psi for the in-place form)
+    const T *phi;
+    const T *psi;
+    T *out;
+    T *vout;             // FP32 only
     const uint32_t *act; // "active" plane: bulk xy > 0, boundary lines xy != 0
     const uint32_t *nz;  // "nonzero" plane: xy != 0
     const T *tcc, *tc, *tg;  // WG_COEF_TABLE tables (tg may be null: uniform)
@@ -45,10 +49,10 @@ void launch_step_exact_energy(const DevParams &p, const double *phi, const doubl
                               const int16_t *xy, long long time, cudaStream_t st);
 void launch_neumann_exact(const DevParams &p, const double *phi, double *out, const int16_t *xy,
                           const wg_neumann_bc *rec, int n, cudaStream_t st);
-template <class T> void launch_point_source(const DevParams &p, T *out, long long time, cudaStream_t st);
+template <class T> void launch_point_source(const DevParams &p, T *out, T *vout, long long time, cudaStream_t st);
 template <class T> void launch_step_fast(const DevParams &p, const FastArgs<T> &a, int coef_mode, long long time,
                                          cudaStream_t st);
-template <class T> void launch_neumann_fast(const DevParams &p, const T *phi, T *out, const int4 *idx,
+template <class T> void launch_neumann_fast(const DevParams &p, const T *phi, T *out, T *vout, const int4 *idx,
                                             const double2 *w, int n, cudaStream_t st);
 template <class T> void launch_energy(const DevParams &p, const T *phi, const T *psi, const int16_t *xy,
                                       const uint32_t *nz, double2 *bot, double2 *top, int ileft, int iright,
@@ -59,6 +63,11 @@ void launch_pack_mask(int nx, int ny, int wpitch, const int16_t *xy, uint32_t *a
 template <class T> void launch_convert_in(int nx, int ny, int pitch, const double *src, T *dst, cudaStream_t st);
 template <class T> void launch_convert_out(int nx, int ny, int pitch, const T *src, double *dst, cudaStream_t st);
 template <class T> void launch_repack_in(int nx, int ny, int pitch, const T *src, T *dst, cudaStream_t st);
+// FP32 state (phi, velocity) from and to host (phi, psi) rows of H = double or float
+template <class H> void launch_state_in32(int nx, int ny, int pitch, const H *phi, const H *psi, float *x, float *v,
+                                          cudaStream_t st);
+template <class H> void launch_state_out32(int nx, int ny, int pitch, const float *x, const float *v, H *phi, H *psi,
+                                           cudaStream_t st);
 
 // add_circular_wave (wg_pulse.cu): the grid geometry, the pulse and the box of cells to visit
 struct PulseArgs {
@@ -69,9 +78,10 @@ struct PulseArgs {
 };
 wg_status pulse_args(const wg_params &p, int pitch, int wpitch, double init_amp, double factor, double x, double y,
                      double variance, double wavelength, PulseArgs *a);
-// xy (int16 mask, nonzero test) or, when xy is NULL, nz (the "nonzero" bit plane)
-template <class T> void launch_add_circular_wave(const PulseArgs &a, T *phi, const int16_t *xy, const uint32_t *nz,
-                                                 cudaStream_t st);
+// xy (int16 mask, nonzero test) or, when xy is NULL, nz (the "nonzero" bit plane); vel
+// (FP32 fields, else NULL): the velocity, which takes the same increment
+template <class T> void launch_add_circular_wave(const PulseArgs &a, T *phi, T *vel, const int16_t *xy,
+                                                 const uint32_t *nz, cudaStream_t st);
 void launch_cell_energy(const DevParams &p, const double *phi, const double *psi, const int16_t *xy, int i, int j,
                         double *out, cudaStream_t st);
 

@@ -4,8 +4,9 @@
 //  k_step_exact   drop-in form: int16 mask, FP64 tables, three buffers, writes exactly
 //                 the cells wave_billiard.c:302-610 writes (bit-identical FP64).
 //  k_step_bulk    native form, interior rows: 1-bit masks, 16-byte vector loads along
-//                 j, in place (the new level overwrites psi), FP64 (reference
-//                 operation order) or FP32 (increment form).
+//                 j; FP64 (reference operation order) in place (the new level
+//                 overwrites psi), or FP32 (phi and velocity, increment form) into the
+//                 other pair of fields.
 //  k_step_edge    native form, the four boundary lines and the point source.
 //  k_neumann      Neumann gather of wave_billiard.c:379-389 for the active records.
 //  k_energy_cols  compute_energy (wave_common.c:453-472) per cell, one warp per
@@ -172,21 +173,25 @@ __global__ void k_neumann_exact(DevParams p, const double *__restrict__ phi, dou
     out[c] = v;
 }
 
+// vout (FP32 fields): the velocity takes the increment too.
 template <class T>
-__global__ void k_point_source(DevParams p, T *out, long long time)
+__global__ void k_point_source(DevParams p, T *out, T *vout, long long time)
 {
     const size_t c = (size_t)p.src_i * p.pitch + p.src_j;
-    out[c] = (T)A_((double)out[c], point_source(p, time));
+    const double add = point_source(p, time);
+    out[c] = (T)A_((double)out[c], add);
+    if (vout) vout[c] = (T)A_((double)vout[c], add);
 }
 
 // ---------------------------------------------------------------------------
 // Fast native kernel
 // ---------------------------------------------------------------------------
-// Interior rows 1..nx-2 of one update, in place (the new level overwrites psi): each
-// thread updates V = 16/sizeof(T) consecutive cells of row i with every load (three
-// phi rows, psi, tcc, the j-1 / j+V neighbours, the mask word) issued before the
-// first use.  Boundary-line cells (j = 0, j = ny-1) and padding are written back
-// unchanged; k_step_edge computes them afterwards.
+// Interior rows 1..nx-2 of one update: each thread updates V = 16/sizeof(T) consecutive
+// cells of row i with every load (three phi rows, psi or the velocity, tcc, the j-1 / j+V
+// neighbours, the mask word) issued before the first use.  FP64: in place, the new level
+// overwriting psi.  FP32: the new phi and velocity into the other pair.  Boundary-line
+// cells (j = 0, j = ny-1) and padding take the rule of an unwritten cell; k_step_edge
+// computes the boundary lines afterwards.
 template <class T, int COEF, int Z = 0>
 __global__ void __launch_bounds__(256) k_step_bulk(const __grid_constant__ DevParams p,
                                                    const __grid_constant__ FastArgs<T> a)
@@ -207,44 +212,50 @@ __global__ void __launch_bounds__(256) k_step_bulk(const __grid_constant__ DevPa
     const uint32_t word = a.act[(size_t)i * p.wpitch + (j0 >> 5)] >> (j0 & 31);
     uint32_t nzw = 0;
     if (p.floor_clamp && a.has_ghosts) nzw = a.nz[(size_t)i * p.wpitch + (j0 >> 5)] >> (j0 & 31);
-    T out[V];
+    T out[V], vo[V];
 #pragma unroll
     for (int k = 0; k < V; k++) {
         const int j = j0 + k;
-        T v = y[k];
         const bool act = (word >> k) & 1u;
-        if (j >= 1 && j < p.ny - 1 && (p.twospeeds || act)) {
-            const T x = c[k];
-            const T w = (k == 0) ? wl : c[k - 1];
-            const T e = (k == V - 1) ? er : c[k + 1];
-            if (sizeof(T) == 8) {
-                const double delta = L4_(A_(A_(A_((double)n[k], (double)s[k]), (double)e), (double)w), (double)x);
+        const bool upd = j >= 1 && j < p.ny - 1 && (p.twospeeds || act);
+        const bool clamp = p.floor_clamp && j >= 1 && j < p.ny - 1 && ((upd && act) || ((nzw >> k) & 1u));
+        const T x = c[k];
+        const T w = (k == 0) ? wl : c[k - 1];
+        const T e = (k == V - 1) ? er : c[k + 1];
+        if constexpr (sizeof(T) == 8) {
+            double v = y[k];
+            if (upd) {
+                const double delta = L4_(A_(A_(A_(n[k], s[k]), e), w), x);
                 const double ccv = (COEF == WG_COEF_TABLE) ? (double)cc[k] : (act ? p.c2 : p.c2b);
                 double g;
                 if (COEF == WG_COEF_TABLE) g = a.tg ? (double)a.tg[row + j] : p.gam;
                 else g = act ? p.gam : p.gamb;
-                v = (T)upd64<Z>((double)x, (double)y[k], ccv, delta, p.kappa, g);
-            } else {
-                const float xf = (float)x;
-                const float delta = (((float)n[k] - xf) + ((float)s[k] - xf)) + (((float)e - xf) + ((float)w - xf));
-                const float ccv = (COEF == WG_COEF_TABLE) ? (float)cc[k] : (act ? a.c2f : a.c2bf);
-                float g;
-                if (COEF == WG_COEF_TABLE) g = a.tg ? (float)a.tg[row + j] : a.gamf;
-                else g = act ? a.gamf : a.gambf;
-                v = (T)upd32(xf, (float)y[k], ccv, delta, a.kappaf, g);
+                v = upd64<Z>(x, y[k], ccv, delta, p.kappa, g);
             }
-            if (p.floor_clamp && (act || ((nzw >> k) & 1u))) v = (T)floor_clamp(p, (double)v);
-        } else if (p.floor_clamp && ((nzw >> k) & 1u) && j >= 1 && j < p.ny - 1) {
-            v = (T)floor_clamp(p, (double)v);
+            if (clamp) v = floor_clamp(p, v);
+            out[k] = (T)v;
+        } else {
+            XV r = keep32(x, y[k]);
+            if (upd) {
+                const float delta = ((n[k] - x) + (s[k] - x)) + ((e - x) + (w - x));
+                const float ccv = (COEF == WG_COEF_TABLE) ? cc[k] : (act ? a.c2f : a.c2bf);
+                float g;
+                if (COEF == WG_COEF_TABLE) g = a.tg ? a.tg[row + j] : a.gamf;
+                else g = act ? a.gamf : a.gambf;
+                r = upd32(x, y[k], ccv, delta, a.kappaf, g);
+            }
+            if (clamp) r = clamp32(x, r, a.vmaxf);
+            out[k] = r.x;
+            vo[k] = r.v;
         }
-        out[k] = v;
     }
     vstore(a.out + row + j0, out);
+    if constexpr (sizeof(T) == 4) vstore(a.vout + row + j0, vo);
 }
 
 // The four boundary lines of one update (one thread per cell, reference rules) and,
 // in the last thread, the point source when it lies inside; runs after k_step_bulk
-// on the same in-place level (boundary cells read only phi and their own psi).
+// (boundary cells read only phi and their own psi or velocity).
 template <class T, int COEF>
 __global__ void __launch_bounds__(256) k_step_edge(const __grid_constant__ DevParams p,
                                                    const __grid_constant__ FastArgs<T> a, long long time)
@@ -261,19 +272,31 @@ __global__ void __launch_bounds__(256) k_step_edge(const __grid_constant__ DevPa
         if (idx == nedge && a.do_source && p.src_on && p.src_i > 0 && p.src_i < NX - 1 && p.src_j > 0 &&
             p.src_j < NY - 1) {
             const size_t o = (size_t)p.src_i * p.pitch + p.src_j;
-            a.out[o] = (T)A_((double)a.out[o], point_source(p, time));
+            const double add = point_source(p, time);
+            a.out[o] = (T)A_((double)a.out[o], add);
+            if constexpr (sizeof(T) == 4) a.vout[o] = (T)A_((double)a.vout[o], add);
         }
         return;
     }
     const size_t o = (size_t)i * p.pitch + j;
-    T v = fast_edge<T, COEF>(p, a, i, j, time, a.psi[o]);
-    if (a.do_source && p.src_on && i == p.src_i && j == p.src_j) v = (T)A_((double)v, point_source(p, time));
-    a.out[o] = v;
+    const bool src = a.do_source && p.src_on && i == p.src_i && j == p.src_j;
+    if constexpr (sizeof(T) == 8) {
+        T v = fast_edge<T, COEF>(p, a, i, j, time, a.psi[o]);
+        if (src) v = (T)A_((double)v, point_source(p, time));
+        a.out[o] = v;
+    } else {
+        XV r = fast_edge_v<COEF>(p, a, i, j, time);
+        if (src) r = source32(r, point_source(p, time));
+        a.out[o] = r.x;
+        a.vout[o] = r.v;
+    }
 }
 
-// Native Neumann gather: active records only, in place on the new level.
+// Native Neumann gather: active records only, from phi (level t) into the new level
+// (vout: FP32 fields, the velocity of the gathered value against the cell's phi at level
+// t, in FP64).
 template <class T>
-__global__ void k_neumann_fast(DevParams p, const T *__restrict__ phi, T *__restrict__ out,
+__global__ void k_neumann_fast(DevParams p, const T *__restrict__ phi, T *__restrict__ out, T *__restrict__ vout,
                                const int4 *__restrict__ idx, const double2 *__restrict__ w, int n)
 {
     const int q = blockIdx.x * blockDim.x + threadIdx.x;
@@ -285,6 +308,7 @@ __global__ void k_neumann_fast(DevParams p, const T *__restrict__ phi, T *__rest
     v = A_(v, M_(cw.y, (double)phi[r.z]));
     if (p.floor_clamp && (r.w & 1)) v = floor_clamp(p, v);
     out[r.x] = (T)v;
+    if (vout) vout[r.x] = (T)S_(v, (double)phi[r.x]);
 }
 
 // ---------------------------------------------------------------------------
@@ -319,11 +343,11 @@ struct DF {
     __device__ __forceinline__ double value() const { return A_((double)h, (double)l); }
 };
 
-// compute_energy in FP32 for FP32 fields (same formula and order as cell_energy).
-__device__ __forceinline__ float cell_energy32(float es2, float hc2, float hc2b, int twospeeds, float x, float psi,
+// compute_energy in FP32 for FP32 fields (same formula and order as cell_energy), with
+// the stored velocity v in place of phi - psi.
+__device__ __forceinline__ float cell_energy32(float es2, float hc2, float hc2b, int twospeeds, float x, float v,
                                                float e, float w, float n, float s, int m)
 {
-    float v = x - psi;
     float a = e - x, b = x - w, c = n - x, d = x - s;
     float g = (a * a + b * b) + (c * c + d * d);
     if (m) return es2 * (v * v + hc2 * g);
@@ -366,7 +390,7 @@ __device__ __forceinline__ void acc_merge(DF &a, const DF &o) { a.merge(o); }
 // boxes of compute_energy_tblr (sub_wave_comp.c:1752-1800) over its columns, and its
 // total.  cols[i] = (sum over j < ny/2, sum over j >= ny/2); part[6 b + k] = box k of
 // block b (0..2 top left/mid/right, 3..5 bottom); the block's total overwrites
-// cols[8 b].y (already folded into the boxes).
+// cols[8 b].y (already folded into the boxes).  FP32 fields: psi is the velocity.
 #define ENERGY_COLS_PER_BLOCK 8
 template <class T, int MASK>
 __global__ void __launch_bounds__(32 * ENERGY_COLS_PER_BLOCK)
@@ -389,7 +413,7 @@ __global__ void __launch_bounds__(32 * ENERGY_COLS_PER_BLOCK)
         const float es2 = (float)p.e_scale2, hc2 = (float)p.ehalf_c2, hc2b = (float)p.ehalf_c2b;
         if (sizeof(T) == 4 && MASK == 1) {
             // FP32 fields: four cells per lane and step as 16-byte loads of the rows i-1, i, i+1
-            // and psi; the j-1 / j+1 neighbours from the adjacent lanes (the row pitch is a
+            // and the velocity; the j-1 / j+1 neighbours from the adjacent lanes (the row pitch is a
             // multiple of 128 elements, so every load stays in the row)
             const float *fc = (const float *)rc, *fy = (const float *)ry, *fe = (const float *)re,
                         *fw = (const float *)rw;
@@ -544,6 +568,35 @@ __global__ void k_convert_out(int nx, int ny, int pitch, const T *__restrict__ s
     dst[(size_t)i * ny + j] = (double)src[(size_t)i * pitch + j];
 }
 
+// FP32 state from host (phi, psi) rows, dense [nx][ny] of H = double or float: phi
+// rounded once, the velocity phi - psi computed in FP64 (exact for two floats) and
+// rounded once; padding zeroed.
+template <class H>
+__global__ void k_state_in32(int nx, int ny, int pitch, const H *__restrict__ phi, const H *__restrict__ psi,
+                             float *__restrict__ x, float *__restrict__ v)
+{
+    const int j = blockIdx.x * blockDim.x + threadIdx.x;
+    const int i = blockIdx.y;
+    if (j >= pitch || i >= nx) return;
+    const size_t o = (size_t)i * pitch + j, c = (size_t)i * ny + j;
+    const double a = j < ny ? (double)phi[c] : 0.0, b = j < ny ? (double)psi[c] : 0.0;
+    x[o] = (float)a;
+    v[o] = (float)S_(a, b);
+}
+// FP32 state to host rows: phi, and psi = phi - v in FP64 (rounded to H); either may be NULL.
+template <class H>
+__global__ void k_state_out32(int nx, int ny, int pitch, const float *__restrict__ x, const float *__restrict__ v,
+                              H *__restrict__ phi, H *__restrict__ psi)
+{
+    const int j = blockIdx.x * blockDim.x + threadIdx.x;
+    const int i = blockIdx.y;
+    if (j >= ny || i >= nx) return;
+    const size_t o = (size_t)i * pitch + j, c = (size_t)i * ny + j;
+    const double a = (double)x[o];
+    if (phi) phi[c] = (H)a;
+    if (psi) psi[c] = (H)S_(a, (double)v[o]);
+}
+
 // ---------------------------------------------------------------------------
 // Host launchers
 // ---------------------------------------------------------------------------
@@ -576,12 +629,12 @@ void launch_neumann_exact(const DevParams &p, const double *phi, double *out, co
 }
 
 template <class T>
-void launch_point_source(const DevParams &p, T *out, long long time, cudaStream_t st)
+void launch_point_source(const DevParams &p, T *out, T *vout, long long time, cudaStream_t st)
 {
-    k_point_source<T><<<1, 1, 0, st>>>(p, out, time);
+    k_point_source<T><<<1, 1, 0, st>>>(p, out, vout, time);
 }
-template void launch_point_source<float>(const DevParams &, float *, long long, cudaStream_t);
-template void launch_point_source<double>(const DevParams &, double *, long long, cudaStream_t);
+template void launch_point_source<float>(const DevParams &, float *, float *, long long, cudaStream_t);
+template void launch_point_source<double>(const DevParams &, double *, double *, long long, cudaStream_t);
 
 // FP64: the bulk update without the terms whose coefficient is zero on every cell
 // (upd64's Z flags: KAPPA = 0; GAMMA = 0 as a uniform value); the values are unchanged.
@@ -618,14 +671,14 @@ template void launch_step_fast<float>(const DevParams &, const FastArgs<float> &
 template void launch_step_fast<double>(const DevParams &, const FastArgs<double> &, int, long long, cudaStream_t);
 
 template <class T>
-void launch_neumann_fast(const DevParams &p, const T *phi, T *out, const int4 *idx, const double2 *w, int n,
+void launch_neumann_fast(const DevParams &p, const T *phi, T *out, T *vout, const int4 *idx, const double2 *w, int n,
                          cudaStream_t st)
 {
     if (n <= 0) return;
-    k_neumann_fast<T><<<(n + 255) / 256, 256, 0, st>>>(p, phi, out, idx, w, n);
+    k_neumann_fast<T><<<(n + 255) / 256, 256, 0, st>>>(p, phi, out, vout, idx, w, n);
 }
-template void launch_neumann_fast<float>(const DevParams &, const float *, float *, const int4 *, const double2 *, int, cudaStream_t);
-template void launch_neumann_fast<double>(const DevParams &, const double *, double *, const int4 *, const double2 *, int, cudaStream_t);
+template void launch_neumann_fast<float>(const DevParams &, const float *, float *, float *, const int4 *, const double2 *, int, cudaStream_t);
+template void launch_neumann_fast<double>(const DevParams &, const double *, double *, double *, const int4 *, const double2 *, int, cudaStream_t);
 
 template <class T>
 void launch_energy(const DevParams &p, const T *phi, const T *psi, const int16_t *xy, const uint32_t *nz,
@@ -679,5 +732,22 @@ template void launch_convert_in<float>(int, int, int, const double *, float *, c
 template void launch_convert_in<double>(int, int, int, const double *, double *, cudaStream_t);
 template void launch_convert_out<float>(int, int, int, const float *, double *, cudaStream_t);
 template void launch_convert_out<double>(int, int, int, const double *, double *, cudaStream_t);
+
+template <class H>
+void launch_state_in32(int nx, int ny, int pitch, const H *phi, const H *psi, float *x, float *v, cudaStream_t st)
+{
+    dim3 grd((pitch + 255) / 256, nx);
+    k_state_in32<H><<<grd, 256, 0, st>>>(nx, ny, pitch, phi, psi, x, v);
+}
+template <class H>
+void launch_state_out32(int nx, int ny, int pitch, const float *x, const float *v, H *phi, H *psi, cudaStream_t st)
+{
+    dim3 grd((ny + 255) / 256, nx);
+    k_state_out32<H><<<grd, 256, 0, st>>>(nx, ny, pitch, x, v, phi, psi);
+}
+template void launch_state_in32<float>(int, int, int, const float *, const float *, float *, float *, cudaStream_t);
+template void launch_state_in32<double>(int, int, int, const double *, const double *, float *, float *, cudaStream_t);
+template void launch_state_out32<float>(int, int, int, const float *, const float *, float *, float *, cudaStream_t);
+template void launch_state_out32<double>(int, int, int, const float *, const float *, double *, double *, cudaStream_t);
 
 }  // namespace wg

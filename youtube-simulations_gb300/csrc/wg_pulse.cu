@@ -2,8 +2,9 @@
 //
 // phi += INITIAL_AMP*factor*exp(-r^2/INITIAL_VARIANCE)*cos(-r/INITIAL_WAVELENGTH) on the
 // cells whose mask is nonzero (every cell with TWOSPEEDS), r the distance of the cell
-// (ij_to_xy, sub_wave.c:469-476) from (x, y); psi is not touched.  The FP64 arithmetic
-// runs in the reference's order without contraction; exp and cos are CUDA's.
+// (ij_to_xy, sub_wave.c:469-476) from (x, y); psi is not touched, so an FP32 scene's
+// velocity phi - psi takes the same increment.  The FP64 arithmetic runs in the
+// reference's order without contraction; exp and cos are CUDA's.
 //
 // Only a box around (x, y) is visited.  Outside it, r^2 > 760 variance, where
 // exp(-r^2/variance) is 0 in double precision (it underflows below about -745.1), so the
@@ -15,7 +16,7 @@
 namespace wg {
 
 template <class T, int MASK>
-__global__ void __launch_bounds__(128) k_add_circular_wave(PulseArgs a, T *__restrict__ phi,
+__global__ void __launch_bounds__(128) k_add_circular_wave(PulseArgs a, T *__restrict__ phi, T *__restrict__ vel,
                                                            const int16_t *__restrict__ xy,
                                                            const uint32_t *__restrict__ nz)
 {
@@ -33,6 +34,10 @@ __global__ void __launch_bounds__(128) k_add_circular_wave(PulseArgs a, T *__res
     const double v = M_(M_(M_(a.init_amp, a.factor), exp(D_(-d2, a.variance))), cos(D_(-sqrt(d2), a.wavelength)));
     T &c = phi[(size_t)i * a.pitch + j];
     c = (T)A_((double)c, v);
+    if (vel) {
+        T &u = vel[(size_t)i * a.pitch + j];
+        u = (T)A_((double)u, v);
+    }
 }
 
 wg_status pulse_args(const wg_params &p, int pitch, int wpitch, double init_amp, double factor, double x, double y,
@@ -77,15 +82,18 @@ wg_status pulse_args(const wg_params &p, int pitch, int wpitch, double init_amp,
 }
 
 template <class T>
-void launch_add_circular_wave(const PulseArgs &a, T *phi, const int16_t *xy, const uint32_t *nz, cudaStream_t st)
+void launch_add_circular_wave(const PulseArgs &a, T *phi, T *vel, const int16_t *xy, const uint32_t *nz,
+                              cudaStream_t st)
 {
     if (a.ni <= 0 || a.nj <= 0) return;
     dim3 grd((a.nj + 127) / 128, a.ni);
-    if (xy) k_add_circular_wave<T, 0><<<grd, 128, 0, st>>>(a, phi, xy, nz);
-    else k_add_circular_wave<T, 1><<<grd, 128, 0, st>>>(a, phi, xy, nz);
+    if (xy) k_add_circular_wave<T, 0><<<grd, 128, 0, st>>>(a, phi, vel, xy, nz);
+    else k_add_circular_wave<T, 1><<<grd, 128, 0, st>>>(a, phi, vel, xy, nz);
 }
-template void launch_add_circular_wave<float>(const PulseArgs &, float *, const int16_t *, const uint32_t *, cudaStream_t);
-template void launch_add_circular_wave<double>(const PulseArgs &, double *, const int16_t *, const uint32_t *, cudaStream_t);
+template void launch_add_circular_wave<float>(const PulseArgs &, float *, float *, const int16_t *, const uint32_t *,
+                                              cudaStream_t);
+template void launch_add_circular_wave<double>(const PulseArgs &, double *, double *, const int16_t *,
+                                               const uint32_t *, cudaStream_t);
 
 }  // namespace wg
 
@@ -100,8 +108,10 @@ extern "C" wg_status wg_scene_add_circular_wave(wg_scene *s, double init_amp, do
     wg_status st = pulse_args(s->prm, s->pitch, s->dp.wpitch, init_amp, factor, x, y, variance, wavelength, &a);
     if (st) return st;
     void *phi = s->f[s->cur];
-    if (s->prec == WG_FP32) launch_add_circular_wave<float>(a, (float *)phi, nullptr, s->nz, s->st);
-    else launch_add_circular_wave<double>(a, (double *)phi, nullptr, s->nz, s->st);
+    if (s->prec == WG_FP32)
+        launch_add_circular_wave<float>(a, (float *)phi, (float *)s->f[1 - s->cur], nullptr, s->nz, s->st);
+    else
+        launch_add_circular_wave<double>(a, (double *)phi, nullptr, nullptr, s->nz, s->st);
     s->launches++;
     WG_CUDA(cudaGetLastError());
     return WG_OK;

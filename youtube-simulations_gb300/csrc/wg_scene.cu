@@ -1,6 +1,7 @@
-// wg_scene.cu — native scene handles: fields resident in HBM in FP64 or FP32, 1-bit
-// masks, optional coefficient tables, in-place leapfrog (the new level overwrites
-// psi), temporal blocking, energy diagnostics and colour-mapped frames.
+// wg_scene.cu — native scene handles: fields resident in HBM in FP64 (phi, psi; in-place
+// leapfrog, the new level overwriting psi) or FP32 (phi and the velocity phi - psi, each
+// update writing the other pair of fields), 1-bit masks, optional coefficient tables,
+// temporal blocking, energy diagnostics and colour-mapped frames.
 #include <algorithm>
 #include <cmath>
 #include <cstring>
@@ -33,8 +34,7 @@ size_t scene_device_bytes(const wg_params &p, int prec, int coef)
         b += (size_t)p.nx * pitch * esz;                // tcc
         if (p.b_cond == WG_BC_ABSORBING || p.b_cond == WG_BC_VPER_HABS) b += (size_t)p.nx * pitch * esz;  // tc
     }
-    if (prec == WG_FP32 && (p.b_cond == WG_BC_DIRICHLET || p.b_cond == WG_BC_ABSORBING))
-        b += 2 * (size_t)p.nx * pitch * esz;            // output pair of temporally blocked passes
+    if (prec == WG_FP32) b += 2 * (size_t)p.nx * pitch * esz;  // FP32: the output pair of every update
     b += (size_t)p.nx * 2 * sizeof(double2) + (p.nx + 8) * sizeof(double) + 64;  // energy scratch
     return b;
 }
@@ -50,6 +50,44 @@ static wg_status upload_f64(wg_scene *s, const double *h, void *dev)
     else launch_convert_in<double>(s->prm.nx, s->prm.ny, s->pitch, (const double *)s->dstage, (double *)dev, s->st);
     WG_CUDA(cudaGetLastError());
     WG_CUDA(cudaStreamSynchronize(s->st));  // the host array may be freed after return
+    return WG_OK;
+}
+
+// FP32 scene state from host (phi, psi) rows of H (double or float): both staged
+// contiguously, then phi and the velocity phi - psi formed on the device.  sync: wait for
+// the copies (the host arrays may then be freed).
+template <class H>
+static wg_status upload_state32(wg_scene *s, const H *phi, const H *psi, bool sync)
+{
+    const size_t n = (size_t)s->prm.nx * s->prm.ny, bytes = n * sizeof(H);
+    wg_status st = scene_alloc_dense_stage(s, 2 * bytes);
+    if (st) return st;
+    H *stage = (H *)s->dstage;
+    WG_CUDA(cudaMemcpyAsync(stage, phi, bytes, cudaMemcpyHostToDevice, s->st));
+    WG_CUDA(cudaMemcpyAsync(stage + n, psi, bytes, cudaMemcpyHostToDevice, s->st));
+    launch_state_in32<H>(s->prm.nx, s->prm.ny, s->pitch, stage, stage + n, (float *)s->f[s->cur],
+                         (float *)s->f[1 - s->cur], s->st);
+    s->launches++;
+    WG_CUDA(cudaGetLastError());
+    if (sync) WG_CUDA(cudaStreamSynchronize(s->st));
+    return WG_OK;
+}
+
+// FP32 scene state to host (phi, psi) rows of H; either pointer may be NULL.
+template <class H>
+static wg_status download_state32(wg_scene *s, H *phi, H *psi)
+{
+    const size_t n = (size_t)s->prm.nx * s->prm.ny, bytes = n * sizeof(H);
+    wg_status st = scene_alloc_dense_stage(s, 2 * bytes);
+    if (st) return st;
+    H *stage = (H *)s->dstage;
+    launch_state_out32<H>(s->prm.nx, s->prm.ny, s->pitch, (const float *)s->f[s->cur], (const float *)s->f[1 - s->cur],
+                          phi ? stage : nullptr, psi ? stage + n : nullptr, s->st);
+    s->launches++;
+    WG_CUDA(cudaGetLastError());
+    if (phi) WG_CUDA(cudaMemcpyAsync(phi, stage, bytes, cudaMemcpyDeviceToHost, s->st));
+    if (psi) WG_CUDA(cudaMemcpyAsync(psi, stage + n, bytes, cudaMemcpyDeviceToHost, s->st));
+    WG_CUDA(cudaStreamSynchronize(s->st));
     return WG_OK;
 }
 
@@ -72,7 +110,9 @@ static FastArgs<T> fast_args(wg_scene *s, int do_source)
     FastArgs<T> a;
     a.phi = (const T *)s->f[s->cur];
     a.psi = (const T *)s->f[1 - s->cur];
-    a.out = (T *)s->f[1 - s->cur];
+    const bool pair = sizeof(T) == 4;  // FP32: the new phi and velocity go to the other pair
+    a.out = (T *)(pair ? s->g[0] : s->f[1 - s->cur]);
+    a.vout = pair ? (T *)s->g[1] : nullptr;
     a.act = s->act;
     a.nz = s->nz;
     a.tcc = (const T *)s->tcc;
@@ -105,14 +145,19 @@ static wg_status single_update(wg_scene *s)
     launch_step_fast<T>(s->dp, a, s->coef, s->time, s->st);  // k_step_bulk + k_step_edge
     s->launches += 2;
     if (recs) {
-        launch_neumann_fast<T>(s->dp, a.phi, a.out, s->nidx, s->nw, s->nrec, s->st);
+        launch_neumann_fast<T>(s->dp, a.phi, a.out, a.vout, s->nidx, s->nw, s->nrec, s->st);
         s->launches++;
         if (s->prm.src_on) {
-            launch_point_source<T>(s->dp, a.out, s->time, s->st);
+            launch_point_source<T>(s->dp, a.out, a.vout, s->time, s->st);
             s->launches++;
         }
     }
-    s->cur = 1 - s->cur;
+    if (sizeof(T) == 4) {  // the output pair becomes the scene's state
+        std::swap(s->f[s->cur], s->g[0]);
+        std::swap(s->f[1 - s->cur], s->g[1]);
+    } else {
+        s->cur = 1 - s->cur;
+    }
     return WG_OK;
 }
 
@@ -199,6 +244,8 @@ wg_status wg_scene_create(const wg_params *p, int32_t precision, int32_t coef_mo
     for (int k = 0; k < 2 && e == cudaSuccess; k++) {
         e = cudaMalloc(&s->f[k], fb);
         if (e == cudaSuccess) e = cudaMemsetAsync(s->f[k], 0, fb, s->st);
+        if (e == cudaSuccess && precision == WG_FP32) e = cudaMalloc(&s->g[k], fb);
+        if (e == cudaSuccess && precision == WG_FP32) e = cudaMemsetAsync(s->g[k], 0, fb, s->st);
     }
     if (e == cudaSuccess) e = cudaMalloc(&s->act, mb);
     if (e == cudaSuccess) e = cudaMalloc(&s->nz, mb);
@@ -298,9 +345,13 @@ wg_status wg_scene_upload(wg_scene *s, const double *phi, const double *psi, con
             if ((st = upload_f64(s, tgamma, s->tg))) return st;
         }
     }
-    if ((st = upload_f64(s, phi, s->f[0]))) return st;
-    if ((st = upload_f64(s, psi, s->f[1]))) return st;
     s->cur = 0;
+    if (s->prec == WG_FP32) {
+        if ((st = upload_state32<double>(s, phi, psi, true))) return st;
+    } else {
+        if ((st = upload_f64(s, phi, s->f[0]))) return st;
+        if ((st = upload_f64(s, psi, s->f[1]))) return st;
+    }
     s->time = 0;
     s->uploaded = true;
     s->has_mask = true;
@@ -314,7 +365,12 @@ wg_status wg_scene_upload_state(wg_scene *s, const void *phi, const void *psi, i
     void *dst[2] = {s->f[s->cur], s->f[1 - s->cur]};
     const void *src[2] = {phi, psi};
     if (!s->has_mask) { set_error("upload or build the mask first"); return WG_ERR_STATE; }
+    if (host_precision != WG_FP32 && host_precision != WG_FP64) { set_error("unknown host precision"); return WG_ERR_INVALID; }
     s->uploaded = true;
+    if (s->prec == WG_FP32) {  // stream-ordered for FP32 host rows, as for same-precision copies below
+        if (host_precision == WG_FP32) return upload_state32<float>(s, (const float *)phi, (const float *)psi, false);
+        return upload_state32<double>(s, (const double *)phi, (const double *)psi, true);
+    }
     if (host_precision == s->prec) {
         // contiguous copies (faster over the host link than row-pitched ones) into the dense
         // stage, then a repack into the pitched fields on the device
@@ -347,6 +403,14 @@ wg_status wg_scene_download(wg_scene *s, void *phi, void *psi, int32_t host_prec
 {
     if (!s) { set_error("NULL scene"); return WG_ERR_INVALID; }
     const int nx = s->prm.nx, ny = s->prm.ny;
+    if (s->prec == WG_FP32) {
+        wg_status st;
+        if (host_precision == WG_FP32) st = download_state32<float>(s, (float *)phi, (float *)psi);
+        else if (host_precision == WG_FP64) st = download_state32<double>(s, (double *)phi, (double *)psi);
+        else { set_error("download precision must be FP64 or the scene's"); return WG_ERR_INVALID; }
+        if (st) return st;
+        return scene_check_flag(s);
+    }
     const void *src[2] = {s->f[s->cur], s->f[1 - s->cur]};
     void *dst[2] = {phi, psi};
     for (int k = 0; k < 2; k++) {

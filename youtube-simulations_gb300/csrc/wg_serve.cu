@@ -149,7 +149,7 @@ struct wg_server {
 static uint64_t request_bytes(const wg_server *s, const wg_params &p)
 {
     const BatchLayout L = batch_layout(p, s->cfg.precision);  // the batch's own layout (ghost layout included)
-    const size_t pairs = batch_skew_ok(p, s->cfg.precision) ? 2 : 1;  // skewed scenes keep a second pair
+    const size_t pairs = s->cfg.precision == WG_FP32 ? 2 : 1;  // FP32 scenes keep a second pair
     const size_t fields = 2 * pairs * L.field_bytes, masks = 2 * L.mask_bytes;
     const size_t frame = (size_t)(p.nx / s->cfg.frame.size) * (p.ny / s->cfg.frame.size) * 3;
     return fields + masks + frame + (size_t)p.nx * 40 + 4096;

@@ -2,13 +2,13 @@
 //
 // k_step_tb<COEF>: one CTA owns an extended tile of L rows (i) x W columns (j, W =
 // blockDim.x = 128 or 256; L = 16..64), i.e. a core of (L-2K) x (W-2K) cells plus a
-// halo of K.  Both time levels of the tile sit in shared memory; K in-place leapfrog
-// updates run on the shrinking region [s, L-s) x [s, W-s) (the new level overwrites
-// psi at the cell itself, as in the single-step form, so a sub-step has no hazards),
-// each thread marching down its column with the i+-1 neighbours in a register window
-// (4 shared loads and 1 shared store per cell update).  Then the core of both levels
-// is stored.  HBM traffic per K updates: one read of phi, psi (and the tcc table) over
-// the extended tile and one write of both levels over the core.
+// halo of K.  The tile's phi (two levels, alternating) and velocity sit in shared
+// memory; K leapfrog updates run on the shrinking region [s, L-s) x [s, W-s) (the new
+// phi goes to the other phi level, the velocity is updated in place at the cell itself,
+// so a sub-step has no hazards), each thread marching down its column with the i+-1
+// neighbours in a register window.  Then the core of phi and the velocity is stored.
+// HBM traffic per K updates: one read of phi, the velocity (and the tcc table) over the
+// extended tile and one write of both over the core.
 //
 // The per-cell rules are the reference's (wave_billiard.c:361-590) for the boundary
 // conditions whose stencils stay inside the tile: the mirror "Dirichlet" box edges,
@@ -30,8 +30,8 @@ namespace wg {
 constexpr int TB_AW = 12;  // mask words loaded per tile row (covers 256 + 3*32 columns)
 
 struct TbArgs {
-    const float *phi, *psi;   // levels t, t-1
-    float *phi_out, *psi_out; // levels t+K, t+K-1 (distinct buffers)
+    const float *phi, *psi;   // phi(t) and the velocity phi(t) - phi(t-1)
+    float *phi_out, *psi_out; // the same after the pass (distinct buffers)
     const uint32_t *act;      // active plane
     const float *tcc, *tc;    // tables (WG_COEF_TABLE)
     float c2, c2b, gam, gamb, kappa, ks, kt, gs, gt, vmax, courant, courantb;
@@ -41,35 +41,37 @@ struct TbArgs {
     int *err;                 // set to 1 when a bounded wait gives up
 };
 
-// FP32 value of one boundary-line or point-source cell after update t, with the
-// reference rules for non-wrapping boundaries (wave_billiard.c:393-590): the mirror
+// FP32 phi and velocity of one boundary-line or point-source cell after update t, with
+// the reference rules for non-wrapping boundaries (wave_billiard.c:393-590): the mirror
 // "Dirichlet" edge and OSCILLATE_TOPBOT rows are the bulk update with the missing
 // neighbours replaced by the cell itself, absorbing edges use their inward neighbour,
-// oscillating cells take the precomputed oscillating_bc value.  Returns the old psi
-// value y where the reference writes nothing.
+// oscillating cells take the precomputed oscillating_bc value; keep32 where the
+// reference writes nothing.
 template <int COEF>
-__device__ __forceinline__ float tb_general(const DevParams &p, const TbArgs &a, int gi, int gj, int s, float x,
-                                            float y, float nip, float nim, float njp, float njm, float cc, int act)
+__device__ __forceinline__ XV tb_general(const DevParams &p, const TbArgs &a, int gi, int gj, int s, float x,
+                                         float v, float nip, float nim, float njp, float njm, float cc, int act)
 {
     const float ccv = (COEF == WG_COEF_TABLE) ? cc : (act ? a.c2 : a.c2b);
     const float g = (COEF == WG_COEF_TABLE) ? a.gam : (act ? a.gam : a.gamb);
     const float tcv = (COEF == WG_COEF_TABLE) ? (a.tc ? a.tc[(size_t)gi * p.pitch + gj] : 0.f)
                                               : (act ? a.courant : a.courantb);
     const Edge32K k{a.kappa, a.ks, a.kt, a.gs, a.gt, a.vmax};
-    float v = edge32<true>(p, gi, gj, x, y, nip, nim, njp, njm, ccv, tcv, g, act != 0, k,
-                           [&] { return a.osc[(size_t)(s - 1) * p.ny + gj]; });
-    if (p.src_on && gi == p.src_i && gj == p.src_j) v = (float)A_((double)v, a.src[s - 1]);
-    return v;
+    XV r = edge32<true>(p, gi, gj, x, v, nip, nim, njp, njm, ccv, tcv, g, act != 0, k,
+                        [&] { return a.osc[(size_t)(s - 1) * p.ny + gj]; });
+    if (p.src_on && gi == p.src_i && gj == p.src_j) r = source32(r, a.src[s - 1]);
+    return r;
 }
 
 // One sub-step down this thread's column for a tile with no boundary-line or source
-// cell: rows [s, L-s), the i+-1 neighbours in a register window, shared-memory
-// addressing by constant offsets.  ACT: the cell's mask bit selects coefficients
-// and whether it is written (otherwise every cell is written with its tcc).
+// cell: rows [r0, r1), the i+-1 neighbours in a register window, shared-memory
+// addressing by constant offsets.  P: phi of the previous level; Q: phi of the new
+// level; Vs: the velocity, in place.  ACT: the cell's mask bit selects coefficients and
+// whether it is written (otherwise every cell is written with its tcc).
 template <int COEF, bool ACT>
 __device__ __forceinline__ void tb_rows_interior(const DevParams &p, const TbArgs &a, const float *__restrict__ P,
-                                                 float *__restrict__ Q, const float *__restrict__ Cs, int Bw, int c,
-                                                 int r0, int r1, uint64_t actb)
+                                                 float *__restrict__ Q, float *__restrict__ Vs,
+                                                 const float *__restrict__ Cs, int Bw, int c, int r0, int r1,
+                                                 uint64_t actb)
 {
     int idx = r0 * Bw + c;
     float up = P[idx - Bw], mid = P[idx];
@@ -77,23 +79,24 @@ __device__ __forceinline__ void tb_rows_interior(const DevParams &p, const TbArg
     const int n = r1 - r0;
 #pragma unroll 4
     for (int q = 0; q < n; q++, idx += Bw) {
-        const float dn = P[idx + Bw], e = P[idx + 1], w = P[idx - 1], y = Q[idx];
+        const float dn = P[idx + Bw], e = P[idx + 1], w = P[idx - 1], y = Vs[idx];
         const float delta = ((dn - mid) + (up - mid)) + ((e - mid) + (w - mid));
-        float v;
+        XV r;
         if (!ACT) {
-            v = upd32(mid, y, Cs[idx], delta, a.kappa, a.gam);
+            r = upd32(mid, y, Cs[idx], delta, a.kappa, a.gam);
         } else {
             const bool act = am & 1u;
             am >>= 1;
             const float ccv = (COEF == WG_COEF_TABLE) ? Cs[idx] : (act ? a.c2 : a.c2b);
             const float g = (COEF == WG_COEF_TABLE) ? a.gam : (act ? a.gam : a.gamb);
-            v = y;
+            r = keep32(mid, y);
             if (p.twospeeds || act) {
-                v = upd32(mid, y, ccv, delta, a.kappa, g);
-                if (p.floor_clamp && act) v = fminf(fmaxf(v, -a.vmax), a.vmax);
+                r = upd32(mid, y, ccv, delta, a.kappa, g);
+                if (p.floor_clamp && act) r = clamp32(mid, r, a.vmax);
             }
         }
-        Q[idx] = v;
+        Q[idx] = r.x;
+        Vs[idx] = r.v;
         up = mid;
         mid = dn;
     }
@@ -111,10 +114,11 @@ __global__ void k_boundary_values(const __grid_constant__ DevParams p, long long
     if (p.src_on && idx < n) src[idx] = point_source(p, t0 + idx + 1);
 }
 
-// Shared-memory layout of one tile: F0, F1 (both levels), Cs (tcc, table mode),
-// Aw (the active-plane words covering the tile), one mbarrier.
+// Shared-memory layout of one tile: F0, F1 (phi, alternating levels), Vs (velocity),
+// Cs (tcc, table mode), Aw (the active-plane words covering the tile), one mbarrier.
+// F0, Vs, Cs and Aw are loaded; F1 is written before it is read.
 struct TbLayout {
-    int f0, f1, cs, aw, bar, bytes, tma_bytes;
+    int f0, f1, vs, cs, aw, bar, bytes, tma_bytes;
 };
 __host__ __device__ inline TbLayout tb_layout(int coef, int L, int Bw)
 {
@@ -122,8 +126,9 @@ __host__ __device__ inline TbLayout tb_layout(int coef, int L, int Bw)
     const int fb = L * Bw * 4;
     t.f0 = 0;
     t.f1 = fb;
-    t.cs = 2 * fb;
-    t.aw = (coef == WG_COEF_TABLE ? 3 : 2) * fb;
+    t.vs = 2 * fb;
+    t.cs = 3 * fb;
+    t.aw = (coef == WG_COEF_TABLE ? 4 : 3) * fb;
     t.bar = t.aw + ((L * TB_AW * 4 + 15) / 16) * 16;
     t.bytes = t.bar + 16;
     t.tma_bytes = (coef == WG_COEF_TABLE ? 3 : 2) * fb + L * TB_AW * 4;
@@ -140,7 +145,8 @@ __global__ void __launch_bounds__(256) k_step_tb(const __grid_constant__ DevPara
     extern __shared__ __align__(1024) unsigned char smem[];
     const int Bw = blockDim.x;
     const TbLayout lay = tb_layout(COEF, L, Bw);
-    float *F0 = (float *)(smem + lay.f0), *F1 = (float *)(smem + lay.f1), *Cs = (float *)(smem + lay.cs);
+    float *F0 = (float *)(smem + lay.f0), *F1 = (float *)(smem + lay.f1), *Vs = (float *)(smem + lay.vs),
+          *Cs = (float *)(smem + lay.cs);
     const uint32_t *Aw = (const uint32_t *)(smem + lay.aw);
     uint64_t *bar = (uint64_t *)(smem + lay.bar);
     const int c = threadIdx.x;
@@ -157,7 +163,7 @@ __global__ void __launch_bounds__(256) k_step_tb(const __grid_constant__ DevPara
         if (c == 0) atomicExch(a.err, 2);
         return;
     }
-    // TMA: the extended tile of phi, psi (tcc) and the mask words, zero outside the grid
+    // TMA: the extended tile of phi, the velocity (tcc) and the mask words, zero outside the grid
     if (c == 0) {
         mbar_init(bar, 1);
         mbar_fence_init();
@@ -166,7 +172,7 @@ __global__ void __launch_bounds__(256) k_step_tb(const __grid_constant__ DevPara
     if (c == 0) {
         mbar_arrive_expect_tx(bar, (unsigned)lay.tma_bytes);
         tma_load_2d(F0, &m_phi, x0, gi0, bar);
-        tma_load_2d(F1, &m_psi, x0, gi0, bar);
+        tma_load_2d(Vs, &m_psi, x0, gi0, bar);
         if (COEF == WG_COEF_TABLE) tma_load_2d(Cs, &m_tcc, x0, gi0, bar);
         tma_load_2d((void *)Aw, &m_act, w0, gi0, bar);
     }
@@ -191,13 +197,13 @@ __global__ void __launch_bounds__(256) k_step_tb(const __grid_constant__ DevPara
     const bool no_act = COEF == WG_COEF_TABLE && p.twospeeds && !p.floor_clamp;
 
     for (int s = 1; s <= K; s++) {
-        const float *P = (s & 1) ? F0 : F1;  // phi level t+s-1
-        float *Q = (s & 1) ? F1 : F0;        // psi level t+s-2, becomes level t+s
+        const float *P = (s & 1) ? F0 : F1;  // phi of level t+s-1
+        float *Q = (s & 1) ? F1 : F0;        // phi of level t+s-2, becomes level t+s
         const bool in_region = c >= Kh - K + s && c < Bw - Kh + K - s;
         if (interior_tile) {
             if (in_region) {
-                if (no_act) tb_rows_interior<COEF, false>(p, a, P, Q, Cs, Bw, c, s, L - s, actb);
-                else tb_rows_interior<COEF, true>(p, a, P, Q, Cs, Bw, c, s, L - s, actb);
+                if (no_act) tb_rows_interior<COEF, false>(p, a, P, Q, Vs, Cs, Bw, c, s, L - s, actb);
+                else tb_rows_interior<COEF, true>(p, a, P, Q, Vs, Cs, Bw, c, s, L - s, actb);
             }
         } else if (col_ok && in_region && !col_special) {
             // a boundary tile, interior column: lean segments between the special rows
@@ -208,19 +214,20 @@ __global__ void __launch_bounds__(256) k_step_tb(const __grid_constant__ DevPara
             int r = lo;
             while (r < hi) {
                 if (r == ra || r == rb || r == rs) {
-                    const int gi = gi0 + r;
-                    const float cc = (COEF == WG_COEF_TABLE) ? Cs[r * Bw + c] : 0.f;
-                    Q[r * Bw + c] = tb_general<COEF>(p, a, gi, gj, s, P[r * Bw + c], Q[r * Bw + c], P[(r + 1) * Bw + c],
-                                                     P[(r - 1) * Bw + c], P[r * Bw + c + 1], P[r * Bw + c - 1], cc,
-                                                     (int)((actb >> r) & 1u));
+                    const int gi = gi0 + r, o = r * Bw + c;
+                    const float cc = (COEF == WG_COEF_TABLE) ? Cs[o] : 0.f;
+                    const XV res = tb_general<COEF>(p, a, gi, gj, s, P[o], Vs[o], P[o + Bw], P[o - Bw], P[o + 1],
+                                                    P[o - 1], cc, (int)((actb >> r) & 1u));
+                    Q[o] = res.x;
+                    Vs[o] = res.v;
                     r++;
                 } else {
                     int nxt = hi;
                     if (ra > r && ra < nxt) nxt = ra;
                     if (rb > r && rb < nxt) nxt = rb;
                     if (rs > r && rs < nxt) nxt = rs;
-                    if (no_act) tb_rows_interior<COEF, false>(p, a, P, Q, Cs, Bw, c, r, nxt, actb);
-                    else tb_rows_interior<COEF, true>(p, a, P, Q, Cs, Bw, c, r, nxt, actb);
+                    if (no_act) tb_rows_interior<COEF, false>(p, a, P, Q, Vs, Cs, Bw, c, r, nxt, actb);
+                    else tb_rows_interior<COEF, true>(p, a, P, Q, Vs, Cs, Bw, c, r, nxt, actb);
                     r = nxt;
                 }
             }
@@ -232,20 +239,22 @@ __global__ void __launch_bounds__(256) k_step_tb(const __grid_constant__ DevPara
                 const float dn = P[(r + 1) * Bw + c];
                 const int gi = gi0 + r;
                 if (gi >= 0 && gi < p.nx) {
-                    const float e = P[r * Bw + c + 1], w = P[r * Bw + c - 1];
-                    const float y = Q[r * Bw + c];
-                    const float cc = (COEF == WG_COEF_TABLE) ? Cs[r * Bw + c] : 0.f;
+                    const int o = r * Bw + c;
+                    const float e = P[o + 1], w = P[o - 1];
+                    const float y = Vs[o];
+                    const float cc = (COEF == WG_COEF_TABLE) ? Cs[o] : 0.f;
                     const int act = (int)((actb >> r) & 1u);
-                    float v = y;
+                    XV res = keep32(mid, y);
                     if (col_special || gi == 0 || gi == p.nx - 1 || (p.src_on && gi == p.src_i && gj == p.src_j)) {
-                        v = tb_general<COEF>(p, a, gi, gj, s, mid, y, dn, up, e, w, cc, act);
+                        res = tb_general<COEF>(p, a, gi, gj, s, mid, y, dn, up, e, w, cc, act);
                     } else if (p.twospeeds || act) {
                         const float ccv = (COEF == WG_COEF_TABLE) ? cc : (act ? a.c2 : a.c2b);
                         const float g = (COEF == WG_COEF_TABLE) ? a.gam : (act ? a.gam : a.gamb);
-                        v = upd32(mid, y, ccv, ((dn - mid) + (up - mid)) + ((e - mid) + (w - mid)), a.kappa, g);
-                        if (p.floor_clamp && act) v = fminf(fmaxf(v, -a.vmax), a.vmax);
+                        res = upd32(mid, y, ccv, ((dn - mid) + (up - mid)) + ((e - mid) + (w - mid)), a.kappa, g);
+                        if (p.floor_clamp && act) res = clamp32(mid, res, a.vmax);
                     }
-                    Q[r * Bw + c] = v;
+                    Q[o] = res.x;
+                    Vs[o] = res.v;
                 }
                 up = mid;
                 mid = dn;
@@ -254,54 +263,55 @@ __global__ void __launch_bounds__(256) k_step_tb(const __grid_constant__ DevPara
         __syncthreads();
     }
 
-    // store the core: level t+K and t+K-1
+    // store the core: phi of level t+K and the velocity
     if (col_ok && c >= Kh && c < Bw - Kh) {
-        const float *newest = (K & 1) ? F1 : F0, *prev = (K & 1) ? F0 : F1;
+        const float *newest = (K & 1) ? F1 : F0;
 #pragma unroll 4
         for (int r = K; r < L - K; r++) {
             const int gi = gi0 + r;
             if (gi < p.nx) {
                 const size_t o = (size_t)gi * p.pitch + gj;
                 a.phi_out[o] = newest[r * Bw + c];
-                a.psi_out[o] = prev[r * Bw + c];
+                a.psi_out[o] = Vs[r * Bw + c];
             }
         }
     }
 }
 
-// One FP32 cell of level s at (gi, gj) from level s-1 (x, its neighbours n = i+1,
-// sv = i-1, e = j+1, w = j-1) and level s-2 (y).  cc is the cell's tcc, tcv its tc (table
-// mode).  GEN = false: a cell off the boundary lines and the source; PLAIN additionally
-// promises twospeeds and no FLOOR clamp, so every such cell takes the leapfrog update.
-// INL: oscillating values and source increments are computed here (batches) instead of
-// read from the per-call arrays; both are the same double values, rounded the same way.
+// One FP32 cell of level s at (gi, gj) from level s-1 (phi x, its neighbours n = i+1,
+// sv = i-1, e = j+1, w = j-1, and the velocity y).  cc is the cell's tcc, tcv its tc
+// (table mode).  GEN = false: a cell off the boundary lines and the source; PLAIN
+// additionally promises twospeeds and no FLOOR clamp, so every such cell takes the
+// leapfrog update.  INL: oscillating values and source increments are computed here
+// (batches) instead of read from the per-call arrays; both are the same double values,
+// rounded the same way.
 // Out of line: they are rare, and inlined copies per level would crowd the instruction cache.
 __device__ __noinline__ float osc_inl(const DevParams &p, long long t, int j) { return (float)osc_bc(p, (int)t, j); }
 __device__ __noinline__ double src_inl(const DevParams &p, long long t) { return point_source(p, t); }
 
 template <int COEF, bool GEN, bool PLAIN, bool INL = false, bool KZ = false>
-__device__ __forceinline__ float skew_cell(const DevParams &p, const TbArgs &a, int gi, int gj, int s, float x, float y,
-                                           float n, float sv, float e, float w, float cc, float tcv, bool act)
+__device__ __forceinline__ XV skew_cell(const DevParams &p, const TbArgs &a, int gi, int gj, int s, float x, float y,
+                                        float n, float sv, float e, float w, float cc, float tcv, bool act)
 {
     const float ccv = (COEF == WG_COEF_TABLE) ? cc : (act ? a.c2 : a.c2b);
     const float g = (COEF == WG_COEF_TABLE) ? a.gam : (act ? a.gam : a.gamb);
     if (!GEN && PLAIN && KZ) return upd32_k0(x, y, ccv, ((n - x) + (sv - x)) + ((e - x) + (w - x)), g);
     if (!GEN && PLAIN) return upd32(x, y, ccv, ((n - x) + (sv - x)) + ((e - x) + (w - x)), a.kappa, g);
     if (!GEN) {
-        float v = y;
+        XV r = keep32(x, y);
         if (p.twospeeds || act) {
-            v = upd32(x, y, ccv, ((n - x) + (sv - x)) + ((e - x) + (w - x)), a.kappa, g);
-            if (p.floor_clamp && act) v = fminf(fmaxf(v, -a.vmax), a.vmax);
+            r = upd32(x, y, ccv, ((n - x) + (sv - x)) + ((e - x) + (w - x)), a.kappa, g);
+            if (p.floor_clamp && act) r = clamp32(x, r, a.vmax);
         }
-        return v;
+        return r;
     }
     const float tce = (COEF == WG_COEF_TABLE) ? tcv : (act ? a.courant : a.courantb);
     const Edge32K k{a.kappa, a.ks, a.kt, a.gs, a.gt, a.vmax};
-    float v = edge32<true>(p, gi, gj, x, y, n, sv, e, w, ccv, tce, g, act, k, [&] {
+    XV r = edge32<true>(p, gi, gj, x, y, n, sv, e, w, ccv, tce, g, act, k, [&] {
         return INL ? osc_inl(p, a.t0 + s, gj) : a.osc[(size_t)(s - 1) * p.ny + gj];
     });
-    if (p.src_on && gi == p.src_i && gj == p.src_j) v = (float)A_((double)v, INL ? src_inl(p, a.t0 + s) : a.src[s - 1]);
-    return v;
+    if (p.src_on && gi == p.src_i && gj == p.src_j) r = source32(r, INL ? src_inl(p, a.t0 + s) : a.src[s - 1]);
+    return r;
 }
 
 
@@ -310,34 +320,35 @@ __device__ __forceinline__ float skew_cell(const DevParams &p, const TbArgs &a, 
 // symmetric, so w - x == -(x - w)), and a lane's four cells share the five differences
 // of its row, 5 subtractions instead of 8.
 template <int COEF, bool PLAIN, bool KZ = false>
-__device__ __forceinline__ float skew_inner(const DevParams &p, const TbArgs &a, float x, float y, float n, float sv,
-                                            float he, float hw, float cc, bool act)
+__device__ __forceinline__ XV skew_inner(const DevParams &p, const TbArgs &a, float x, float y, float n, float sv,
+                                         float he, float hw, float cc, bool act)
 {
     const float ccv = (COEF == WG_COEF_TABLE) ? cc : (act ? a.c2 : a.c2b);
     const float g = (COEF == WG_COEF_TABLE) ? a.gam : (act ? a.gam : a.gamb);
     const float lap = ((n - x) + (sv - x)) + (he - hw);
     if (PLAIN && KZ) return upd32_k0(x, y, ccv, lap, g);
     if (PLAIN) return upd32(x, y, ccv, lap, a.kappa, g);
-    float v = y;
+    XV r = keep32(x, y);
     if (p.twospeeds || act) {
-        v = upd32(x, y, ccv, lap, a.kappa, g);
-        if (p.floor_clamp && act) v = fminf(fmaxf(v, -a.vmax), a.vmax);
+        r = upd32(x, y, ccv, lap, a.kappa, g);
+        if (p.floor_clamp && act) r = clamp32(x, r, a.vmax);
     }
-    return v;
+    return r;
 }
 
 // ---------------------------------------------------------------------------
 // Time-skewed streaming (k_step_skew): every warp owns a tile of 128 columns (four
 // adjacent columns j per lane, loaded as float4; a column halo of H = K rounded up to 4
 // on each side) and a strip of S rows (i), and marches down the strip once.  At input
-// row m it computes level s at row m - s for s = 1..K (level 0 = phi(t), level -1 =
-// psi(t-1)), so each level keeps only a window of three rows in registers.  Column
-// neighbours inside a lane are registers; across lanes they are one warp shuffle each
-// way.  Input rows are prefetched QD rows ahead through a per-warp shared-memory ring;
-// table scenes also keep the tcc values of the last K+1 rows in a second small ring.
-// One row per loop trip (SKEW_UNROLL): longer trips turn the window rotation into
-// register renaming but miss the instruction cache.  Core columns [H, 128-H) store level
-// K (new phi) and level K-1 (new psi) of the rows in the strip.
+// row m it computes level s at row m - s for s = 1..K (level 0 = phi(t) and its
+// velocity), so each level keeps only a window of three phi rows and one velocity row in
+// registers (plus the new velocity row of the level just computed, held until the next
+// level has read the row it replaces).  Column neighbours inside a lane are registers;
+// across lanes they are one warp shuffle each way.  Input rows are prefetched QD rows
+// ahead through a per-warp shared-memory ring; table scenes also keep the tcc values of
+// the last K+1 rows in a second small ring.  One row per loop trip (SKEW_UNROLL): longer
+// trips turn the window rotation into register renaming but miss the instruction cache.
+// Core columns [H, 128-H) store phi and the velocity of level K for the rows in the strip.
 //
 // Tiles that reach an edge row or column or hold the point source (edge tiles) take three
 // extra steps after the common update: the lane holding column 0 or ny-1 redoes that
@@ -354,8 +365,8 @@ __device__ __forceinline__ float pick4(float a0, float a1, float a2, float a3, i
 // evolve_wave_half for the top/bottom lines (wave_billiard.c:366-452, B_COND Dirichlet or
 // absorbing, OSCILLATE_TOPBOT), same branches as skew_cell's general form.
 template <int COEF>
-__device__ __forceinline__ float col_edge_cell(const DevParams &p, const TbArgs &a, int gi, float x, float y, float n,
-                                               float sv, float e, float w, float cc, float tcv, bool act, bool right)
+__device__ __forceinline__ XV col_edge_cell(const DevParams &p, const TbArgs &a, int gi, float x, float y, float n,
+                                            float sv, float e, float w, float cc, float tcv, bool act, bool right)
 {
     const float ccv = (COEF == WG_COEF_TABLE) ? cc : (act ? a.c2 : a.c2b);
     const float g = (COEF == WG_COEF_TABLE) ? a.gam : (act ? a.gam : a.gamb);
@@ -368,15 +379,15 @@ __device__ __forceinline__ float col_edge_cell(const DevParams &p, const TbArgs 
     } else {
         mode = 1;
     }
-    float v = y;
+    XV r = keep32(x, y);
     if (p.twospeeds || act) {
         if (mode == 0)
-            v = upd32(x, y, ccv, ((n - x) + (sv - x)) + ((e - x) + (w - x)), a.kappa, g);
+            r = upd32(x, y, ccv, ((n - x) + (sv - x)) + ((e - x) + (w - x)), a.kappa, g);
         else
-            v = absorb32(x, y, (COEF == WG_COEF_TABLE) ? tcv : (act ? a.courant : a.courantb), right ? w : e, a.kt, a.gt);
-        if (p.floor_clamp && act) v = fminf(fmaxf(v, -a.vmax), a.vmax);
+            r = absorb32(x, y, (COEF == WG_COEF_TABLE) ? tcv : (act ? a.courant : a.courantb), right ? w : e, a.kt, a.gt);
+        if (p.floor_clamp && act) r = clamp32(x, r, a.vmax);
     }
-    return v;
+    return r;
 }
 
 // Asynchronous global->shared copies of one lane's 16 (or 4) bytes; with src_bytes 0
@@ -434,8 +445,12 @@ __device__ __forceinline__ void skew_strip(const DevParams &p, const TbArgs &a, 
     const int ce = !edge ? -1 : (gj0 == 0 ? 0 : (cr >= 0 && cr <= 3 ? cr : -1));
     const bool src_lane = edge && p.src_on && p.src_j >= gj0 && p.src_j < gj0 + 4;
 
-    float W[K + 1][3][4];  // W[s][k][c] = level s at row m-s-2+k, column gj0+c
-    float Yp[4];           // psi(t-1) at row m-1
+    float W[K + 1][3][4];  // W[s][k][c] = phi of level s at row m-s-2+k, column gj0+c
+    // V[s][c] = velocity of level s at row m-s-1, column gj0+c, until level s+1 of the trip
+    // for row m has read it; pend[c] = the new velocity row of the level just computed.
+    // (Kept in a per-warp shared-memory row per level instead, the single-grid pass ran as
+    // fast at its best depth and the batch passes 8% slower.)
+    float V[K][4], pend[4];
     // tcc at rows m, m-1, ..., m-K (table scenes): the warp's shared ring tring of K+1 rows
     // (slot ts holds row m), each lane writing and reading back only its own 16 bytes
     int ts = 0;
@@ -444,11 +459,12 @@ __device__ __forceinline__ void skew_strip(const DevParams &p, const TbArgs &a, 
 #pragma unroll
     for (int q = 0; q <= K; q++) {
 #pragma unroll
-        for (int c = 0; c < 4; c++) { W[q][0][c] = W[q][1][c] = W[q][2][c] = 0.f; }
+        for (int c = 0; c < 4; c++) {
+            W[q][0][c] = W[q][1][c] = W[q][2][c] = 0.f;
+            if (q < K) V[q][c] = 0.f;
+        }
         TE[q] = 0.f;
     }
-#pragma unroll
-    for (int c = 0; c < 4; c++) Yp[c] = 0.f;
 
     // row m goes to slot (m - m0) % D; each lane copies, and later reads, only its own bytes
     auto issue = [&](int m, int slot) {
@@ -495,14 +511,12 @@ __device__ __forceinline__ void skew_strip(const DevParams &p, const TbArgs &a, 
             // the slot of row m-1 (read in the previous row) takes row m+QD
             issue(m + QD, slot == 0 ? D - 1 : slot - 1);
             slot = (slot == D - 1) ? 0 : slot + 1;
-            float ylev1[4];
 #pragma unroll
             for (int c = 0; c < 4; c++) {
                 W[0][0][c] = W[0][1][c];
                 W[0][1][c] = W[0][2][c];
                 W[0][2][c] = xin[c];
-                ylev1[c] = Yp[c];
-                Yp[c] = yin[c];
+                pend[c] = yin[c];
             }
             if (need_tce) {  // warp-uniform: only tiles that hold a boundary column read TE
 #pragma unroll
@@ -512,13 +526,13 @@ __device__ __forceinline__ void skew_strip(const DevParams &p, const TbArgs &a, 
 #pragma unroll
             for (int lv = 1; lv <= K; lv++) {
                 const int r = m - lv;  // row of this level's new value
-                float v[4] = {0.f, 0.f, 0.f, 0.f};
+                XV v[4] = {{0.f, 0.f}, {0.f, 0.f}, {0.f, 0.f}, {0.f, 0.f}};
                 // Level lv at row r reaches the stored rows only from r >= i_s - K + lv on, i.e.
                 // from input row m0 + 2 lv + 1: in the pipeline fill the earlier levels are skipped
                 // (warp-uniform), and their window slots hold zeros that nothing reads.
                 if (m - m0 >= 2 * lv + 1) {
                 const float *Wc = W[lv - 1][1];
-                const float *Yl = (lv == 1) ? ylev1 : W[lv - 2 >= 0 ? lv - 2 : 0][0];
+                const float *Yl = V[lv - 1];  // velocity of level lv-1 at row r
                 float Tl[4] = {0.f, 0.f, 0.f, 0.f};  // tcc at row r
                 if (COEF == WG_COEF_TABLE) {
                     const int tsl = ts >= lv ? ts - lv : ts - lv + K + 1;
@@ -541,7 +555,7 @@ __device__ __forceinline__ void skew_strip(const DevParams &p, const TbArgs &a, 
                 if (!GEN && edge) {  // warp-uniform
                     if (ce >= 0 && r > 0 && r < p.nx - 1) {  // the lane holding column 0 (c = 0) or ny-1 (c = 3)
                         const bool lf = ce == 0;
-                        const float res = col_edge_cell<COEF>(
+                        const XV res = col_edge_cell<COEF>(
                             p, a, r, lf ? Wc[0] : Wc[3], lf ? Yl[0] : Yl[3], lf ? W[lv - 1][2][0] : W[lv - 1][2][3],
                             lf ? W[lv - 1][0][0] : W[lv - 1][0][3], lf ? Wc[1] : e3, lf ? w0 : Wc[2],
                             lf ? Tl[0] : Tl[3], TE[lv], NEED_ACT ? ((aq >> (4 * lv + ce)) & 1u) : true, !lf);
@@ -552,13 +566,13 @@ __device__ __forceinline__ void skew_strip(const DevParams &p, const TbArgs &a, 
                         const double add = INL ? src_inl(p, a.t0 + lv) : a.src[lv - 1];
                         const int cs = p.src_j - gj0;
 #pragma unroll
-                        for (int c = 0; c < 4; c++) v[c] = (cs == c) ? (float)A_((double)v[c], add) : v[c];
+                        for (int c = 0; c < 4; c++) v[c] = (cs == c) ? source32(v[c], add) : v[c];
                     }
                 }
                 if (GEN) {
                     const bool row_edge = r == 0 || r == p.nx - 1;  // warp-uniform
                     if (ce >= 0 && r > 0 && r < p.nx - 1) {  // the lane holding column 0 or ny-1: picked by index
-                        const float res = col_edge_cell<COEF>(
+                        const XV res = col_edge_cell<COEF>(
                             p, a, r, pick4(Wc[0], Wc[1], Wc[2], Wc[3], ce), pick4(Yl[0], Yl[1], Yl[2], Yl[3], ce),
                             pick4(W[lv - 1][2][0], W[lv - 1][2][1], W[lv - 1][2][2], W[lv - 1][2][3], ce),
                             pick4(W[lv - 1][0][0], W[lv - 1][0][1], W[lv - 1][0][2], W[lv - 1][0][3], ce),
@@ -576,7 +590,7 @@ __device__ __forceinline__ void skew_strip(const DevParams &p, const TbArgs &a, 
                             const int gj = gj0 + c;
                             if (gj < 0 || gj >= p.ny) continue;
                             const float tcv = (COEF == WG_COEF_TABLE && a.tc) ? a.tc[(size_t)r * p.pitch + gj] : 0.f;
-                            const float res = skew_cell<COEF, true, false, INL>(
+                            const XV res = skew_cell<COEF, true, false, INL>(
                                 p, a, r, gj, lv, pick4(Wc[0], Wc[1], Wc[2], Wc[3], c), pick4(Yl[0], Yl[1], Yl[2], Yl[3], c),
                                 pick4(W[lv - 1][2][0], W[lv - 1][2][1], W[lv - 1][2][2], W[lv - 1][2][3], c),
                                 pick4(W[lv - 1][0][0], W[lv - 1][0][1], W[lv - 1][0][2], W[lv - 1][0][3], c),
@@ -592,7 +606,7 @@ __device__ __forceinline__ void skew_strip(const DevParams &p, const TbArgs &a, 
                         const double add = INL ? src_inl(p, a.t0 + lv) : a.src[lv - 1];
                         const int cs = p.src_j - gj0;
 #pragma unroll
-                        for (int c = 0; c < 4; c++) v[c] = (cs == c) ? (float)A_((double)v[c], add) : v[c];
+                        for (int c = 0; c < 4; c++) v[c] = (cs == c) ? source32(v[c], add) : v[c];
                     }
                 }
                 }  // levels in use
@@ -600,7 +614,9 @@ __device__ __forceinline__ void skew_strip(const DevParams &p, const TbArgs &a, 
                 for (int c = 0; c < 4; c++) {
                     W[lv][0][c] = W[lv][1][c];
                     W[lv][1][c] = W[lv][2][c];
-                    W[lv][2][c] = v[c];
+                    W[lv][2][c] = v[c].x;
+                    V[lv - 1][c] = pend[c];  // level lv-1's row r+1: level lv has read row r
+                    pend[c] = v[c].v;
                 }
             }
             ts = (ts == K) ? 0 : ts + 1;  // row m+1's tcc slot
@@ -610,15 +626,14 @@ __device__ __forceinline__ void skew_strip(const DevParams &p, const TbArgs &a, 
                 if (gj0 + 3 < p.ny) {
                     if (grp_ok) {
                         *reinterpret_cast<float4 *>(a.phi_out + o) = make_float4(W[K][2][0], W[K][2][1], W[K][2][2], W[K][2][3]);
-                        *reinterpret_cast<float4 *>(a.psi_out + o) =
-                            make_float4(W[K - 1][1][0], W[K - 1][1][1], W[K - 1][1][2], W[K - 1][1][3]);
+                        *reinterpret_cast<float4 *>(a.psi_out + o) = make_float4(pend[0], pend[1], pend[2], pend[3]);
                     }
                 } else if (grp_ok) {
 #pragma unroll
                     for (int c = 0; c < 4; c++)
                         if (gj0 + c < p.ny) {
                             a.phi_out[o + c] = W[K][2][c];
-                            a.psi_out[o + c] = W[K - 1][1][c];
+                            a.psi_out[o + c] = pend[c];
                         }
                 }
             }
@@ -855,10 +870,10 @@ __global__ void __launch_bounds__(128, 4) k_batch_skew(const SlotDev *__restrict
         }
         __syncwarp();
         const SlotDyn dy = dyn[sd.slot];
-        const int pin = dy.pair ^ (q & 1), cin = q == 0 ? dy.cur : 0, pout = pin ^ 1;
+        const int pin = dy.pair ^ (q & 1), pout = pin ^ 1;
         TbArgs a;
-        a.phi = (const float *)sd.f[2 * pin + cin];
-        a.psi = (const float *)sd.f[2 * pin + 1 - cin];
+        a.phi = (const float *)sd.f[2 * pin];
+        a.psi = (const float *)sd.f[2 * pin + 1];
         a.phi_out = (float *)sd.f[2 * pout];
         a.psi_out = (float *)sd.f[2 * pout + 1];
         a.act = sd.act;
@@ -890,10 +905,17 @@ __global__ void __launch_bounds__(128, 4) k_batch_skew(const SlotDev *__restrict
     }
 }
 
+// dynamic shared memory of k_batch_skew: 4 warps x row ring
+template <int K>
+constexpr size_t batch_skew_smem()
+{
+    return 4 * SkewSlot<WG_COEF_MASK>::DEPTH * SkewSlot<WG_COEF_MASK>::SIZE * sizeof(float);
+}
+
 template <int K>
 static int batch_skew_cap_k()
 {
-    constexpr size_t smem = 4 * SkewSlot<WG_COEF_MASK>::DEPTH * SkewSlot<WG_COEF_MASK>::SIZE * sizeof(float);
+    constexpr size_t smem = batch_skew_smem<K>();
     static int per_sm = 0;
     if (!per_sm) {
         cudaFuncSetAttribute(k_batch_skew<K>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
@@ -926,14 +948,13 @@ int batch_skew_capacity(int K)
 void launch_batch_skew(int K, const SlotDev *tab, const SlotDyn *dyn, const int4 *tasks, const int *ntasks, int *ticket,
                        int q, int toff, cudaStream_t st)
 {
-    constexpr size_t smem = 4 * SkewSlot<WG_COEF_MASK>::DEPTH * SkewSlot<WG_COEF_MASK>::SIZE * sizeof(float);
     const int blocks = std::max(1, batch_skew_capacity(K) / 4);
     switch (K) {
-    case 2: k_batch_skew<2><<<blocks, 128, smem, st>>>(tab, dyn, tasks, ntasks, ticket, q, toff); break;
-    case 3: k_batch_skew<3><<<blocks, 128, smem, st>>>(tab, dyn, tasks, ntasks, ticket, q, toff); break;
-    case 4: k_batch_skew<4><<<blocks, 128, smem, st>>>(tab, dyn, tasks, ntasks, ticket, q, toff); break;
-    case 5: k_batch_skew<5><<<blocks, 128, smem, st>>>(tab, dyn, tasks, ntasks, ticket, q, toff); break;
-    case 6: k_batch_skew<6><<<blocks, 128, smem, st>>>(tab, dyn, tasks, ntasks, ticket, q, toff); break;
+    case 2: k_batch_skew<2><<<blocks, 128, batch_skew_smem<2>(), st>>>(tab, dyn, tasks, ntasks, ticket, q, toff); break;
+    case 3: k_batch_skew<3><<<blocks, 128, batch_skew_smem<3>(), st>>>(tab, dyn, tasks, ntasks, ticket, q, toff); break;
+    case 4: k_batch_skew<4><<<blocks, 128, batch_skew_smem<4>(), st>>>(tab, dyn, tasks, ntasks, ticket, q, toff); break;
+    case 5: k_batch_skew<5><<<blocks, 128, batch_skew_smem<5>(), st>>>(tab, dyn, tasks, ntasks, ticket, q, toff); break;
+    case 6: k_batch_skew<6><<<blocks, 128, batch_skew_smem<6>(), st>>>(tab, dyn, tasks, ntasks, ticket, q, toff); break;
     default: break;
     }
 }
