@@ -211,6 +211,8 @@ typedef struct wg_scene wg_scene;
 
 /* Creates a scene with device buffers for phi/psi, the packed mask and coefficients.
  * precision: WG_FP64 or WG_FP32.  coef_mode: WG_COEF_MASK or WG_COEF_TABLE.
+ * An FP32 scene stores phi and the velocity phi - psi (each rounded once from FP64
+ * values), in two pairs of fields: every update writes the other pair.
  * stream: cudaStream_t to run on (NULL = a stream owned by the scene).
  * FP64 scenes give the values of the reference's stepper (evolve_wave_half,
  * wave_billiard.c:302-610).  Where KAPPA = 0, or GAMMA is 0 on every cell, the zero
@@ -224,7 +226,7 @@ wg_status wg_scene_bytes(const wg_params *p, int32_t precision, int32_t coef_mod
 
 /* Uploads flat [nx][ny] FP64 host arrays (j contiguous).  xy_in is the reference's
  * short mask.  tcc/tc/tgamma may be NULL in WG_COEF_MASK mode.  Values are rounded
- * to the scene precision on the device. */
+ * to the scene precision on the device (FP32: phi and the FP64 difference phi - psi). */
 wg_status wg_scene_upload(wg_scene *s, const double *phi, const double *psi, const int16_t *xy_in,
                           const double *tcc, const double *tc, const double *tgamma);
 /* Uploads only phi/psi (the state), from FP64 or from the scene's own precision. */
@@ -233,7 +235,8 @@ wg_status wg_scene_set_neumann(wg_scene *s, const wg_neumann_bc *recs, int32_t n
 /* Advances nsteps leapfrog updates (one kernel pass per temporal block). */
 wg_status wg_scene_step(wg_scene *s, int32_t nsteps);
 /* Copies phi (time t) and psi (time t-1) to flat host arrays in FP64 or the scene's
- * precision.  Either pointer may be NULL. */
+ * precision.  Either pointer may be NULL.  FP32 scenes return psi = phi - v computed in
+ * FP64 (rounded to FP32 for an FP32 host array). */
 wg_status wg_scene_download(wg_scene *s, void *phi, void *psi, int32_t host_precision);
 /* Energy diagnostics (compute_energy per cell, wave_common.c:453-472) with compensated
  * sums: FP64 Neumaier accumulators for FP64 fields; for FP32 fields (cell energies in

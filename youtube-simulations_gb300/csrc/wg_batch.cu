@@ -630,11 +630,11 @@ static void batch_enqueue_frame(wg_batch *b, int n, bool skewed)
                                                           sizeof(T) == 4 ? 1 : 0);
 }
 
-// Depth and row chunk per size class, in two stages: depths 2..6 with the list-wide
+// Depth and row chunk per size class, in two stages: depths 2..4 with the list-wide
 // chunk, then chunks of 32, 64, 128 and 256 rows at the best depth.  Each candidate
 // times one skewed pass over the class's scenes (reading their current fields, writing
 // the other pair, so the state does not change), best of five after one untimed pass;
-// the fastest per update is kept.  Nine candidates per class keep the tuning frame of a
+// the fastest per update is kept.  Seven candidates per class keep the tuning frame of a
 // server tick short.
 // Tuned classes are kept for the process, keyed by device, size class and the kinds of
 // scene in the class (their boundary conditions, the ghost layout, two speeds): a later
@@ -708,7 +708,9 @@ static wg_status batch_autotune(wg_batch *b)
         int4 *dev = nullptr;
         cudaError_t err = cudaSuccess;
         static const int ROWS[] = {32, 64, 128, 256};
-        const int ndepth = WG_SKEW_MAX_K - 1;
+        // depths 2..4: at 5 and 6 the velocity rows push the pass past its 128 registers
+        // (spills) and those depths measured slower on every size class tried
+        const int ndepth = 3;
         for (int cand = 0; cand < ndepth + 4 && err == cudaSuccess; cand++) {
             const int K = cand < ndepth ? 2 + cand : best, R = cand < ndepth ? 0 : ROWS[cand - ndepth];
             std::vector<int4> tasks;
