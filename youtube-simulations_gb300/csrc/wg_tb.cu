@@ -315,17 +315,19 @@ __device__ __forceinline__ XV skew_cell(const DevParams &p, const TbArgs &a, int
 }
 
 
-// skew_cell's inner rule (GEN = false) with the horizontal part of the Laplacian given
-// as he = e - x and hw = x - w: (e - x) + (w - x) == he - hw exactly (round to nearest is
-// symmetric, so w - x == -(x - w)), and a lane's four cells share the five differences
-// of its row, 5 subtractions instead of 8.
+// skew_cell's inner rule (GEN = false) with the Laplacian given in differences.  Vertical:
+// vert = dn - dp with dn = n - x and dp = x - sv, which equals (n - x) + (sv - x) exactly
+// (round to nearest is symmetric, so sv - x == -(x - sv)); dp is the previous row's dn,
+// so each row's difference is formed once per column.  Horizontal: he = e - x and
+// hw = x - w, (e - x) + (w - x) == he - hw exactly, and a lane's four cells share the
+// five differences of its row.  4 operations per cell for the Laplacian instead of 7.
 template <int COEF, bool PLAIN, bool KZ = false>
-__device__ __forceinline__ XV skew_inner(const DevParams &p, const TbArgs &a, float x, float y, float n, float sv,
-                                         float he, float hw, float cc, bool act)
+__device__ __forceinline__ XV skew_inner(const DevParams &p, const TbArgs &a, float x, float y, float vert, float he,
+                                         float hw, float cc, bool act)
 {
     const float ccv = (COEF == WG_COEF_TABLE) ? cc : (act ? a.c2 : a.c2b);
     const float g = (COEF == WG_COEF_TABLE) ? a.gam : (act ? a.gam : a.gamb);
-    const float lap = ((n - x) + (sv - x)) + (he - hw);
+    const float lap = vert + (he - hw);
     if (PLAIN && KZ) return upd32_k0(x, y, ccv, lap, g);
     if (PLAIN) return upd32(x, y, ccv, lap, a.kappa, g);
     XV r = keep32(x, y);
@@ -363,10 +365,11 @@ __device__ __forceinline__ float pick4(float a0, float a1, float a2, float a3, i
 
 // Column 0 (right = false) or ny-1 (right = true) at a row 1..nx-2: the boundary rule of
 // evolve_wave_half for the top/bottom lines (wave_billiard.c:366-452, B_COND Dirichlet or
-// absorbing, OSCILLATE_TOPBOT), same branches as skew_cell's general form.
+// absorbing, OSCILLATE_TOPBOT), same branches as skew_cell's general form.  vert: the
+// vertical part of the Laplacian, (n - x) + (sv - x), as skew_inner takes it.
 template <int COEF>
-__device__ __forceinline__ XV col_edge_cell(const DevParams &p, const TbArgs &a, int gi, float x, float y, float n,
-                                            float sv, float e, float w, float cc, float tcv, bool act, bool right)
+__device__ __forceinline__ XV col_edge_cell(const DevParams &p, const TbArgs &a, int gi, float x, float y, float vert,
+                                            float e, float w, float cc, float tcv, bool act, bool right)
 {
     const float ccv = (COEF == WG_COEF_TABLE) ? cc : (act ? a.c2 : a.c2b);
     const float g = (COEF == WG_COEF_TABLE) ? a.gam : (act ? a.gam : a.gamb);
@@ -382,7 +385,7 @@ __device__ __forceinline__ XV col_edge_cell(const DevParams &p, const TbArgs &a,
     XV r = keep32(x, y);
     if (p.twospeeds || act) {
         if (mode == 0)
-            r = upd32(x, y, ccv, ((n - x) + (sv - x)) + ((e - x) + (w - x)), a.kappa, g);
+            r = upd32(x, y, ccv, vert + ((e - x) + (w - x)), a.kappa, g);
         else
             r = absorb32(x, y, (COEF == WG_COEF_TABLE) ? tcv : (act ? a.courant : a.courantb), right ? w : e, a.kt, a.gt);
         if (p.floor_clamp && act) r = clamp32(x, r, a.vmax);
@@ -445,7 +448,10 @@ __device__ __forceinline__ void skew_strip(const DevParams &p, const TbArgs &a, 
     const int ce = !edge ? -1 : (gj0 == 0 ? 0 : (cr >= 0 && cr <= 3 ? cr : -1));
     const bool src_lane = edge && p.src_on && p.src_j >= gj0 && p.src_j < gj0 + 4;
 
-    float W[K + 1][3][4];  // W[s][k][c] = phi of level s at row m-s-2+k, column gj0+c
+    float W[K + 1][3][4];  // W[s][k][c] = phi of level s at row m-s-2+k, column gj0+c (k = 0: GEN only)
+    // Dp[s][c] = phi_s(m-s-1) - phi_s(m-s-2): the vertical difference level s+1 formed in
+    // the previous trip, its dp in this one (not GEN)
+    float Dp[K][4];
     // V[s][c] = velocity of level s at row m-s-1, column gj0+c, until level s+1 of the trip
     // for row m has read it; pend[c] = the new velocity row of the level just computed.
     // (Kept in a per-warp shared-memory row per level instead, the single-grid pass ran as
@@ -461,7 +467,7 @@ __device__ __forceinline__ void skew_strip(const DevParams &p, const TbArgs &a, 
 #pragma unroll
         for (int c = 0; c < 4; c++) {
             W[q][0][c] = W[q][1][c] = W[q][2][c] = 0.f;
-            if (q < K) V[q][c] = 0.f;
+            if (q < K) V[q][c] = Dp[q][c] = 0.f;
         }
         TE[q] = 0.f;
     }
@@ -513,7 +519,7 @@ __device__ __forceinline__ void skew_strip(const DevParams &p, const TbArgs &a, 
             slot = (slot == D - 1) ? 0 : slot + 1;
 #pragma unroll
             for (int c = 0; c < 4; c++) {
-                W[0][0][c] = W[0][1][c];
+                if (GEN) W[0][0][c] = W[0][1][c];
                 W[0][1][c] = W[0][2][c];
                 W[0][2][c] = xin[c];
                 pend[c] = yin[c];
@@ -527,6 +533,21 @@ __device__ __forceinline__ void skew_strip(const DevParams &p, const TbArgs &a, 
             for (int lv = 1; lv <= K; lv++) {
                 const int r = m - lv;  // row of this level's new value
                 XV v[4] = {{0.f, 0.f}, {0.f, 0.f}, {0.f, 0.f}, {0.f, 0.f}};
+                // vertical part of the Laplacian of level lv-1 at row r: from the kept
+                // difference (formed in every trip, so that the first active trip of the
+                // level finds its dp), or from the three rows in GEN strips, which keep them
+                // for the general rule
+                float vt[4];
+#pragma unroll
+                for (int c = 0; c < 4; c++) {
+                    if (GEN) {
+                        vt[c] = (W[lv - 1][2][c] - W[lv - 1][1][c]) + (W[lv - 1][0][c] - W[lv - 1][1][c]);
+                    } else {
+                        const float dn = W[lv - 1][2][c] - W[lv - 1][1][c];
+                        vt[c] = dn - Dp[lv - 1][c];
+                        Dp[lv - 1][c] = dn;
+                    }
+                }
                 // Level lv at row r reaches the stored rows only from r >= i_s - K + lv on, i.e.
                 // from input row m0 + 2 lv + 1: in the pipeline fill the earlier levels are skipped
                 // (warp-uniform), and their window slots hold zeros that nothing reads.
@@ -549,15 +570,14 @@ __device__ __forceinline__ void skew_strip(const DevParams &p, const TbArgs &a, 
 #pragma unroll
                 for (int c = 0; c < 4; c++) {
                     const bool act = NEED_ACT ? ((aq >> (4 * lv + c)) & 1u) : true;
-                    v[c] = skew_inner<COEF, PLAIN, KZ>(p, a, Wc[c], Yl[c], W[lv - 1][2][c], W[lv - 1][0][c], hd[c + 1],
-                                                       hd[c], Tl[c], act);
+                    v[c] = skew_inner<COEF, PLAIN, KZ>(p, a, Wc[c], Yl[c], vt[c], hd[c + 1], hd[c], Tl[c], act);
                 }
                 if (!GEN && edge) {  // warp-uniform
                     if (ce >= 0 && r > 0 && r < p.nx - 1) {  // the lane holding column 0 (c = 0) or ny-1 (c = 3)
                         const bool lf = ce == 0;
                         const XV res = col_edge_cell<COEF>(
-                            p, a, r, lf ? Wc[0] : Wc[3], lf ? Yl[0] : Yl[3], lf ? W[lv - 1][2][0] : W[lv - 1][2][3],
-                            lf ? W[lv - 1][0][0] : W[lv - 1][0][3], lf ? Wc[1] : e3, lf ? w0 : Wc[2],
+                            p, a, r, lf ? Wc[0] : Wc[3], lf ? Yl[0] : Yl[3], lf ? vt[0] : vt[3], lf ? Wc[1] : e3,
+                            lf ? w0 : Wc[2],
                             lf ? Tl[0] : Tl[3], TE[lv], NEED_ACT ? ((aq >> (4 * lv + ce)) & 1u) : true, !lf);
                         v[0] = lf ? res : v[0];
                         v[3] = lf ? v[3] : res;
@@ -574,8 +594,7 @@ __device__ __forceinline__ void skew_strip(const DevParams &p, const TbArgs &a, 
                     if (ce >= 0 && r > 0 && r < p.nx - 1) {  // the lane holding column 0 or ny-1: picked by index
                         const XV res = col_edge_cell<COEF>(
                             p, a, r, pick4(Wc[0], Wc[1], Wc[2], Wc[3], ce), pick4(Yl[0], Yl[1], Yl[2], Yl[3], ce),
-                            pick4(W[lv - 1][2][0], W[lv - 1][2][1], W[lv - 1][2][2], W[lv - 1][2][3], ce),
-                            pick4(W[lv - 1][0][0], W[lv - 1][0][1], W[lv - 1][0][2], W[lv - 1][0][3], ce),
+                            pick4(vt[0], vt[1], vt[2], vt[3], ce),
                             pick4(Wc[1], Wc[2], Wc[3], e3, ce), pick4(w0, Wc[0], Wc[1], Wc[2], ce),
                             pick4(Tl[0], Tl[1], Tl[2], Tl[3], ce), TE[lv],
                             NEED_ACT ? ((aq >> (4 * lv + ce)) & 1u) : true, gj0 != 0);
@@ -612,7 +631,7 @@ __device__ __forceinline__ void skew_strip(const DevParams &p, const TbArgs &a, 
                 }  // levels in use
 #pragma unroll
                 for (int c = 0; c < 4; c++) {
-                    W[lv][0][c] = W[lv][1][c];
+                    if (GEN) W[lv][0][c] = W[lv][1][c];
                     W[lv][1][c] = W[lv][2][c];
                     W[lv][2][c] = v[c].x;
                     V[lv - 1][c] = pend[c];  // level lv-1's row r+1: level lv has read row r
