@@ -85,9 +85,13 @@ struct XV {
 // Laplacian as differences from the centre.  Same mathematics as upd64.  Every rounding
 // is spelled out as an operation or a fused multiply-add (nothing left for the compiler
 // to contract), so every kernel that applies it rounds each cell the same way.
+__device__ __forceinline__ float vel32(float x, float v, float cc, float delta, float kappa, float g)
+{
+    return fmaf(cc, delta, fmaf(-kappa, x, fmaf(-g, v, v)));
+}
 __device__ __forceinline__ XV upd32(float x, float v, float cc, float delta, float kappa, float g)
 {
-    const float vn = fmaf(cc, delta, fmaf(-kappa, x, fmaf(-g, v, v)));
+    const float vn = vel32(x, v, cc, delta, kappa, g);
     return XV{__fadd_rn(x, vn), vn};
 }
 // upd32 with KAPPA = 0: the kappa*x term is then an exact zero, so leaving it out changes
@@ -109,6 +113,13 @@ __device__ __forceinline__ XV set32(float x, float xn) { return XV{xn, __fsub_rn
 // A cell the reference does not write: the in-place two-level form swaps phi and psi
 // there, so phi' = psi = x - v and v' = -v.
 __device__ __forceinline__ XV keep32(float x, float v) { return XV{__fsub_rn(x, v), -v}; }
+// upd32 or keep32 by a flag, as one addition: x - v == x + (-v) exactly (signs of zero
+// included), so the unwritten cell's rule is the update's x + v' with v' = -v.
+__device__ __forceinline__ XV updkeep32(bool upd, float x, float v, float cc, float delta, float kappa, float g)
+{
+    const float vn = upd ? vel32(x, v, cc, delta, kappa, g) : -v;
+    return XV{__fadd_rn(x, vn), vn};
+}
 // FLOOR: phi clamped to [-vmax, vmax] by the reference's two comparisons (a NaN passes,
 // as there); an unchanged value keeps its velocity.
 __device__ __forceinline__ XV clamp32(float x, XV r, float vmax)

@@ -330,11 +330,8 @@ __device__ __forceinline__ XV skew_inner(const DevParams &p, const TbArgs &a, fl
     const float lap = vert + (he - hw);
     if (PLAIN && KZ) return upd32_k0(x, y, ccv, lap, g);
     if (PLAIN) return upd32(x, y, ccv, lap, a.kappa, g);
-    XV r = keep32(x, y);
-    if (p.twospeeds || act) {
-        r = upd32(x, y, ccv, lap, a.kappa, g);
-        if (p.floor_clamp && act) r = clamp32(x, r, a.vmax);
-    }
+    XV r = updkeep32(p.twospeeds || act, x, y, ccv, lap, a.kappa, g);
+    if (p.floor_clamp && act) r = clamp32(x, r, a.vmax);
     return r;
 }
 
