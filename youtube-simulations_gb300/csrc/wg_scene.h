@@ -19,8 +19,8 @@ struct wg_scene {
     bool own_stream = false;
     size_t esz = 8;
     int pitch = 0;
-    void *f[2] = {nullptr, nullptr};  // f[cur] = phi (level t), f[1-cur] = psi (level t-1)
-    void *g[2] = {nullptr, nullptr};  // output pair of a temporally blocked pass (FP32)
+    void *f[2] = {nullptr, nullptr};  // f[cur] = phi (level t), f[1-cur] = psi (FP64) or the velocity (FP32)
+    void *g[2] = {nullptr, nullptr};  // FP32: the output pair of every update and blocked pass
     int cur = 0;
     uint32_t *act = nullptr, *nz = nullptr;
     int has_ghosts = 0;

@@ -320,6 +320,8 @@ class Scene:
         check(lib().wg_scene_sync(self.h))
 
     def download(self, native=False):
+        """(phi, psi) in FP64, or in the scene's precision with native=True; an FP32 scene
+        returns psi = phi - v formed in FP64."""
         n = self.params.nx * self.params.ny
         dt = self.dtype if native else np.float64
         phi, psi = np.empty(n, dt), np.empty(n, dt)
@@ -433,8 +435,9 @@ def scene_bytes(params, precision=P.FP32, coef=P.COEF_MASK):
 class Batch:
     """Uneven scenes advanced together, each frame replayed as a CUDA graph (wg_batch_*):
     single updates by one persistent kernel per update, or skewed passes of 2..6 updates
-    for FP32 scenes with mirror or absorbing boundaries (same fields bit for bit).  Masks
-    are 0/1 (WG_COEF_MASK coefficients)."""
+    for FP32 scenes with mirror, absorbing or periodic boundaries (same fields bit for
+    bit).  FP32 scenes hold phi and the velocity phi - psi.  Masks are 0/1 (WG_COEF_MASK
+    coefficients)."""
 
     def __init__(self, precision=P.FP32, stream=None):
         h = ctypes.c_void_p()
