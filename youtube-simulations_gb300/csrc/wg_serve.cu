@@ -375,8 +375,24 @@ wg_status wg_server_tick(wg_server *s, int32_t *frames_out)
     wg_status st;
     if (frames_out) *frames_out = 0;
     const int q = (int)(s->ticks & 1), prev = q ^ 1;
+    int32_t done_early = 0;
+    // pipelined: the previous tick's frames, once its copy has landed, are taken before
+    // this tick's retirement and admission work (downloads, uploads, table refreshes), so
+    // that work does not add to their latency
+    auto take_prev_if_ready = [&]() -> wg_status {
+        if (!s->cfg.pipeline || !s->rec[prev].pending) return WG_OK;
+        const cudaError_t e = cudaEventQuery(s->ev_done[prev]);
+        if (e == cudaErrorNotReady) return WG_OK;
+        if (e != cudaSuccess) return cuda_fail(e, "cudaEventQuery");
+        int32_t n = 0;
+        const wg_status r = server_complete(s, prev, &n);
+        done_early += n;
+        return r;
+    };
+    if ((st = take_prev_if_ready())) return st;
     // 1. finished and cancelled requests leave the batch (their last frames stay readable)
     if ((st = server_retire_finished(s))) return st;
+    if ((st = take_prev_if_ready())) return st;
     // 2. admission, first come first served, while the budget and the slots allow
     while (!s->queue.empty() && (int)s->resident.size() < s->cfg.max_scenes) {
         ServeReq &r = s->reqs[s->queue.front()];
@@ -395,6 +411,7 @@ wg_status wg_server_tick(wg_server *s, int32_t *frames_out)
         s->admitted++;
         s->layout_dirty[0] = s->layout_dirty[1] = true;
     }
+    if ((st = take_prev_if_ready())) return st;
     int32_t done_prev = 0;
     if (!s->resident.empty()) {
         // 3. buffer q's frame table follows the membership (buffer q was last used two
@@ -435,7 +452,7 @@ wg_status wg_server_tick(wg_server *s, int32_t *frames_out)
         if ((st = server_complete(s, q, &done_prev))) return st;
         if ((st = server_retire_finished(s))) return st;
     }
-    if (frames_out) *frames_out = done_prev;
+    if (frames_out) *frames_out = done_prev + done_early;
     s->busy += now_s() - t0;
     return WG_OK;
 }
