@@ -74,7 +74,10 @@ DevParams make_dev_params(const wg_params &p, int pitch)
     d.src_i = p.src_i;
     d.src_j = p.src_j;
     d.corner2_on = p.nx <= p.ny;
-    d.tb_shift = p.oscillate_topbot ? (double)(int)((p.xmax - p.xmin) * (double)p.nx / (p.xmax - p.xmin)) : 0.0;
+    // the reference's tb_shift, (int)((XMAX-XMIN)*NX/(XMAX-XMIN)), an integer: its row test
+    // i < tb_shift is i < tb_ilim
+    d.tb_ilim = p.oscillate_topbot ? (int)((p.xmax - p.xmin) * (double)p.nx / (p.xmax - p.xmin)) : 0;
+    d.pad0_ = 0;
     d.kappa = p.kappa;
     d.kappa_sides = p.kappa_sides;
     d.kappa_topbot = p.kappa_topbot;

@@ -22,7 +22,10 @@ struct DevParams {
     int osc_sine_jmax, osc_sine_jmin;  // xy_to_ij(0, OSCIL_YMID +- OSCIL_YMAX)[1]
     int src_on, src_i, src_j;
     int corner2_on;                // the reference's phi_out[0][NX-1] write is in bounds
-    double tb_shift;
+    // OSCILLATE_TOPBOT: rows i < tb_ilim take the top/bottom oscillation rule (the
+    // reference's i < tb_shift, with tb_shift an integer value: an integer comparison, no
+    // FP64 conversion on the device)
+    int tb_ilim, pad0_;
     double kappa, kappa_sides, kappa_topbot, gamma_sides, gamma_topbot, vmax;
     double c2, c2b, gam, gamb, courant, courantb;   // WG_COEF_MASK coefficients
     double omega, omega_b, amplitude, damping, achirp, yshift, ivar, ishift, wpshift;
@@ -262,7 +265,7 @@ __device__ __forceinline__ XV edge32(const DevParams &p, int gi, int gj, float x
     int mode = 0;  // 0 leapfrog with mirrored neighbours, 1 absorbing, 2 oscillating value
     float nb = 0.f, kk = 0.f, gg = 0.f;
     if (bj0 || bj1) {
-        if (p.osc_topbot && gi > 0 && gi < NX - 1 && ((double)gi < p.tb_shift)) {
+        if (p.osc_topbot && gi > 0 && gi < NX - 1 && gi < p.tb_ilim) {
             e = x;
             w = x;
         } else if (p.b_cond == WG_BC_DIRICHLET) {
@@ -318,7 +321,7 @@ __device__ inline bool edge_cell(const DevParams &p, long long time, int i, int 
         const int jb = j, jn = (j == NY - 1) ? NY - 2 : 1, jw = (j == NY - 1) ? 0 : NY - 1;
         if (p.twospeeds || ACT(i, jb)) {
             double x = (double)PHI(i, jb), y = (double)PSI(i, jb);
-            if (p.osc_topbot && ((double)i < p.tb_shift) && (i < NX - 1) && (i > 0)) {
+            if (p.osc_topbot && i < p.tb_ilim && (i < NX - 1) && (i > 0)) {
                 double delta = A_(A_((double)PHI(i + 1, jb), (double)PHI(i - 1, jb)), -M_(2.0, x));
                 v = upd64(x, y, CF.tcc(i, jb), delta, p.kappa, CF.tg(i, jb));
             } else {

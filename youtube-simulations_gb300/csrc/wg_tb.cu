@@ -371,7 +371,7 @@ __device__ __forceinline__ XV col_edge_cell(const DevParams &p, const TbArgs &a,
     const float ccv = (COEF == WG_COEF_TABLE) ? cc : (act ? a.c2 : a.c2b);
     const float g = (COEF == WG_COEF_TABLE) ? a.gam : (act ? a.gam : a.gamb);
     int mode = 0;
-    if (p.osc_topbot && ((double)gi < p.tb_shift)) {
+    if (p.osc_topbot && gi < p.tb_ilim) {
         e = x;
         w = x;
     } else if (p.b_cond == WG_BC_DIRICHLET) {
