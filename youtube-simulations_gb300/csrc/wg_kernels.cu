@@ -583,6 +583,26 @@ __global__ void k_state_in32(int nx, int ny, int pitch, const H *__restrict__ ph
     x[o] = (float)a;
     v[o] = (float)S_(a, b);
 }
+// The same for FP32 host rows four columns per thread (ny a multiple of 4, so every dense
+// row starts on 16 bytes), padding zeroed.
+__global__ void k_state_in32_v4(int nx, int ny, int pitch, const float4 *__restrict__ phi,
+                                const float4 *__restrict__ psi, float *__restrict__ x, float *__restrict__ v)
+{
+    const int j = 4 * (blockIdx.x * blockDim.x + threadIdx.x);
+    const int i = blockIdx.y;
+    if (j >= pitch || i >= nx) return;
+    const size_t o = (size_t)i * pitch + j;
+    float4 a = make_float4(0.f, 0.f, 0.f, 0.f), b = a;
+    if (j < ny) {
+        const size_t c = ((size_t)i * ny + j) / 4;
+        a = phi[c];
+        b = psi[c];
+    }
+    const float4 dv = make_float4((float)S_(a.x, b.x), (float)S_(a.y, b.y), (float)S_(a.z, b.z), (float)S_(a.w, b.w));
+    *reinterpret_cast<float4 *>(x + o) = a;
+    *reinterpret_cast<float4 *>(v + o) = dv;
+}
+
 // FP32 state to host rows: phi, and psi = phi - v in FP64 (rounded to H); either may be NULL.
 template <class H>
 __global__ void k_state_out32(int nx, int ny, int pitch, const float *__restrict__ x, const float *__restrict__ v,
@@ -595,6 +615,21 @@ __global__ void k_state_out32(int nx, int ny, int pitch, const float *__restrict
     const double a = (double)x[o];
     if (phi) phi[c] = (H)a;
     if (psi) psi[c] = (H)S_(a, (double)v[o]);
+}
+// The same into FP32 host rows four columns per thread (ny a multiple of 4).
+__global__ void k_state_out32_v4(int nx, int ny, int pitch, const float *__restrict__ x, const float *__restrict__ v,
+                                 float4 *__restrict__ phi, float4 *__restrict__ psi)
+{
+    const int j = 4 * (blockIdx.x * blockDim.x + threadIdx.x);
+    const int i = blockIdx.y;
+    if (j >= ny || i >= nx) return;
+    const size_t o = (size_t)i * pitch + j, c = ((size_t)i * ny + j) / 4;
+    const float4 a = *reinterpret_cast<const float4 *>(x + o);
+    if (phi) phi[c] = a;
+    if (psi) {
+        const float4 b = *reinterpret_cast<const float4 *>(v + o);
+        psi[c] = make_float4((float)S_(a.x, b.x), (float)S_(a.y, b.y), (float)S_(a.z, b.z), (float)S_(a.w, b.w));
+    }
 }
 
 // ---------------------------------------------------------------------------
@@ -733,15 +768,30 @@ template void launch_convert_in<double>(int, int, int, const double *, double *,
 template void launch_convert_out<float>(int, int, int, const float *, double *, cudaStream_t);
 template void launch_convert_out<double>(int, int, int, const double *, double *, cudaStream_t);
 
+// dense FP32 rows of ny % 4 == 0 columns from 16-byte aligned bases take the 4-wide kernels
+static bool rows_v4(int ny, const void *a, const void *b)
+{
+    return ny % 4 == 0 && ((uintptr_t)a & 15) == 0 && ((uintptr_t)b & 15) == 0;
+}
 template <class H>
 void launch_state_in32(int nx, int ny, int pitch, const H *phi, const H *psi, float *x, float *v, cudaStream_t st)
 {
+    if (sizeof(H) == 4 && rows_v4(ny, phi, psi)) {
+        dim3 grd((pitch / 4 + 255) / 256, nx);
+        k_state_in32_v4<<<grd, 256, 0, st>>>(nx, ny, pitch, (const float4 *)phi, (const float4 *)psi, x, v);
+        return;
+    }
     dim3 grd((pitch + 255) / 256, nx);
     k_state_in32<H><<<grd, 256, 0, st>>>(nx, ny, pitch, phi, psi, x, v);
 }
 template <class H>
 void launch_state_out32(int nx, int ny, int pitch, const float *x, const float *v, H *phi, H *psi, cudaStream_t st)
 {
+    if (sizeof(H) == 4 && rows_v4(ny, phi ? (const void *)phi : (const void *)psi, psi ? (const void *)psi : (const void *)phi)) {
+        dim3 grd((ny / 4 + 255) / 256, nx);
+        k_state_out32_v4<<<grd, 256, 0, st>>>(nx, ny, pitch, x, v, (float4 *)phi, (float4 *)psi);
+        return;
+    }
     dim3 grd((ny + 255) / 256, nx);
     k_state_out32<H><<<grd, 256, 0, st>>>(nx, ny, pitch, x, v, phi, psi);
 }
