@@ -390,16 +390,14 @@ __device__ __forceinline__ XV col_edge_cell(const DevParams &p, const TbArgs &a,
     return r;
 }
 
-// Asynchronous global->shared copies of one lane's 16 (or 4) bytes; with src_bytes 0
-// nothing is read and the destination is zero-filled.
-__device__ __forceinline__ void cp_async16(void *dst, const void *src, int src_bytes)
+// Asynchronous global->shared copies of one lane's 16 (or 4) bytes to a 32-bit shared-window
+// address; with src_bytes 0 nothing is read and the destination is zero-filled.
+__device__ __forceinline__ void cp_async16s(unsigned d, const void *src, int src_bytes)
 {
-    const unsigned d = (unsigned)__cvta_generic_to_shared(dst);
     asm volatile("cp.async.cg.shared.global [%0], [%1], 16, %2;\n" ::"r"(d), "l"(src), "r"(src_bytes) : "memory");
 }
-__device__ __forceinline__ void cp_async4(void *dst, const void *src, int src_bytes)
+__device__ __forceinline__ void cp_async4s(unsigned d, const void *src, int src_bytes)
 {
-    const unsigned d = (unsigned)__cvta_generic_to_shared(dst);
     asm volatile("cp.async.ca.shared.global [%0], [%1], 4, %2;\n" ::"r"(d), "l"(src), "r"(src_bytes) : "memory");
 }
 __device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
@@ -470,23 +468,27 @@ __device__ __forceinline__ void skew_strip(const DevParams &p, const TbArgs &a, 
     }
 
     // row m goes to slot (m - m0) % D; each lane copies, and later reads, only its own bytes
+    // shared-memory addresses of this lane's bytes in slot 0 (a slot is SL::SIZE floats)
+    const unsigned s16 = (unsigned)__cvta_generic_to_shared(ring) + 16u * lane;
+    const unsigned s4 = (unsigned)__cvta_generic_to_shared(ring) + 4u * lane;
     auto issue = [&](int m, int slot) {
-        float *b = ring + slot * SL::SIZE;
+        const unsigned so = (unsigned)(slot * SL::SIZE * 4);
         const bool ok = wrap ? (gj0 >= -BATCH_GHOST_COLS && gj0 < p.ny + BATCH_GHOST_COLS && m >= -BATCH_GHOST_ROWS &&
                                 m < p.nx + BATCH_GHOST_ROWS)
-                             : (grp_ok && m >= 0 && m < p.nx);
+                             : (grp_ok && (unsigned)m < (unsigned)p.nx);
         const long long o = ok ? (long long)m * p.pitch + gj0 : 0;
         const int n16 = ok ? 16 : 0;
-        cp_async16(b + 4 * lane, a.phi + o, n16);
-        cp_async16(b + SL::PSI + 4 * lane, a.psi + o, n16);
-        if (COEF == WG_COEF_TABLE) cp_async16(b + SL::TCC + 4 * lane, a.tcc + o, n16);
+        cp_async16s(s16 + so, a.phi + o, n16);
+        cp_async16s(s16 + so + 4 * SL::PSI, a.psi + o, n16);
+        if (COEF == WG_COEF_TABLE) cp_async16s(s16 + so + 4 * SL::TCC, a.tcc + o, n16);
         // mask word of the group: floor division, so that the ghost columns left of column 0
         // read the row's ghost word (index -1)
         if (NEED_ACT)
-            cp_async4(b + SL::ACT + lane, a.act + (ok ? (long long)m * p.wpitch + ((gj0 + 32) / 32 - 1) : 0), ok ? 4 : 0);
+            cp_async4s(s4 + so + 4 * SL::ACT, a.act + (ok ? (long long)m * p.wpitch + ((gj0 + 32) / 32 - 1) : 0),
+                       ok ? 4 : 0);
         if (need_tce) {
             const bool te = ok && ce >= 0 && a.tc;  // the table exists with an absorbing boundary
-            cp_async4(b + SL::TCE + lane, te ? a.tc + o + (unsigned)ce : a.phi, te ? 4 : 0);
+            cp_async4s(s4 + so + 4 * SL::TCE, te ? a.tc + o + (unsigned)ce : a.phi, te ? 4 : 0);
         }
         cp_async_commit();
     };
