@@ -104,6 +104,81 @@ class Clocks:
                 "reasons": reasons, "samples": len(rows)}
 
 
+class NvmlClocks:
+    """SM clock and clock-event reasons read through NVML (libnvidia-ml, ctypes) every 2 ms
+    from a thread while the timed region runs, so that even a region of a few tens of
+    milliseconds has samples inside it.  Reads only; falls back to nvidia-smi (Clocks)
+    where NVML cannot be loaded."""
+    REASONS = {0x4: "sw_power_cap", 0x8: "hw_slowdown", 0x20: "sw_thermal_slowdown", 0x40: "hw_thermal_slowdown",
+               0x80: "hw_power_brake_slowdown"}
+
+    def __init__(self, gpu_index, device=None):
+        import ctypes
+        import threading
+        self.ct, self.threading = ctypes, threading
+        self.lib = ctypes.CDLL("libnvidia-ml.so.1")
+        if self.lib.nvmlInit_v2() != 0:
+            raise OSError("nvmlInit failed")
+        self.h = ctypes.c_void_p()
+        bus = None
+        try:
+            import torch
+            pr = torch.cuda.get_device_properties(device)
+            bus = "%08x:%02x:%02x.0" % (pr.pci_domain_id, pr.pci_bus_id, pr.pci_device_id)
+        except Exception:
+            bus = None
+        ok = bus is not None and self.lib.nvmlDeviceGetHandleByPciBusId_v2(bus.encode(), ctypes.byref(self.h)) == 0
+        if not ok and self.lib.nvmlDeviceGetHandleByIndex_v2(gpu_index, ctypes.byref(self.h)) != 0:
+            raise OSError("no NVML handle")
+        mx = ctypes.c_uint()
+        self.max_mhz = float(mx.value) if self.lib.nvmlDeviceGetMaxClockInfo(self.h, 1, ctypes.byref(mx)) == 0 else None
+        self.rows, self.stop_flag, self.t = [], False, None
+
+    def _sample(self):
+        ct = self.ct
+        clk, rs = ct.c_uint(), ct.c_ulonglong()
+        if self.lib.nvmlDeviceGetClockInfo(self.h, 1, ct.byref(clk)) != 0:  # NVML_CLOCK_SM
+            return
+        fn = getattr(self.lib, "nvmlDeviceGetCurrentClocksEventReasons", None) or \
+            self.lib.nvmlDeviceGetCurrentClocksThrottleReasons
+        r = int(rs.value) if fn(self.h, ct.byref(rs)) == 0 else 0
+        self.rows.append((float(clk.value), r))
+
+    def _loop(self):
+        import time as _t
+        while not self.stop_flag:
+            self._sample()
+            _t.sleep(0.002)
+
+    def start(self):
+        self._sample()
+        self.t = self.threading.Thread(target=self._loop, daemon=True)
+        self.t.start()
+
+    def stop(self):
+        self.stop_flag = True
+        self.t.join(timeout=5)
+        self._sample()
+        return self.summary(self.rows, self.max_mhz)
+
+    @classmethod
+    def summary(cls, rows, max_mhz):
+        """Median SM clock of the samples, the maximum clock and the reasons seen active."""
+        if not rows:
+            return {"sm_mhz": None, "sm_max_mhz": max_mhz, "reasons": ["no samples"]}
+        reasons = sorted({name for _, r in rows for bit, name in cls.REASONS.items() if r & bit})
+        return {"sm_mhz": statistics.median(c for c, _ in rows), "sm_max_mhz": max_mhz, "reasons": reasons,
+                "samples": len(rows), "source": "NVML, every 2 ms during the timed region"}
+
+
+def clock_sampler(gpu_index, device=None):
+    """NVML sampler where the library loads, else nvidia-smi."""
+    try:
+        return NvmlClocks(gpu_index, device)
+    except Exception:
+        return Clocks(gpu_index)
+
+
 def dist_env():
     rank = int(os.environ.get("RANK", "0"))
     world = int(os.environ.get("WORLD_SIZE", "1"))
@@ -260,7 +335,7 @@ def run_ours(args):
         l0 = s.launches()
         step_ms, energy_ms = 0.0, 0.0
         energies = []
-        clocks = Clocks(local)
+        clocks = clock_sampler(local, dev)
         clocks.start()
         wall0 = time.perf_counter()
         for _ in range(steps):

@@ -71,3 +71,21 @@ def test_serve_stream_submits_on_the_wall_clock():
     for t, a in zip(srv.submit_times, arrivals):
         assert t - t0 >= a - 1e-3  # never submitted before its arrival time
     assert wall >= 0.12 and max_q == 0 and max_res >= 1
+
+
+def test_clock_summary_decodes_the_event_reasons():
+    """NVML clock-event reason bits (sw power cap 0x4, hw slowdown 0x8, sw thermal 0x20, hw
+    thermal 0x40) become the names the bench line reports; the clock is the median sample."""
+    rows = [(2070.0, 0x0), (2070.0, 0x4), (1995.0, 0x4 | 0x8), (2070.0, 0x1)]
+    out = bench.NvmlClocks.summary(rows, 2070.0)
+    assert out["sm_mhz"] == 2070.0 and out["sm_max_mhz"] == 2070.0 and out["samples"] == 4
+    assert out["reasons"] == ["hw_slowdown", "sw_power_cap"]
+    assert bench.NvmlClocks.summary([(1500.0, 0x40 | 0x20)], 2070.0)["reasons"] == ["hw_thermal_slowdown",
+                                                                                   "sw_thermal_slowdown"]
+    assert bench.NvmlClocks.summary([], 2070.0)["reasons"] == ["no samples"]
+
+
+def test_clock_sampler_falls_back_without_nvml():
+    """Where NVML cannot be loaded (this host has no GPU driver), the nvidia-smi sampler is used."""
+    s = bench.clock_sampler(0)
+    assert isinstance(s, (bench.Clocks, bench.NvmlClocks))
