@@ -680,6 +680,12 @@ __global__ void __launch_bounds__(128, 4) k_step_skew(const __grid_constant__ De
     const int gj0 = t.x * STEP - H + 4 * lane;
     const int lo = t.x * STEP, hi = lo + STEP;  // the core columns of tile t.x
     constexpr bool PLAIN = PL >= 1, KZ = PL == 2;
+    // Programmatic dependent launch: this pass may be launched while the previous one is
+    // finishing (its blocks take the SMs the previous pass's blocks leave); it reads and
+    // writes the fields only after the previous pass has completed and its writes are
+    // visible.  The next pass may be launched from here on.
+    asm volatile("griddepcontrol.wait;\n" ::: "memory");
+    asm volatile("griddepcontrol.launch_dependents;\n" ::: "memory");
     if (t.w == 2) skew_strip<COEF, K, PLAIN, true, false, KZ>(p, a, t.y, t.z, gj0, lane, ring, tring, true, lo, hi);
     else skew_strip<COEF, K, PLAIN, false, false, KZ>(p, a, t.y, t.z, gj0, lane, ring, tring, t.w == 1, lo, hi);
 }
@@ -727,7 +733,18 @@ static void launch_skew_k(const DevParams &p, const TbArgs &a, const int4 *tasks
 {
     constexpr size_t smem = skew_smem_bytes<COEF, K>();
     skew_capacity<COEF, K, PL>();  // sets the shared-memory attribute once
-    k_step_skew<COEF, K, PL><<<(ntasks + 3) / 4, 128, smem, st>>>(p, a, tasks, ntasks);
+    // launched with programmatic stream serialization: see the kernel's dependency wait
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3((unsigned)((ntasks + 3) / 4));
+    cfg.blockDim = dim3(128);
+    cfg.dynamicSmemBytes = smem;
+    cfg.stream = st;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    attr[0].val.programmaticStreamSerializationAllowed = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    cudaLaunchKernelEx(&cfg, k_step_skew<COEF, K, PL>, p, a, tasks, ntasks);
 }
 
 template <int COEF, int PL>
