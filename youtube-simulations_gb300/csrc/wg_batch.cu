@@ -220,6 +220,8 @@ __global__ void __launch_bounds__(256, 4) k_batch_step(const BatchHdr *__restric
                                                     int *__restrict__ counter, int u, int all)
 {
     __shared__ int s_next[2];
+    pdl_wait();  // launched by launch_pdl: the previous update has completed
+    pdl_trigger();
     const int total = all ? hdr->total_tiles : hdr->plain_tiles;
     const int tid = threadIdx.y * blockDim.x + threadIdx.x;
     if (tid == 0) s_next[0] = atomicAdd(counter + u, 1);
@@ -621,8 +623,8 @@ static void batch_enqueue_frame(wg_batch *b, int n, bool skewed)
     if (!skewed || (b->graph_sig & 1u)) {  // the chain of single updates
         dim3 blk(BT_THREADS, 4);
         for (int u = 0; u < n; u++)
-            k_batch_step<T><<<b->persistent_blocks, blk, 0, b->st>>>(b->d_hdr, b->d_tab, b->d_items, b->d_dyn,
-                                                                     b->d_counter, u, skewed ? 0 : 1);
+            launch_pdl(k_batch_step<T>, dim3(b->persistent_blocks), blk, 0, b->st, (const BatchHdr *)b->d_hdr,
+                       (const SlotDev *)b->d_tab, (const int4 *)b->d_items, b->d_dyn, b->d_counter, u, skewed ? 0 : 1);
     }
     for (int K : groups) cudaStreamWaitEvent(b->st, b->ev_join[K], 0);
     const int cap = std::max(b->tab_cap, 1);

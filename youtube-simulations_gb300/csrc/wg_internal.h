@@ -27,6 +27,29 @@ struct FastArgs {
     int do_source;       // add the point source in this kernel
 };
 
+// Programmatic dependent launch.  A kernel launched by launch_pdl may start while the
+// previous kernel in its stream is finishing; it calls pdl_wait() before its first access to
+// memory that kernel reads or writes (the wait returns once that kernel has completed and
+// its writes are visible), then pdl_trigger() to let the next such kernel launch early.
+__device__ __forceinline__ void pdl_wait() { asm volatile("griddepcontrol.wait;\n" ::: "memory"); }
+__device__ __forceinline__ void pdl_trigger() { asm volatile("griddepcontrol.launch_dependents;\n" ::: "memory"); }
+template <class... KArgs, class... Args>
+inline cudaError_t launch_pdl(void (*kernel)(KArgs...), dim3 grid, dim3 block, size_t smem, cudaStream_t st,
+                              Args &&...args)
+{
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = grid;
+    cfg.blockDim = block;
+    cfg.dynamicSmemBytes = smem;
+    cfg.stream = st;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    attr[0].val.programmaticStreamSerializationAllowed = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    return cudaLaunchKernelEx(&cfg, kernel, static_cast<Args &&>(args)...);
+}
+
 // error state (thread-local message)
 void set_error(const char *fmt, ...);
 void clear_error();

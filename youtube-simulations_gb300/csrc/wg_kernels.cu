@@ -197,6 +197,8 @@ __global__ void __launch_bounds__(256) k_step_bulk(const __grid_constant__ DevPa
                                                    const __grid_constant__ FastArgs<T> a)
 {
     constexpr int V = Vec<T>::n;
+    pdl_wait();  // launched by launch_pdl: the previous update has completed
+    pdl_trigger();
     const int i = 1 + blockIdx.y * blockDim.y + threadIdx.y;
     const int j0 = (blockIdx.x * blockDim.x + threadIdx.x) * V;
     if (i >= p.nx - 1 || j0 >= p.pitch) return;
@@ -260,6 +262,8 @@ template <class T, int COEF>
 __global__ void __launch_bounds__(256) k_step_edge(const __grid_constant__ DevParams p,
                                                    const __grid_constant__ FastArgs<T> a, long long time)
 {
+    pdl_wait();  // launched by launch_pdl: the bulk kernel of this update has completed
+    pdl_trigger();
     const int idx = blockIdx.x * blockDim.x + threadIdx.x;
     const int NX = p.nx, NY = p.ny;
     const int nedge = 2 * NX + 2 * (NY - 2);
@@ -679,13 +683,13 @@ static void launch_bulk(const DevParams &p, const FastArgs<T> &a, dim3 grd, dim3
     if constexpr (sizeof(T) == 8) {
         const bool g0 = (COEF == WG_COEF_TABLE) ? (!a.tg && p.gam == 0.0) : (p.gam == 0.0 && p.gamb == 0.0);
         switch ((p.kappa == 0.0 ? Z_KAPPA : 0) | (g0 ? Z_GAMMA : 0)) {
-        case Z_KAPPA: k_step_bulk<T, COEF, Z_KAPPA><<<grd, blk, 0, st>>>(p, a); return;
-        case Z_GAMMA: k_step_bulk<T, COEF, Z_GAMMA><<<grd, blk, 0, st>>>(p, a); return;
-        case Z_KAPPA | Z_GAMMA: k_step_bulk<T, COEF, Z_KAPPA | Z_GAMMA><<<grd, blk, 0, st>>>(p, a); return;
+        case Z_KAPPA: launch_pdl(k_step_bulk<T, COEF, Z_KAPPA>, grd, blk, 0, st, p, a); return;
+        case Z_GAMMA: launch_pdl(k_step_bulk<T, COEF, Z_GAMMA>, grd, blk, 0, st, p, a); return;
+        case Z_KAPPA | Z_GAMMA: launch_pdl(k_step_bulk<T, COEF, Z_KAPPA | Z_GAMMA>, grd, blk, 0, st, p, a); return;
         default: break;
         }
     }
-    k_step_bulk<T, COEF><<<grd, blk, 0, st>>>(p, a);
+    launch_pdl(k_step_bulk<T, COEF>, grd, blk, 0, st, p, a);
 }
 
 template <class T>
@@ -696,10 +700,10 @@ void launch_step_fast(const DevParams &p, const FastArgs<T> &a, int coef_mode, l
     const int nedge = 2 * p.nx + 2 * (p.ny - 2) + 1;
     if (coef_mode == WG_COEF_MASK) {
         launch_bulk<T, WG_COEF_MASK>(p, a, grd, blk, st);
-        k_step_edge<T, WG_COEF_MASK><<<(nedge + 255) / 256, 256, 0, st>>>(p, a, time);
+        launch_pdl(k_step_edge<T, WG_COEF_MASK>, dim3((nedge + 255) / 256), dim3(256), 0, st, p, a, time);
     } else {
         launch_bulk<T, WG_COEF_TABLE>(p, a, grd, blk, st);
-        k_step_edge<T, WG_COEF_TABLE><<<(nedge + 255) / 256, 256, 0, st>>>(p, a, time);
+        launch_pdl(k_step_edge<T, WG_COEF_TABLE>, dim3((nedge + 255) / 256), dim3(256), 0, st, p, a, time);
     }
 }
 template void launch_step_fast<float>(const DevParams &, const FastArgs<float> &, int, long long, cudaStream_t);

@@ -684,8 +684,8 @@ __global__ void __launch_bounds__(128, 4) k_step_skew(const __grid_constant__ De
     // finishing (its blocks take the SMs the previous pass's blocks leave); it reads and
     // writes the fields only after the previous pass has completed and its writes are
     // visible.  The next pass may be launched from here on.
-    asm volatile("griddepcontrol.wait;\n" ::: "memory");
-    asm volatile("griddepcontrol.launch_dependents;\n" ::: "memory");
+    pdl_wait();
+    pdl_trigger();
     if (t.w == 2) skew_strip<COEF, K, PLAIN, true, false, KZ>(p, a, t.y, t.z, gj0, lane, ring, tring, true, lo, hi);
     else skew_strip<COEF, K, PLAIN, false, false, KZ>(p, a, t.y, t.z, gj0, lane, ring, tring, t.w == 1, lo, hi);
 }
@@ -733,18 +733,7 @@ static void launch_skew_k(const DevParams &p, const TbArgs &a, const int4 *tasks
 {
     constexpr size_t smem = skew_smem_bytes<COEF, K>();
     skew_capacity<COEF, K, PL>();  // sets the shared-memory attribute once
-    // launched with programmatic stream serialization: see the kernel's dependency wait
-    cudaLaunchConfig_t cfg = {};
-    cfg.gridDim = dim3((unsigned)((ntasks + 3) / 4));
-    cfg.blockDim = dim3(128);
-    cfg.dynamicSmemBytes = smem;
-    cfg.stream = st;
-    cudaLaunchAttribute attr[1];
-    attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
-    attr[0].val.programmaticStreamSerializationAllowed = 1;
-    cfg.attrs = attr;
-    cfg.numAttrs = 1;
-    cudaLaunchKernelEx(&cfg, k_step_skew<COEF, K, PL>, p, a, tasks, ntasks);
+    launch_pdl(k_step_skew<COEF, K, PL>, dim3((unsigned)((ntasks + 3) / 4)), dim3(128), smem, st, p, a, tasks, ntasks);
 }
 
 template <int COEF, int PL>
@@ -887,6 +876,8 @@ __global__ void __launch_bounds__(128, 4) k_batch_skew(const SlotDev *__restrict
     const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
     float *ring = reinterpret_cast<float *>(skew_smem) + wid * SL::DEPTH * SL::SIZE;
     DevParams &p = s_p[wid];
+    pdl_wait();  // launched by launch_pdl: the previous pass (or ghost refresh) has completed
+    pdl_trigger();
     const int n = *ntasks;
     for (;;) {
         int t = 0;
@@ -984,12 +975,13 @@ void launch_batch_skew(int K, const SlotDev *tab, const SlotDyn *dyn, const int4
                        int q, int toff, cudaStream_t st)
 {
     const int blocks = std::max(1, batch_skew_capacity(K) / 4);
+    const dim3 g(blocks), b(128);
     switch (K) {
-    case 2: k_batch_skew<2><<<blocks, 128, batch_skew_smem<2>(), st>>>(tab, dyn, tasks, ntasks, ticket, q, toff); break;
-    case 3: k_batch_skew<3><<<blocks, 128, batch_skew_smem<3>(), st>>>(tab, dyn, tasks, ntasks, ticket, q, toff); break;
-    case 4: k_batch_skew<4><<<blocks, 128, batch_skew_smem<4>(), st>>>(tab, dyn, tasks, ntasks, ticket, q, toff); break;
-    case 5: k_batch_skew<5><<<blocks, 128, batch_skew_smem<5>(), st>>>(tab, dyn, tasks, ntasks, ticket, q, toff); break;
-    case 6: k_batch_skew<6><<<blocks, 128, batch_skew_smem<6>(), st>>>(tab, dyn, tasks, ntasks, ticket, q, toff); break;
+    case 2: launch_pdl(k_batch_skew<2>, g, b, batch_skew_smem<2>(), st, tab, dyn, tasks, ntasks, ticket, q, toff); break;
+    case 3: launch_pdl(k_batch_skew<3>, g, b, batch_skew_smem<3>(), st, tab, dyn, tasks, ntasks, ticket, q, toff); break;
+    case 4: launch_pdl(k_batch_skew<4>, g, b, batch_skew_smem<4>(), st, tab, dyn, tasks, ntasks, ticket, q, toff); break;
+    case 5: launch_pdl(k_batch_skew<5>, g, b, batch_skew_smem<5>(), st, tab, dyn, tasks, ntasks, ticket, q, toff); break;
+    case 6: launch_pdl(k_batch_skew<6>, g, b, batch_skew_smem<6>(), st, tab, dyn, tasks, ntasks, ticket, q, toff); break;
     default: break;
     }
 }
