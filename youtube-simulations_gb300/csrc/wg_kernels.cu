@@ -406,6 +406,8 @@ __global__ void __launch_bounds__(32 * ENERGY_COLS_PER_BLOCK)
     __shared__ Acc sh[ENERGY_COLS_PER_BLOCK][2];
     __shared__ Acc sbx[6];
     __shared__ int sbox[ENERGY_COLS_PER_BLOCK];
+    pdl_wait();  // launched by launch_pdl: the update that wrote the fields has completed
+    pdl_trigger();
     const int wid = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int i = blockIdx.x * ENERGY_COLS_PER_BLOCK + wid;
     Acc ab = {0, 0}, at = {0, 0};  // bottom (j < ny/2) and top halves of the column
@@ -500,6 +502,8 @@ __global__ void __launch_bounds__(32 * ENERGY_COLS_PER_BLOCK)
 __global__ void __launch_bounds__(32) k_energy_final(int nx, int nblocks, const double2 *__restrict__ cols,
                                                      const double *__restrict__ part, double *__restrict__ out)
 {
+    pdl_wait();  // launched by launch_pdl: k_energy_cols has completed
+    pdl_trigger();
     const int k = blockIdx.x, lane = threadIdx.x;
     for (int i = k * 32 + lane; i < nx; i += 7 * 32) out[7 + i] = cols[i].x;
     Neu acc = {0.0, 0.0};
@@ -726,9 +730,10 @@ void launch_energy(const DevParams &p, const T *phi, const T *psi, const int16_t
     // bot: per-column sums; top (2 nx doubles): six box partials per block of 8 columns
     const int nblocks = (p.nx + ENERGY_COLS_PER_BLOCK - 1) / ENERGY_COLS_PER_BLOCK;
     double *part = reinterpret_cast<double *>(top);
-    if (xy) k_energy_cols<T, 0><<<nblocks, 32 * ENERGY_COLS_PER_BLOCK, 0, st>>>(p, phi, psi, xy, nz, ileft, iright, bot, part);
-    else k_energy_cols<T, 1><<<nblocks, 32 * ENERGY_COLS_PER_BLOCK, 0, st>>>(p, phi, psi, xy, nz, ileft, iright, bot, part);
-    k_energy_final<<<7, 32, 0, st>>>(p.nx, nblocks, bot, part, out);
+    const dim3 g(nblocks), b(32 * ENERGY_COLS_PER_BLOCK);
+    if (xy) launch_pdl(k_energy_cols<T, 0>, g, b, 0, st, p, phi, psi, xy, nz, ileft, iright, bot, part);
+    else launch_pdl(k_energy_cols<T, 1>, g, b, 0, st, p, phi, psi, xy, nz, ileft, iright, bot, part);
+    launch_pdl(k_energy_final, dim3(7), dim3(32), 0, st, p.nx, nblocks, (const double2 *)bot, (const double *)part, out);
 }
 template void launch_energy<float>(const DevParams &, const float *, const float *, const int16_t *, const uint32_t *, double2 *, double2 *, int, int, double *, cudaStream_t);
 template void launch_energy<double>(const DevParams &, const double *, const double *, const int16_t *, const uint32_t *, double2 *, double2 *, int, int, double *, cudaStream_t);

@@ -106,6 +106,8 @@ __device__ __forceinline__ void tb_rows_interior(const DevParams &p, const TbArg
 // increment of update t0 + s, rounded to FP32, for the passes of one step() call.
 __global__ void k_boundary_values(const __grid_constant__ DevParams p, long long t0, int n, float *osc, double *src)
 {
+    pdl_wait();  // launched by launch_pdl: the previous pass, which read these arrays, has completed
+    pdl_trigger();
     const int idx = blockIdx.x * blockDim.x + threadIdx.x;
     if (p.osc_left && idx < n * p.ny) {
         const int s = idx / p.ny, j = idx % p.ny;
@@ -1138,7 +1140,7 @@ wg_status tb_prepare(wg_scene *s, int n)
     }
     s->bv_t0 = s->time;
     const int threads = 256, blocks = (int)((need + threads - 1) / threads);
-    k_boundary_values<<<blocks, threads, 0, s->st>>>(s->dp, s->time, n, s->bv_osc, s->bv_src);
+    launch_pdl(k_boundary_values, dim3(blocks), dim3(threads), 0, s->st, s->dp, s->time, n, s->bv_osc, s->bv_src);
     s->launches++;
     WG_CUDA(cudaGetLastError());
     return WG_OK;
