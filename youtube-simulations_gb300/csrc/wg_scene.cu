@@ -53,6 +53,9 @@ static wg_status upload_f64(wg_scene *s, const double *h, void *dev)
     return WG_OK;
 }
 
+static wg_status flag_copy(wg_scene *s);
+static wg_status flag_result(wg_scene *s);
+
 // FP32 scene state from host (phi, psi) rows of H (double or float): both staged
 // contiguously, then phi and the velocity phi - psi formed on the device.  sync: wait for
 // the copies (the host arrays may then be freed).
@@ -87,8 +90,9 @@ static wg_status download_state32(wg_scene *s, H *phi, H *psi)
     WG_CUDA(cudaGetLastError());
     if (phi) WG_CUDA(cudaMemcpyAsync(phi, stage, bytes, cudaMemcpyDeviceToHost, s->st));
     if (psi) WG_CUDA(cudaMemcpyAsync(psi, stage + n, bytes, cudaMemcpyDeviceToHost, s->st));
+    if ((st = flag_copy(s))) return st;
     WG_CUDA(cudaStreamSynchronize(s->st));
-    return WG_OK;
+    return flag_result(s);
 }
 
 static wg_status download_f64(wg_scene *s, const void *dev, double *h)
@@ -192,18 +196,32 @@ wg_status scene_step_impl(wg_scene *s, int nsteps)
 }
 template wg_status scene_step_impl<float>(wg_scene *, int);
 
-// Reads (and clears) the flag a kernel sets when one of its bounded waits gave up.
-wg_status scene_check_flag(wg_scene *s)
+// The flag a kernel sets when one of its bounded waits gave up: copied into the last slot
+// of the pinned report buffer in stream order (flag_copy), read after the caller's
+// synchronisation (flag_result), so a download or a sync pays one synchronisation.
+static int *flag_slot(wg_scene *s) { return reinterpret_cast<int *>(s->hout + s->prm.nx + 7); }
+static wg_status flag_copy(wg_scene *s)
 {
-    int h = 0;
-    WG_CUDA(cudaMemcpyAsync(&h, s->dflag, sizeof h, cudaMemcpyDeviceToHost, s->st));
-    WG_CUDA(cudaStreamSynchronize(s->st));
-    if (h) {
+    WG_CUDA(cudaMemcpyAsync(flag_slot(s), s->dflag, sizeof(int), cudaMemcpyDeviceToHost, s->st));
+    return WG_OK;
+}
+static wg_status flag_result(wg_scene *s)
+{
+    if (*flag_slot(s)) {
+        *flag_slot(s) = 0;
         WG_CUDA(cudaMemsetAsync(s->dflag, 0, sizeof(int), s->st));
         set_error("a tile load did not complete within its bounded wait; the last step is invalid");
         return WG_ERR_TIMEOUT;
     }
     return WG_OK;
+}
+
+// Reads (and clears) the flag.
+wg_status scene_check_flag(wg_scene *s)
+{
+    if (wg_status st = flag_copy(s)) return st;
+    WG_CUDA(cudaStreamSynchronize(s->st));
+    return flag_result(s);
 }
 template wg_status scene_step_impl<double>(wg_scene *, int);
 
@@ -408,8 +426,7 @@ wg_status wg_scene_download(wg_scene *s, void *phi, void *psi, int32_t host_prec
         if (host_precision == WG_FP32) st = download_state32<float>(s, (float *)phi, (float *)psi);
         else if (host_precision == WG_FP64) st = download_state32<double>(s, (double *)phi, (double *)psi);
         else { set_error("download precision must be FP64 or the scene's"); return WG_ERR_INVALID; }
-        if (st) return st;
-        return scene_check_flag(s);
+        return st;
     }
     const void *src[2] = {s->f[s->cur], s->f[1 - s->cur]};
     void *dst[2] = {phi, psi};
