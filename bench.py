@@ -404,6 +404,7 @@ def run_ours(args):
     batch_res = run_batch(args, P, scenes, W, stream, rank) if not args.no_batch else None
     sweep_res = run_sweep(args, P, scenes, W, stream, rank) if not args.no_sweep else None
     serve_res = run_serving(args, P, scenes, W, stream, rank) if not args.no_serving else None
+    fd_res = run_frames_domain(args, P, scenes, W, stream, rank, sc) if not args.no_frames else None
 
     if rank != 0:
         return 0
@@ -476,6 +477,8 @@ def run_ours(args):
         line["sweep"] = sweep_res
     if serve_res:
         line["serving"] = serve_res
+    if fd_res:
+        line.update(fd_res)
     print(json.dumps(line))
     return 0
 
@@ -757,6 +760,85 @@ def run_serving(args, P, scenes, W, stream, rank):
     return out
 
 
+PLOT_NAMES = ["amplitude", "energy", "mixed", "mean_energy", "log_energy", "log_mean_energy", "energy_flux",
+              "total_energy_flux", "average_energy", "log_average_energy"]
+
+
+def run_frames_domain(args, P, scenes, W, stream, rank, sc):
+    """Untimed legs on the config-2 grid (rank 0): the colour-mapped frame (size 2) in every
+    plot mode into device memory, device time per frame from CUDA events over repeated
+    calls, and the amplitude frame copied to host memory; and the device-side mask and
+    tables builder for the config's 64 discs against the host builder (numpy)."""
+    if rank != 0:
+        return None
+    import ctypes
+    import numpy as np
+    import torch
+    lut, lut_name = frame_palette()
+    lut = np.ascontiguousarray(lut, np.uint8)
+    lib = W.lib()
+    p = sc.params
+    size, reps = 2, 10
+    s = W.Scene(p, P.FP32, P.COEF_TABLE, stream=stream.cuda_stream)
+    s.upload(sc.phi, sc.psi, sc.xy, sc.tcc, sc.tc, sc.tgamma)
+    s.step(200)
+    pixels = (p.nx // size) * (p.ny // size)
+    d_out = torch.empty(pixels * 3, dtype=torch.uint8, device=torch.device("cuda", torch.cuda.current_device()))
+    h_out = np.zeros(pixels * 3, np.uint8)
+    modes = {}
+    for plot, name in enumerate(PLOT_NAMES):
+        fp = P.WgFrameParams(size, 0, -0.2, 1.0, 1.0, 0.8, 1.0, 1.0, 0, plot, 0.75, 0.75, 250.0, 0.95, 0.0, 0, 0)
+        s.frame_reset()
+        call = lambda: W.check(lib.wg_scene_frame_rgb8(s.h, ctypes.byref(fp), lut.ctypes.data, None,
+                                                       ctypes.c_void_p(d_out.data_ptr())))
+        for _ in range(2):
+            call()
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for _ in range(reps):
+            call()
+        e1.record(stream)
+        e1.synchronize()
+        us = 1e3 * e0.elapsed_time(e1) / reps
+        modes[name] = {"us_per_call": us, "mpixel_per_s": pixels / us}
+    fp = P.WgFrameParams(size, 0, -0.2, 1.0, 1.0, 0.8, 1.0, 1.0, 0, P.P_AMPLITUDE, 0.75, 0.75, 250.0, 0.95, 0.0, 0, 0)
+    t0 = time.perf_counter()
+    for _ in range(reps):
+        W.check(lib.wg_scene_frame_rgb8(s.h, ctypes.byref(fp), lut.ctypes.data, h_out.ctypes.data, None))
+    host_us = 1e6 * (time.perf_counter() - t0) / reps
+    s.close()
+    frames = {"grid": f"{p.nx}x{p.ny}", "size": size, "pixels": pixels, "palette": lut_name, "modes": modes,
+              "amplitude_to_host_us": host_us,
+              "definition": "time per wg_scene_frame_rgb8 call into device memory (CUDA events over "
+                            f"{reps} back-to-back calls after 2 untimed; each call ends with its stream's "
+                            "synchronisation, so the host's turnaround between calls is included), FP32 fields "
+                            "after 200 updates; the amplitude frame to host memory on the host clock, copy "
+                            "included"}
+    # the mask and tables of the config's discs: on the device, and by the host builder
+    discs = np.asarray(sc.meta["discs"], np.float64)
+    s = W.Scene(p, P.FP32, P.COEF_TABLE, stream=stream.cuda_stream)
+    s.build_domain(scenes.D_CIRCLES, circles=discs)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(3):
+        s.build_domain(scenes.D_CIRCLES, circles=discs)
+    torch.cuda.synchronize()
+    dev_ms = 1e3 * (time.perf_counter() - t0) / 3
+    same = bool(np.array_equal(s.download_mask(), sc.xy))
+    s.close()
+    t0 = time.perf_counter()
+    xy = scenes.mask(p, scenes.D_CIRCLES, circles=sc.meta["discs"])
+    scenes.tables(p, xy)
+    host_ms = 1e3 * (time.perf_counter() - t0)
+    domain = {"grid": f"{p.nx}x{p.ny}", "shape": f"{len(discs)} discs, two-medium tables",
+              "device_ms": dev_ms, "host_builder_ms": host_ms, "mask_equals_host": same,
+              "definition": "wg_scene_build_domain (mask bit planes and init_ior_2d's tables on the device; "
+                            "host clock, synchronised, mean of 3 after one untimed) against scenes.mask + "
+                            "scenes.tables (numpy, one thread)"}
+    return {"frames": frames, "domain_build": domain}
+
+
 def frame_palette():
     """(256x3 bytes, name): the reference's turbo palette (turbo_srgb_bytes of
     turbo_colormap.c), read as data from the snapshot of the reference's sources kept
@@ -841,6 +923,7 @@ def main():
     ap.add_argument("--no-batch", action="store_true")
     ap.add_argument("--no-serving", action="store_true")
     ap.add_argument("--no-sweep", action="store_true")
+    ap.add_argument("--no-frames", action="store_true", help="skip the frame and domain-builder legs")
     ap.add_argument("--no-accuracy", action="store_true")
     ap.add_argument("--accuracy-updates", type=int, default=ACCURACY_UPDATES,
                     help="updates of the accuracy leg against the reference (a multiple of 100)")

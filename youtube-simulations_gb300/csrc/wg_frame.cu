@@ -222,8 +222,7 @@ extern "C" wg_status wg_scene_frame_rgb8(wg_scene *s, const wg_frame_params *fp,
         return st;
     s->launches++;
     if (rgb_host) WG_CUDA(cudaMemcpyAsync(rgb_host, dst, bytes, cudaMemcpyDeviceToHost, s->st));
-    WG_CUDA(cudaStreamSynchronize(s->st));
-    return scene_check_flag(s);
+    return scene_check_flag(s);  // synchronises the stream (the image is ready on return)
 }
 
 extern "C" wg_status wg_scene_frame_reset(wg_scene *s)

@@ -216,7 +216,7 @@ static wg_status flag_result(wg_scene *s)
     return WG_OK;
 }
 
-// Reads (and clears) the flag.
+// Synchronises the scene's stream and reads (and clears) the flag, one synchronisation.
 wg_status scene_check_flag(wg_scene *s)
 {
     if (wg_status st = flag_copy(s)) return st;
@@ -443,8 +443,7 @@ wg_status wg_scene_download(wg_scene *s, void *phi, void *psi, int32_t host_prec
             return WG_ERR_INVALID;
         }
     }
-    WG_CUDA(cudaStreamSynchronize(s->st));
-    return scene_check_flag(s);
+    return scene_check_flag(s);  // one synchronisation for the copies and the flag
 }
 
 wg_status wg_scene_set_neumann(wg_scene *s, const wg_neumann_bc *r, int32_t n)
