@@ -405,6 +405,7 @@ def run_ours(args):
     sweep_res = run_sweep(args, P, scenes, W, stream, rank) if not args.no_sweep else None
     serve_res = run_serving(args, P, scenes, W, stream, rank) if not args.no_serving else None
     fd_res = run_frames_domain(args, P, scenes, W, stream, rank, sc) if not args.no_frames else None
+    di_res = run_dropin(args, P, W, rank, sc) if not args.no_frames else None
 
     if rank != 0:
         return 0
@@ -479,6 +480,8 @@ def run_ours(args):
         line["serving"] = serve_res
     if fd_res:
         line.update(fd_res)
+    if di_res:
+        line["dropin"] = di_res
     print(json.dumps(line))
     return 0
 
@@ -839,6 +842,41 @@ def run_frames_domain(args, P, scenes, W, stream, rank, sc):
     return {"frames": frames, "domain_build": domain}
 
 
+def run_dropin(args, P, W, rank, sc):
+    """Untimed leg on the config-2 grid (rank 0): the drop-in evolve_wave of
+    include/wavegpu_dropin.h (FP64, the reference's operation order, its int16 mask and three
+    FP64 tables, three buffers) on the reference's row-pointer fields, in resident mode (the
+    fields stay in HBM between calls) and in strict mode (every call copies the fields and
+    tables in and out, as a reference program calling it unchanged would).  Host clock over
+    whole calls, with a device synchronisation at the end."""
+    if rank != 0:
+        return None
+    import numpy as np
+    import torch
+    p = sc.params
+    cells = p.nx * p.ny
+    out = {"grid": f"{p.nx}x{p.ny}", "updates_per_call": 3}
+    W.configure(p)
+    for mode, calls in (("resident", 30), ("strict", 3)):
+        W.set_mode(mode == "resident")
+        rf = W.RowFields(p, sc.phi, sc.psi, np.zeros_like(sc.phi), sc.xy, sc.tcc, sc.tc, sc.tgamma)
+        W.evolve_wave(rf)  # first call: uploads (resident) / warms up
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        for _ in range(calls):
+            W.evolve_wave(rf)
+        torch.cuda.synchronize()
+        dt = time.perf_counter() - t0
+        out[mode] = {"value": cells * 3 * calls / dt / 1e9, "unit": METRIC, "calls": calls,
+                     "ms_per_call": 1e3 * dt / calls}
+        W.invalidate()
+    W.set_mode(False)
+    out["definition"] = ("evolve_wave through the drop-in C ABI (3 updates per call), fields bit-identical to the "
+                         "reference's stepper; strict mode includes the host copies of phi, psi, tmp, the mask "
+                         "and the three tables every call")
+    return out
+
+
 def frame_palette():
     """(256x3 bytes, name): the reference's turbo palette (turbo_srgb_bytes of
     turbo_colormap.c), read as data from the snapshot of the reference's sources kept
@@ -923,7 +961,7 @@ def main():
     ap.add_argument("--no-batch", action="store_true")
     ap.add_argument("--no-serving", action="store_true")
     ap.add_argument("--no-sweep", action="store_true")
-    ap.add_argument("--no-frames", action="store_true", help="skip the frame and domain-builder legs")
+    ap.add_argument("--no-frames", action="store_true", help="skip the frame, domain-builder and drop-in legs")
     ap.add_argument("--no-accuracy", action="store_true")
     ap.add_argument("--accuracy-updates", type=int, default=ACCURACY_UPDATES,
                     help="updates of the accuracy leg against the reference (a multiple of 100)")

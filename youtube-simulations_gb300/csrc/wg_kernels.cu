@@ -27,6 +27,8 @@ __global__ void __launch_bounds__(256) k_step_exact(DevParams p, const double *_
                                                     const double *__restrict__ tc, const double *__restrict__ tg,
                                                     long long time, int do_source)
 {
+    pdl_wait();  // launched by launch_pdl: the previous update has completed
+    pdl_trigger();
     const int j = blockIdx.x * blockDim.x + threadIdx.x;
     const int i = blockIdx.y * blockDim.y + threadIdx.y;
     if (i >= p.nx || j >= p.ny) return;
@@ -648,7 +650,7 @@ void launch_step_exact(const DevParams &p, const double *phi, const double *psi,
                        cudaStream_t st)
 {
     dim3 blk(64, 4), grd((p.ny + 63) / 64, (p.nx + 3) / 4);
-    k_step_exact<<<grd, blk, 0, st>>>(p, phi, psi, out, xy, tcc, tc, tg, time, do_source);
+    launch_pdl(k_step_exact, grd, blk, 0, st, p, phi, psi, out, xy, tcc, tc, tg, time, do_source);
 }
 
 void launch_step_exact_energy(const DevParams &p, const double *phi, const double *psi, double *out,
