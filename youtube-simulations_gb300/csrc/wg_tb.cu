@@ -317,24 +317,66 @@ __device__ __forceinline__ XV skew_cell(const DevParams &p, const TbArgs &a, int
 }
 
 
-// skew_cell's inner rule (GEN = false) with the Laplacian given in differences.  Vertical:
-// vert = dn - dp with dn = n - x and dp = x - sv, which equals (n - x) + (sv - x) exactly
-// (round to nearest is symmetric, so sv - x == -(x - sv)); dp is the previous row's dn,
-// so each row's difference is formed once per column.  Horizontal: he = e - x and
-// hw = x - w, (e - x) + (w - x) == he - hw exactly, and a lane's four cells share the
-// five differences of its row.  4 operations per cell for the Laplacian instead of 7.
-template <int COEF, bool PLAIN, bool KZ = false>
-__device__ __forceinline__ XV skew_inner(const DevParams &p, const TbArgs &a, float x, float y, float vert, float he,
-                                         float hw, float cc, bool act)
+// Paired FP32 arithmetic: the two-wide add, sub and fma of this GPU (.f32x2) round each
+// element exactly as the scalar instruction does, so two cells computed together get the
+// same bits as two computed one at a time, for one instruction issued instead of two.
+__device__ __forceinline__ float2 add2(float2 a, float2 b) { return __fadd2_rn(a, b); }
+__device__ __forceinline__ float2 fma2(float2 a, float2 b, float2 c) { return __ffma2_rn(a, b, c); }
+__device__ __forceinline__ float2 sub2(float2 a, float2 b)
 {
-    const float ccv = (COEF == WG_COEF_TABLE) ? cc : (act ? a.c2 : a.c2b);
-    const float g = (COEF == WG_COEF_TABLE) ? a.gam : (act ? a.gam : a.gamb);
-    const float lap = vert + (he - hw);
-    if (PLAIN && KZ) return upd32_k0(x, y, ccv, lap, g);
-    if (PLAIN) return upd32(x, y, ccv, lap, a.kappa, g);
-    XV r = updkeep32(p.twospeeds || act, x, y, ccv, lap, a.kappa, g);
-    if (p.floor_clamp && act) r = clamp32(x, r, a.vmax);
-    return r;
+    float2 d;
+    asm("{\n\t.reg .b64 ra, rb, rd;\n\tmov.b64 ra, {%2, %3};\n\tmov.b64 rb, {%4, %5};\n\t"
+        "sub.rn.f32x2 rd, ra, rb;\n\tmov.b64 {%0, %1}, rd;\n\t}"
+        : "=f"(d.x), "=f"(d.y)
+        : "f"(a.x), "f"(a.y), "f"(b.x), "f"(b.y));
+    return d;
+}
+// element c (0..3) of a lane's four cells held as the pairs (0, 1) and (2, 3)
+__device__ __forceinline__ float el(const float2 (&q)[2], int c)
+{
+    return (c & 2) ? ((c & 1) ? q[1].y : q[1].x) : ((c & 1) ? q[0].y : q[0].x);
+}
+
+// skew_cell's inner rule (GEN = false) for the two cells of a pair, with the Laplacian
+// given in differences.  Vertical: vert = dn - dp with dn = n - x and dp = x - sv, which
+// equals (n - x) + (sv - x) exactly (round to nearest is symmetric, so sv - x == -(x - sv));
+// dp is the previous row's dn, so each row's difference is formed once per column.
+// Horizontal: hh = he - hw with he = e - x and hw = x - w, (e - x) + (w - x) == he - hw
+// exactly, and a lane's four cells share the five differences of their row.  x, y, vert,
+// cc: the cells' phi, velocity, vertical part and tcc.  New phi in xo, new velocity in vo:
+// upd32_k0 (PLAIN, KZ), upd32 (PLAIN) or updkeep32 and clamp32, element by element.
+template <int COEF, bool PLAIN, bool KZ = false>
+__device__ __forceinline__ void skew_inner2(const DevParams &p, const TbArgs &a, float2 x, float2 y, float2 vert,
+                                            float2 hh, float2 cc, bool act0, bool act1, float2 &xo, float2 &vo)
+{
+    const float2 ccv = (COEF == WG_COEF_TABLE) ? cc : make_float2(act0 ? a.c2 : a.c2b, act1 ? a.c2 : a.c2b);
+    const float2 ng = (COEF == WG_COEF_TABLE) ? make_float2(-a.gam, -a.gam)
+                                              : make_float2(act0 ? -a.gam : -a.gamb, act1 ? -a.gam : -a.gamb);
+    const float2 lap = add2(vert, hh);
+    float2 vn;
+    if (PLAIN && KZ) {
+        vn = fma2(ccv, lap, fma2(ng, y, y));                                    // upd32_k0
+    } else {
+        vn = fma2(ccv, lap, fma2(make_float2(-a.kappa, -a.kappa), x, fma2(ng, y, y)));  // vel32
+        if (!PLAIN) {                                                           // updkeep32
+            if (!(p.twospeeds || act0)) vn.x = -y.x;
+            if (!(p.twospeeds || act1)) vn.y = -y.y;
+        }
+    }
+    xo = add2(x, vn);
+    vo = vn;
+    if (!PLAIN && p.floor_clamp) {
+        if (act0) {
+            const XV r = clamp32(x.x, XV{xo.x, vo.x}, a.vmax);
+            xo.x = r.x;
+            vo.x = r.v;
+        }
+        if (act1) {
+            const XV r = clamp32(x.y, XV{xo.y, vo.y}, a.vmax);
+            xo.y = r.x;
+            vo.y = r.v;
+        }
+    }
 }
 
 // ---------------------------------------------------------------------------
@@ -365,7 +407,7 @@ __device__ __forceinline__ float pick4(float a0, float a1, float a2, float a3, i
 // Column 0 (right = false) or ny-1 (right = true) at a row 1..nx-2: the boundary rule of
 // evolve_wave_half for the top/bottom lines (wave_billiard.c:366-452, B_COND Dirichlet or
 // absorbing, OSCILLATE_TOPBOT), same branches as skew_cell's general form.  vert: the
-// vertical part of the Laplacian, (n - x) + (sv - x), as skew_inner takes it.
+// vertical part of the Laplacian, (n - x) + (sv - x), as skew_inner2 takes it.
 template <int COEF>
 __device__ __forceinline__ XV col_edge_cell(const DevParams &p, const TbArgs &a, int gi, float x, float y, float vert,
                                             float e, float w, float cc, float tcv, bool act, bool right)
@@ -445,15 +487,17 @@ __device__ __forceinline__ void skew_strip(const DevParams &p, const TbArgs &a, 
     const int ce = !edge ? -1 : (gj0 == 0 ? 0 : (cr >= 0 && cr <= 3 ? cr : -1));
     const bool src_lane = edge && p.src_on && p.src_j >= gj0 && p.src_j < gj0 + 4;
 
-    float W[K + 1][3][4];  // W[s][k][c] = phi of level s at row m-s-2+k, column gj0+c (k = 0: GEN only)
-    // Dp[s][c] = phi_s(m-s-1) - phi_s(m-s-2): the vertical difference level s+1 formed in
-    // the previous trip, its dp in this one (not GEN)
-    float Dp[K][4];
-    // V[s][c] = velocity of level s at row m-s-1, column gj0+c, until level s+1 of the trip
-    // for row m has read it; pend[c] = the new velocity row of the level just computed.
-    // (Kept in a per-warp shared-memory row per level instead, the single-grid pass ran as
-    // fast at its best depth and the batch passes 8% slower.)
-    float V[K][4], pend[4];
+    // The lane's four cells are held as two pairs, (gj0, gj0+1) and (gj0+2, gj0+3), for
+    // the paired instructions; el(q, c) reads cell c.
+    float2 W[K + 1][3][2];  // W[s][k] = phi of level s at row m-s-2+k (k = 0: GEN only)
+    // Dp[s] = phi_s(m-s-1) - phi_s(m-s-2): the vertical difference level s+1 formed in the
+    // previous trip, its dp in this one (not GEN)
+    float2 Dp[K][2];
+    // V[s] = velocity of level s at row m-s-1, until level s+1 of the trip for row m has
+    // read it; pend = the new velocity row of the level just computed.  (Kept in a per-warp
+    // shared-memory row per level instead, the single-grid pass ran as fast at its best
+    // depth and the batch passes 8% slower.)
+    float2 V[K][2], pend[2];
     // tcc at rows m, m-1, ..., m-K (table scenes): the warp's shared ring tring of K+1 rows
     // (slot ts holds row m), each lane writing and reading back only its own 16 bytes
     int ts = 0;
@@ -462,9 +506,9 @@ __device__ __forceinline__ void skew_strip(const DevParams &p, const TbArgs &a, 
 #pragma unroll
     for (int q = 0; q <= K; q++) {
 #pragma unroll
-        for (int c = 0; c < 4; c++) {
-            W[q][0][c] = W[q][1][c] = W[q][2][c] = 0.f;
-            if (q < K) V[q][c] = Dp[q][c] = 0.f;
+        for (int h = 0; h < 2; h++) {
+            W[q][0][h] = W[q][1][h] = W[q][2][h] = make_float2(0.f, 0.f);
+            if (q < K) V[q][h] = Dp[q][h] = make_float2(0.f, 0.f);
         }
         TE[q] = 0.f;
     }
@@ -511,19 +555,19 @@ __device__ __forceinline__ void skew_strip(const DevParams &p, const TbArgs &a, 
                                                       : make_float4(0.f, 0.f, 0.f, 0.f);
             const uint32_t aw = NEED_ACT ? reinterpret_cast<const uint32_t *>(b)[SL::ACT + lane] : 0u;
             const float tein = need_tce ? b[SL::TCE + lane] : 0.f;
-            const float xin[4] = {xq.x, xq.y, xq.z, xq.w};
-            const float yin[4] = {yq.x, yq.y, yq.z, yq.w};
+            const float2 xin[2] = {make_float2(xq.x, xq.y), make_float2(xq.z, xq.w)};
+            const float2 yin[2] = {make_float2(yq.x, yq.y), make_float2(yq.z, yq.w)};
             if (COEF == WG_COEF_TABLE) *reinterpret_cast<float4 *>(tring + ts * 128 + 4 * lane) = cq;
             if (NEED_ACT) aq = (aq << 4) | ((aw >> (gj0 & 31)) & 0xFu);
             // the slot of row m-1 (read in the previous row) takes row m+QD
             issue(m + QD, slot == 0 ? D - 1 : slot - 1);
             slot = (slot == D - 1) ? 0 : slot + 1;
 #pragma unroll
-            for (int c = 0; c < 4; c++) {
-                if (GEN) W[0][0][c] = W[0][1][c];
-                W[0][1][c] = W[0][2][c];
-                W[0][2][c] = xin[c];
-                pend[c] = yin[c];
+            for (int h = 0; h < 2; h++) {
+                if (GEN) W[0][0][h] = W[0][1][h];
+                W[0][1][h] = W[0][2][h];
+                W[0][2][h] = xin[h];
+                pend[h] = yin[h];
             }
             if (need_tce) {  // warp-uniform: only tiles that hold a boundary column read TE
 #pragma unroll
@@ -538,40 +582,47 @@ __device__ __forceinline__ void skew_strip(const DevParams &p, const TbArgs &a, 
                 // difference (formed in every trip, so that the first active trip of the
                 // level finds its dp), or from the three rows in GEN strips, which keep them
                 // for the general rule
-                float vt[4];
+                float2 vt2[2];
 #pragma unroll
-                for (int c = 0; c < 4; c++) {
+                for (int h = 0; h < 2; h++) {
                     if (GEN) {
-                        vt[c] = (W[lv - 1][2][c] - W[lv - 1][1][c]) + (W[lv - 1][0][c] - W[lv - 1][1][c]);
+                        vt2[h] = add2(sub2(W[lv - 1][2][h], W[lv - 1][1][h]), sub2(W[lv - 1][0][h], W[lv - 1][1][h]));
                     } else {
-                        const float dn = W[lv - 1][2][c] - W[lv - 1][1][c];
-                        vt[c] = dn - Dp[lv - 1][c];
-                        Dp[lv - 1][c] = dn;
+                        const float2 dn = sub2(W[lv - 1][2][h], W[lv - 1][1][h]);
+                        vt2[h] = sub2(dn, Dp[lv - 1][h]);
+                        Dp[lv - 1][h] = dn;
                     }
                 }
                 // Level lv at row r reaches the stored rows only from r >= i_s - K + lv on, i.e.
                 // from input row m0 + 2 lv + 1: in the pipeline fill the earlier levels are skipped
                 // (warp-uniform), and their window slots hold zeros that nothing reads.
                 if (m - m0 >= 2 * lv + 1) {
-                const float *Wc = W[lv - 1][1];
-                const float *Yl = V[lv - 1];  // velocity of level lv-1 at row r
-                float Tl[4] = {0.f, 0.f, 0.f, 0.f};  // tcc at row r
+                // per-cell views of the pairs, for the horizontal differences and the edge rules
+                const float Wc[4] = {W[lv - 1][1][0].x, W[lv - 1][1][0].y, W[lv - 1][1][1].x, W[lv - 1][1][1].y};
+                const float Yl[4] = {V[lv - 1][0].x, V[lv - 1][0].y, V[lv - 1][1].x, V[lv - 1][1].y};  // row r
+                const float vt[4] = {vt2[0].x, vt2[0].y, vt2[1].x, vt2[1].y};
+                float2 Tl2[2] = {make_float2(0.f, 0.f), make_float2(0.f, 0.f)};  // tcc at row r
                 if (COEF == WG_COEF_TABLE) {
                     const int tsl = ts >= lv ? ts - lv : ts - lv + K + 1;
                     const float4 tq = *reinterpret_cast<const float4 *>(tring + tsl * 128 + 4 * lane);
-                    Tl[0] = tq.x;
-                    Tl[1] = tq.y;
-                    Tl[2] = tq.z;
-                    Tl[3] = tq.w;
+                    Tl2[0] = make_float2(tq.x, tq.y);
+                    Tl2[1] = make_float2(tq.z, tq.w);
                 }
+                const float Tl[4] = {Tl2[0].x, Tl2[0].y, Tl2[1].x, Tl2[1].y};
                 const float e3 = __shfl_down_sync(0xffffffffu, Wc[0], 1);
                 const float w0 = __shfl_up_sync(0xffffffffu, Wc[3], 1);
-                // hd[c] = x(gj0+c) - x(gj0+c-1): cell c's e - x is hd[c+1], its x - w is hd[c]
+                // hd[c] = x(gj0+c) - x(gj0+c-1): cell c's e - x is hd[c+1], its x - w is hd[c];
+                // the horizontal part of cell c is hd[c+1] - hd[c]
                 const float hd[5] = {Wc[0] - w0, Wc[1] - Wc[0], Wc[2] - Wc[1], Wc[3] - Wc[2], e3 - Wc[3]};
+                const float2 hh[2] = {make_float2(hd[1] - hd[0], hd[2] - hd[1]), make_float2(hd[3] - hd[2], hd[4] - hd[3])};
 #pragma unroll
-                for (int c = 0; c < 4; c++) {
-                    const bool act = NEED_ACT ? ((aq >> (4 * lv + c)) & 1u) : true;
-                    v[c] = skew_inner<COEF, PLAIN, KZ>(p, a, Wc[c], Yl[c], vt[c], hd[c + 1], hd[c], Tl[c], act);
+                for (int h = 0; h < 2; h++) {
+                    const bool a0 = NEED_ACT ? ((aq >> (4 * lv + 2 * h)) & 1u) : true;
+                    const bool a1 = NEED_ACT ? ((aq >> (4 * lv + 2 * h + 1)) & 1u) : true;
+                    float2 xo, vo;
+                    skew_inner2<COEF, PLAIN, KZ>(p, a, W[lv - 1][1][h], V[lv - 1][h], vt2[h], hh[h], Tl2[h], a0, a1, xo, vo);
+                    v[2 * h] = XV{xo.x, vo.x};
+                    v[2 * h + 1] = XV{xo.y, vo.y};
                 }
                 if (!GEN && edge) {  // warp-uniform
                     if (ce >= 0 && r > 0 && r < p.nx - 1) {  // the lane holding column 0 (c = 0) or ny-1 (c = 3)
@@ -612,8 +663,8 @@ __device__ __forceinline__ void skew_strip(const DevParams &p, const TbArgs &a, 
                             const float tcv = (COEF == WG_COEF_TABLE && a.tc) ? a.tc[(size_t)r * p.pitch + gj] : 0.f;
                             const XV res = skew_cell<COEF, true, false, INL>(
                                 p, a, r, gj, lv, pick4(Wc[0], Wc[1], Wc[2], Wc[3], c), pick4(Yl[0], Yl[1], Yl[2], Yl[3], c),
-                                pick4(W[lv - 1][2][0], W[lv - 1][2][1], W[lv - 1][2][2], W[lv - 1][2][3], c),
-                                pick4(W[lv - 1][0][0], W[lv - 1][0][1], W[lv - 1][0][2], W[lv - 1][0][3], c),
+                                pick4(el(W[lv - 1][2], 0), el(W[lv - 1][2], 1), el(W[lv - 1][2], 2), el(W[lv - 1][2], 3), c),
+                                pick4(el(W[lv - 1][0], 0), el(W[lv - 1][0], 1), el(W[lv - 1][0], 2), el(W[lv - 1][0], 3), c),
                                 pick4(Wc[1], Wc[2], Wc[3], e3, c), pick4(w0, Wc[0], Wc[1], Wc[2], c),
                                 pick4(Tl[0], Tl[1], Tl[2], Tl[3], c), tcv,
                                 NEED_ACT ? ((aq >> (4 * lv + c)) & 1u) : true);
@@ -631,12 +682,12 @@ __device__ __forceinline__ void skew_strip(const DevParams &p, const TbArgs &a, 
                 }
                 }  // levels in use
 #pragma unroll
-                for (int c = 0; c < 4; c++) {
-                    if (GEN) W[lv][0][c] = W[lv][1][c];
-                    W[lv][1][c] = W[lv][2][c];
-                    W[lv][2][c] = v[c].x;
-                    V[lv - 1][c] = pend[c];  // level lv-1's row r+1: level lv has read row r
-                    pend[c] = v[c].v;
+                for (int h = 0; h < 2; h++) {
+                    if (GEN) W[lv][0][h] = W[lv][1][h];
+                    W[lv][1][h] = W[lv][2][h];
+                    W[lv][2][h] = make_float2(v[2 * h].x, v[2 * h + 1].x);
+                    V[lv - 1][h] = pend[h];  // level lv-1's row r+1: level lv has read row r
+                    pend[h] = make_float2(v[2 * h].v, v[2 * h + 1].v);
                 }
             }
             ts = (ts == K) ? 0 : ts + 1;  // row m+1's tcc slot
@@ -645,15 +696,15 @@ __device__ __forceinline__ void skew_strip(const DevParams &p, const TbArgs &a, 
                 const size_t o = (size_t)r * p.pitch + gj0;
                 if (gj0 + 3 < p.ny) {
                     if (grp_ok) {
-                        *reinterpret_cast<float4 *>(a.phi_out + o) = make_float4(W[K][2][0], W[K][2][1], W[K][2][2], W[K][2][3]);
-                        *reinterpret_cast<float4 *>(a.psi_out + o) = make_float4(pend[0], pend[1], pend[2], pend[3]);
+                        *reinterpret_cast<float4 *>(a.phi_out + o) = make_float4(W[K][2][0].x, W[K][2][0].y, W[K][2][1].x, W[K][2][1].y);
+                        *reinterpret_cast<float4 *>(a.psi_out + o) = make_float4(pend[0].x, pend[0].y, pend[1].x, pend[1].y);
                     }
                 } else if (grp_ok) {
 #pragma unroll
                     for (int c = 0; c < 4; c++)
                         if (gj0 + c < p.ny) {
-                            a.phi_out[o + c] = W[K][2][c];
-                            a.psi_out[o + c] = pend[c];
+                            a.phi_out[o + c] = el(W[K][2], c);
+                            a.psi_out[o + c] = el(pend, c);
                         }
                 }
             }
