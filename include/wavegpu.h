@@ -229,7 +229,12 @@ wg_status wg_scene_bytes(const wg_params *p, int32_t precision, int32_t coef_mod
  * to the scene precision on the device (FP32: phi and the FP64 difference phi - psi). */
 wg_status wg_scene_upload(wg_scene *s, const double *phi, const double *psi, const int16_t *xy_in,
                           const double *tcc, const double *tc, const double *tgamma);
-/* Uploads only phi/psi (the state), from FP64 or from the scene's own precision. */
+/* Uploads only phi/psi (the state), from FP64 or from the scene's own precision.  From
+ * arrays in an FP32 scene's own precision the call returns without waiting: page-locked
+ * arrays are read by the device in stream order (leave them unchanged until a call that
+ * waits: energy, download, sync), pageable arrays are copied before the call returns.
+ * Page-locked host arrays (cudaHostAlloc, cudaHostRegister) of FP32 scenes are read and
+ * written by the device in place, over the host link, with no staging copy. */
 wg_status wg_scene_upload_state(wg_scene *s, const void *phi, const void *psi, int32_t host_precision);
 wg_status wg_scene_set_neumann(wg_scene *s, const wg_neumann_bc *recs, int32_t n);
 /* Advances nsteps leapfrog updates (one kernel pass per temporal block). */

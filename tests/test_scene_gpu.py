@@ -131,6 +131,72 @@ def test_state_roundtrip_and_time():
         assert s.time == 103
 
 
+def _special_pairs(n, seed):
+    """FP32 (phi, psi) rows: normals, then signed zeros, subnormals, differences that
+    overflow FP32 and exponent gaps wider than FP32 can hold in one difference."""
+    rng = np.random.default_rng(seed)
+    a = rng.standard_normal(n).astype(np.float32)
+    b = rng.standard_normal(n).astype(np.float32)
+    tiny = np.float32(1.4e-45)
+    sa = np.array([0.0, -0.0, 0.0, -0.0, tiny, -tiny, 3 * tiny, 1.2e-38, 3.0e38, -3.0e38, 1.0e30, 1.0e-30,
+                   1.0, 16777217.0, 1.0e8], np.float32)
+    sb = np.array([0.0, 0.0, -0.0, -0.0, tiny, 2 * tiny, -tiny, 1.1e-38, -3.0e38, 3.0e38, 1.0e-30, 1.0e30,
+                   5.9604645e-08, 1.0, -3.0e-8], np.float32)
+    a[:len(sa)] = sa
+    b[:len(sb)] = sb
+    return a, b
+
+
+def test_state_special_values():
+    """The velocity phi - psi and psi = phi - v are formed by the FP32 subtraction for FP32
+    host rows; they must equal the FP64 difference rounded once to FP32, bit for bit, on
+    signed zeros, subnormals, overflow and wide exponent gaps."""
+    p, f, xy, _ = variant_inputs("s_per", seed=9)
+    n = p.nx * p.ny
+    a, b = _special_pairs(n, 3)
+    with W.Scene(p, P.FP32, P.COEF_MASK) as s:
+        s.upload(f["phi"], f["psi"], xy)
+        s.upload_state(a, b)
+        x, y = s.download(native=True)
+        with np.errstate(over="ignore"):
+            v = (a.astype(np.float64) - b.astype(np.float64)).astype(np.float32)
+            want = (a.astype(np.float64) - v.astype(np.float64)).astype(np.float32)
+        assert np.array_equal(x.view(np.uint32), a.view(np.uint32))
+        assert np.array_equal(y.view(np.uint32), want.view(np.uint32))
+
+
+def test_state_in_place_page_locked():
+    """Page-locked host rows are read and written by the device in place (no staging copy):
+    the same bits as pageable rows, from and to FP32 and FP64 host arrays."""
+    torch = pytest.importorskip("torch")
+    p, f, xy, _ = variant_inputs("s_per", seed=9)
+    n = p.nx * p.ny
+    a32, b32 = _special_pairs(n, 4)
+    lib = W.lib()
+    with W.Scene(p, P.FP32, P.COEF_MASK) as s:
+        s.upload(f["phi"], f["psi"], xy)
+        for prec, dt in ((P.FP32, np.float32), (P.FP64, np.float64)):
+            a, b = a32.astype(dt), b32.astype(dt)
+            if dt == np.float64:
+                a[len(a) // 2:] += 1e-12 * b[len(a) // 2:]  # values FP32 cannot hold
+            W.check(lib.wg_scene_upload_state(s.h, a.ctypes.data, b.ctypes.data, prec))
+            W.check(lib.wg_scene_sync(s.h))
+            x0, y0 = np.empty(n, dt), np.empty(n, dt)
+            W.check(lib.wg_scene_download(s.h, x0.ctypes.data, y0.ctypes.data, prec))
+            ha, hb = torch.from_numpy(a).pin_memory(), torch.from_numpy(b).pin_memory()
+            hx, hy = torch.empty(n, dtype=ha.dtype).pin_memory(), torch.empty(n, dtype=ha.dtype).pin_memory()
+            W.check(lib.wg_scene_upload_state(s.h, ha.data_ptr(), hb.data_ptr(), prec))
+            W.check(lib.wg_scene_download(s.h, hx.data_ptr(), hy.data_ptr(), prec))
+            x1, y1 = hx.numpy(), hy.numpy()
+            assert np.array_equal(x0.view(np.uint8), x1.view(np.uint8))
+            assert np.array_equal(y0.view(np.uint8), y1.view(np.uint8))
+            # phi alone, into a view that starts 4 elements into its page-locked allocation
+            big = torch.zeros(n + 4, dtype=ha.dtype).pin_memory()
+            W.check(lib.wg_scene_download(s.h, big.data_ptr() + 4 * big.element_size(), None, prec))
+            assert np.array_equal(big.numpy()[4:].view(np.uint8), x0.view(np.uint8))
+            assert not big.numpy()[:4].any()
+
+
 def test_state_copies_are_stream_ordered():
     """wg_scene_upload_state returns before its copies and repacks finish: a state upload
     followed at once, with no sync, by a step and a download (the end-to-end step) gives

@@ -60,6 +60,10 @@ wg_status cuda_fail(cudaError_t e, const char *what);
         if (e_ != cudaSuccess) return cuda_fail(e_, #call); \
     } while (0)
 
+// device address of mapped page-locked host memory covering [p, p + bytes), else nullptr
+// (wg_scene.cu)
+void *mapped_host(const void *p, size_t bytes);
+
 DevParams make_dev_params(const wg_params &p, int pitch);
 wg_status validate_params(const wg_params &p);
 int pitch_for(int ny, int elem_bytes);

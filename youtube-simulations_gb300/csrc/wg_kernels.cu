@@ -578,9 +578,15 @@ __global__ void k_convert_out(int nx, int ny, int pitch, const T *__restrict__ s
     dst[(size_t)i * ny + j] = (double)src[(size_t)i * pitch + j];
 }
 
+// a - b of two floats rounded once to FP32, i.e. the FP32 subtraction.  The difference
+// computed in FP64 and then rounded to FP32 is the same value (53 >= 2*24 + 2 bits, so the
+// double rounding is innocuous for a sum of two floats), without the FP64 pipe.
+__device__ __forceinline__ float dif32(float a, float b) { return __fsub_rn(a, b); }
+
 // FP32 state from host (phi, psi) rows, dense [nx][ny] of H = double or float: phi
-// rounded once, the velocity phi - psi computed in FP64 (exact for two floats) and
-// rounded once; padding zeroed.
+// rounded once, the velocity phi - psi computed exactly and rounded once (FP64 rows: in
+// FP64; FP32 rows: dif32); padding zeroed.  The rows may be the caller's page-locked
+// host memory, read in place.
 template <class H>
 __global__ void k_state_in32(int nx, int ny, int pitch, const H *__restrict__ phi, const H *__restrict__ psi,
                              float *__restrict__ x, float *__restrict__ v)
@@ -589,9 +595,15 @@ __global__ void k_state_in32(int nx, int ny, int pitch, const H *__restrict__ ph
     const int i = blockIdx.y;
     if (j >= pitch || i >= nx) return;
     const size_t o = (size_t)i * pitch + j, c = (size_t)i * ny + j;
-    const double a = j < ny ? (double)phi[c] : 0.0, b = j < ny ? (double)psi[c] : 0.0;
-    x[o] = (float)a;
-    v[o] = (float)S_(a, b);
+    if constexpr (sizeof(H) == 4) {
+        const float a = j < ny ? phi[c] : 0.f, b = j < ny ? psi[c] : 0.f;
+        x[o] = a;
+        v[o] = dif32(a, b);
+    } else {
+        const double a = j < ny ? phi[c] : 0.0, b = j < ny ? psi[c] : 0.0;
+        x[o] = (float)a;
+        v[o] = (float)S_(a, b);
+    }
 }
 // The same for FP32 host rows four columns per thread (ny a multiple of 4, so every dense
 // row starts on 16 bytes), padding zeroed.
@@ -608,12 +620,14 @@ __global__ void k_state_in32_v4(int nx, int ny, int pitch, const float4 *__restr
         a = phi[c];
         b = psi[c];
     }
-    const float4 dv = make_float4((float)S_(a.x, b.x), (float)S_(a.y, b.y), (float)S_(a.z, b.z), (float)S_(a.w, b.w));
+    const float4 dv = make_float4(dif32(a.x, b.x), dif32(a.y, b.y), dif32(a.z, b.z), dif32(a.w, b.w));
     *reinterpret_cast<float4 *>(x + o) = a;
     *reinterpret_cast<float4 *>(v + o) = dv;
 }
 
-// FP32 state to host rows: phi, and psi = phi - v in FP64 (rounded to H); either may be NULL.
+// FP32 state to host rows: phi, and psi = phi - v computed exactly and rounded once to H
+// (FP64 rows: in FP64; FP32 rows: dif32); either may be NULL.  The rows may be the caller's
+// page-locked host memory, written in place.
 template <class H>
 __global__ void k_state_out32(int nx, int ny, int pitch, const float *__restrict__ x, const float *__restrict__ v,
                               H *__restrict__ phi, H *__restrict__ psi)
@@ -622,9 +636,13 @@ __global__ void k_state_out32(int nx, int ny, int pitch, const float *__restrict
     const int i = blockIdx.y;
     if (j >= ny || i >= nx) return;
     const size_t o = (size_t)i * pitch + j, c = (size_t)i * ny + j;
-    const double a = (double)x[o];
+    const float a = x[o];
     if (phi) phi[c] = (H)a;
-    if (psi) psi[c] = (H)S_(a, (double)v[o]);
+    if constexpr (sizeof(H) == 4) {
+        if (psi) psi[c] = dif32(a, v[o]);
+    } else {
+        if (psi) psi[c] = S_((double)a, (double)v[o]);
+    }
 }
 // The same into FP32 host rows four columns per thread (ny a multiple of 4).
 __global__ void k_state_out32_v4(int nx, int ny, int pitch, const float *__restrict__ x, const float *__restrict__ v,
@@ -638,7 +656,7 @@ __global__ void k_state_out32_v4(int nx, int ny, int pitch, const float *__restr
     if (phi) phi[c] = a;
     if (psi) {
         const float4 b = *reinterpret_cast<const float4 *>(v + o);
-        psi[c] = make_float4((float)S_(a.x, b.x), (float)S_(a.y, b.y), (float)S_(a.z, b.z), (float)S_(a.w, b.w));
+        psi[c] = make_float4(dif32(a.x, b.x), dif32(a.y, b.y), dif32(a.z, b.z), dif32(a.w, b.w));
     }
 }
 

@@ -2,6 +2,7 @@
 // leapfrog, the new level overwriting psi) or FP32 (phi and the velocity phi - psi, each
 // update writing the other pair of fields), 1-bit masks, optional coefficient tables,
 // temporal blocking, energy diagnostics and colour-mapped frames.
+#include <cuda.h>
 #include <algorithm>
 #include <cmath>
 #include <cstring>
@@ -12,6 +13,48 @@
 using namespace wg;
 
 namespace wg {
+
+// Device address of host memory that kernels can read and write in place: page-locked
+// memory mapped into the device's address space (cudaHostAlloc, cudaMallocHost or
+// cudaHostRegister) whose allocation covers [p, p + bytes).  nullptr for pageable memory,
+// or when the driver cannot tell the allocation's range.  The range comes from the
+// driver's pointer attributes, reached through the runtime's entry-point query (the
+// library does not link libcuda itself).
+void *mapped_host(const void *p, size_t bytes)
+{
+    typedef CUresult (*PfnPtrAttr)(void *, CUpointer_attribute, CUdeviceptr);
+    static PfnPtrAttr attr = [] {
+        void *f = nullptr;
+        cudaDriverEntryPointQueryResult q;
+        if (cudaGetDriverEntryPointByVersion("cuPointerGetAttribute", &f, 12000, cudaEnableDefault, &q) != cudaSuccess ||
+            q != cudaDriverEntryPointSuccess)
+            f = nullptr;
+        cudaGetLastError();
+        return (PfnPtrAttr)f;
+    }();
+    if (!p || !bytes || !attr) return nullptr;
+    cudaPointerAttributes a;
+    if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
+        cudaGetLastError();
+        return nullptr;
+    }
+    if (a.type != cudaMemoryTypeHost || !a.devicePointer) return nullptr;
+    CUdeviceptr start = 0;
+    size_t size = 0;
+    if (attr(&start, CU_POINTER_ATTRIBUTE_RANGE_START_ADDR, (CUdeviceptr)(uintptr_t)p) != CUDA_SUCCESS ||
+        attr(&size, CU_POINTER_ATTRIBUTE_RANGE_SIZE, (CUdeviceptr)(uintptr_t)p) != CUDA_SUCCESS)
+        return nullptr;
+    const uintptr_t b = (uintptr_t)p;
+    if (b < (uintptr_t)start || b - (uintptr_t)start > size || bytes > size - (b - (uintptr_t)start)) return nullptr;
+    // the last byte must be reachable at the same offset from the device address
+    cudaPointerAttributes z;
+    if (cudaPointerGetAttributes(&z, (const char *)p + bytes - 1) != cudaSuccess) {
+        cudaGetLastError();
+        return nullptr;
+    }
+    if (z.type != cudaMemoryTypeHost || (char *)z.devicePointer != (char *)a.devicePointer + bytes - 1) return nullptr;
+    return a.devicePointer;
+}
 
 wg_status scene_alloc_dense_stage(wg_scene *s, size_t bytes)
 {
@@ -56,40 +99,57 @@ static wg_status upload_f64(wg_scene *s, const double *h, void *dev)
 static wg_status flag_copy(wg_scene *s);
 static wg_status flag_result(wg_scene *s);
 
-// FP32 scene state from host (phi, psi) rows of H (double or float): both staged
-// contiguously, then phi and the velocity phi - psi formed on the device.  sync: wait for
-// the copies (the host arrays may then be freed).
+// FP32 scene state from host (phi, psi) rows of H (double or float), phi and the velocity
+// phi - psi formed on the device.  Page-locked mapped rows are read in place by the
+// forming kernel, at the host link's rate (a copy engine reaches the same rate, and a
+// staged copy adds a pass over HBM); other rows are staged contiguously first.  sync: wait
+// for the reads (the host arrays may then be freed or changed).
 template <class H>
 static wg_status upload_state32(wg_scene *s, const H *phi, const H *psi, bool sync)
 {
     const size_t n = (size_t)s->prm.nx * s->prm.ny, bytes = n * sizeof(H);
-    wg_status st = scene_alloc_dense_stage(s, 2 * bytes);
-    if (st) return st;
-    H *stage = (H *)s->dstage;
-    WG_CUDA(cudaMemcpyAsync(stage, phi, bytes, cudaMemcpyHostToDevice, s->st));
-    WG_CUDA(cudaMemcpyAsync(stage + n, psi, bytes, cudaMemcpyHostToDevice, s->st));
-    launch_state_in32<H>(s->prm.nx, s->prm.ny, s->pitch, stage, stage + n, (float *)s->f[s->cur],
-                         (float *)s->f[1 - s->cur], s->st);
+    const H *mphi = (const H *)mapped_host(phi, bytes), *mpsi = (const H *)mapped_host(psi, bytes);
+    if (mphi && mpsi) {
+        launch_state_in32<H>(s->prm.nx, s->prm.ny, s->pitch, mphi, mpsi, (float *)s->f[s->cur],
+                             (float *)s->f[1 - s->cur], s->st);
+    } else {
+        wg_status st = scene_alloc_dense_stage(s, 2 * bytes);
+        if (st) return st;
+        H *stage = (H *)s->dstage;
+        WG_CUDA(cudaMemcpyAsync(stage, phi, bytes, cudaMemcpyHostToDevice, s->st));
+        WG_CUDA(cudaMemcpyAsync(stage + n, psi, bytes, cudaMemcpyHostToDevice, s->st));
+        launch_state_in32<H>(s->prm.nx, s->prm.ny, s->pitch, stage, stage + n, (float *)s->f[s->cur],
+                             (float *)s->f[1 - s->cur], s->st);
+    }
     s->launches++;
     WG_CUDA(cudaGetLastError());
     if (sync) WG_CUDA(cudaStreamSynchronize(s->st));
     return WG_OK;
 }
 
-// FP32 scene state to host (phi, psi) rows of H; either pointer may be NULL.
+// FP32 scene state to host (phi, psi) rows of H; either pointer may be NULL.  Page-locked
+// mapped rows are written in place by the forming kernel; other rows through a stage.
 template <class H>
 static wg_status download_state32(wg_scene *s, H *phi, H *psi)
 {
     const size_t n = (size_t)s->prm.nx * s->prm.ny, bytes = n * sizeof(H);
-    wg_status st = scene_alloc_dense_stage(s, 2 * bytes);
-    if (st) return st;
-    H *stage = (H *)s->dstage;
-    launch_state_out32<H>(s->prm.nx, s->prm.ny, s->pitch, (const float *)s->f[s->cur], (const float *)s->f[1 - s->cur],
-                          phi ? stage : nullptr, psi ? stage + n : nullptr, s->st);
-    s->launches++;
-    WG_CUDA(cudaGetLastError());
-    if (phi) WG_CUDA(cudaMemcpyAsync(phi, stage, bytes, cudaMemcpyDeviceToHost, s->st));
-    if (psi) WG_CUDA(cudaMemcpyAsync(psi, stage + n, bytes, cudaMemcpyDeviceToHost, s->st));
+    wg_status st;
+    H *mphi = phi ? (H *)mapped_host(phi, bytes) : nullptr, *mpsi = psi ? (H *)mapped_host(psi, bytes) : nullptr;
+    if ((!phi || mphi) && (!psi || mpsi)) {
+        launch_state_out32<H>(s->prm.nx, s->prm.ny, s->pitch, (const float *)s->f[s->cur],
+                              (const float *)s->f[1 - s->cur], mphi, mpsi, s->st);
+        s->launches++;
+        WG_CUDA(cudaGetLastError());
+    } else {
+        if ((st = scene_alloc_dense_stage(s, 2 * bytes))) return st;
+        H *stage = (H *)s->dstage;
+        launch_state_out32<H>(s->prm.nx, s->prm.ny, s->pitch, (const float *)s->f[s->cur],
+                              (const float *)s->f[1 - s->cur], phi ? stage : nullptr, psi ? stage + n : nullptr, s->st);
+        s->launches++;
+        WG_CUDA(cudaGetLastError());
+        if (phi) WG_CUDA(cudaMemcpyAsync(phi, stage, bytes, cudaMemcpyDeviceToHost, s->st));
+        if (psi) WG_CUDA(cudaMemcpyAsync(psi, stage + n, bytes, cudaMemcpyDeviceToHost, s->st));
+    }
     if ((st = flag_copy(s))) return st;
     WG_CUDA(cudaStreamSynchronize(s->st));
     return flag_result(s);
