@@ -133,6 +133,15 @@ enum { WG_DROPIN_STRICT = 0, WG_DROPIN_RESIDENT = 1 };
 wg_status wg_dropin_set_mode(int32_t mode);
 wg_status wg_dropin_sync(void);
 wg_status wg_dropin_invalidate(void);
+/* How the drop-in moves rows between the caller's row arrays and the GPU.
+ *  WG_ROWS_AUTO  : in place where the GPU can address the host's pageable memory
+ *                  (cudaDevAttrPageableMemoryAccess, e.g. a Grace host): kernels read
+ *                  and write the rows over the host link, with no host-side packing;
+ *                  elsewhere as WG_ROWS_PACKED.  The default.
+ *  WG_ROWS_PACKED: host threads pack the rows into a page-locked stage, one copy.
+ * Either way each call waits for its reads of the caller's rows before it returns. */
+enum { WG_ROWS_AUTO = 0, WG_ROWS_PACKED = 1 };
+wg_status wg_dropin_set_rows(int32_t rows_mode);
 /* Step counter of the drop-in (the reference's `static long time`, wave_billiard.c:310). */
 wg_status wg_dropin_get_time(int64_t *t);
 wg_status wg_dropin_set_time(int64_t t);

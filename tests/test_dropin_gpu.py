@@ -121,3 +121,55 @@ def test_bad_records_rejected():
     rf = W.RowFields(p, f["phi"], f["psi"], f["tmp"], xy, f["tcc"], f["tc"], f["tgamma"])
     with pytest.raises(W.WaveGpuError):
         W.evolve_wave(rf, nbc=bad)
+
+
+class _ScatteredRows:
+    """Row arrays whose rows are separate allocations starting 8 bytes past a 16-byte
+    boundary (as rows from a general allocator may), for the row transfers' element path."""
+
+    def __init__(self, rf):
+        import ctypes
+        self.rf = rf
+        self._keep, self._r = [], {}
+        for name in ("phi", "psi", "tmp", "xy", "tcc", "tc", "tgamma"):
+            a = getattr(rf, name)
+            rows = []
+            for i in range(a.shape[0]):
+                buf = np.zeros(a.shape[1] + 16, a.dtype)
+                k = next(k for k in range(16) if (buf.ctypes.data + k * a.itemsize) % 16 == 8)
+                v = buf[k:k + a.shape[1]]
+                v[:] = a[i]
+                rows.append(v)
+            self._keep.append(rows)
+            ptrs = (ctypes.c_void_p * len(rows))(*[r.ctypes.data for r in rows])
+            self._r[name] = (ctypes.cast(ptrs, W._PP), ptrs, rows)
+
+    def rows(self, name):
+        return self._r[name][0]
+
+    def field(self, name):
+        return np.stack(self._r[name][2]).reshape(-1)
+
+
+@pytest.mark.parametrize("rows_mode", [0, 1])  # WG_ROWS_AUTO (in place where the device can), WG_ROWS_PACKED
+@pytest.mark.parametrize("variant,scattered", [("s_square", False), ("s_square", True), ("s_dir", True)])
+def test_row_transfers(rows_mode, variant, scattered):
+    """Strict evolve_wave with the rows moved in place by the device or packed by host
+    threads: the oracle's fields either way, for rows of one buffer and for rows in separate
+    allocations 8 bytes off a 16-byte boundary (even NY, and odd NY = 45)."""
+    p, f, xy, nbc = variant_inputs(variant, seed=13)
+    new, prev, third, _ = oracle.run(p, f["phi"], f["psi"], f["tmp"], xy, f["tcc"], f["tc"], f["tgamma"], 9, nbc=nbc)
+    W.configure(p)
+    W.set_mode(False)
+    W.check(W.lib().wg_dropin_set_rows(rows_mode))
+    try:
+        rf = W.RowFields(p, f["phi"], f["psi"], f["tmp"], xy, f["tcc"], f["tc"], f["tgamma"])
+        target = _ScatteredRows(rf) if scattered else rf
+        for _ in range(3):
+            W.evolve_wave(target, nbc=nbc)
+        get = (lambda n: target.field(n)) if scattered else (lambda n: getattr(rf, n).reshape(-1))
+        check_close(get("phi"), new, p)
+        check_close(get("psi"), prev, p)
+        check_close(get("tmp"), third, p)
+    finally:
+        W.check(W.lib().wg_dropin_set_rows(0))

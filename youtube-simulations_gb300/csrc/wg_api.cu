@@ -150,6 +150,8 @@ struct DropIn {
     DevParams dp;
     int pitch = 0;
     int mode = WG_DROPIN_STRICT;
+    int rows_mode = WG_ROWS_AUTO;
+    int pageable = -1;           // the device addresses pageable host memory (-1: not asked yet)
     long long time = 0;
     cudaStream_t st = nullptr;
     double *buf[3] = {nullptr, nullptr, nullptr};
@@ -198,7 +200,61 @@ static wg_status di_stage(size_t bytes)
     return WG_OK;
 }
 
-// rows (NX pointers to NY values) -> pitched device array, through pinned staging
+// Rows read and written in place by the device: one block per row, 16-byte accesses where
+// the row and its byte count allow (a pitched row starts on 512 bytes), the padding zeroed.
+// Only on devices that address pageable host memory with the host's page tables.
+template <class E>
+__global__ void k_rows_in(const E *const *__restrict__ rows, int nx, int ny, int pitch, E *__restrict__ dst)
+{
+    const int i = blockIdx.x;
+    if (i >= nx) return;
+    const E *r = rows[i];
+    E *d = dst + (size_t)i * pitch;
+    const size_t rb = (size_t)ny * sizeof(E);
+    if (((uintptr_t)r & 15) == 0 && rb % 16 == 0) {
+        const int4 *s4 = reinterpret_cast<const int4 *>(r);
+        int4 *d4 = reinterpret_cast<int4 *>(d);
+        for (size_t k = threadIdx.x; k < rb / 16; k += blockDim.x) d4[k] = s4[k];
+    } else {
+        for (int j = threadIdx.x; j < ny; j += blockDim.x) d[j] = r[j];
+    }
+    for (int j = ny + threadIdx.x; j < pitch; j += blockDim.x) d[j] = E(0);
+}
+__global__ void k_rows_out(double *const *__restrict__ rows, int nx, int ny, int pitch, const double *__restrict__ src)
+{
+    const int i = blockIdx.x;
+    if (i >= nx) return;
+    double *r = rows[i];
+    const double *s = src + (size_t)i * pitch;
+    const size_t rb = (size_t)ny * sizeof(double);
+    if (((uintptr_t)r & 15) == 0 && rb % 16 == 0) {
+        const int4 *s4 = reinterpret_cast<const int4 *>(s);
+        int4 *d4 = reinterpret_cast<int4 *>(r);
+        for (size_t k = threadIdx.x; k < rb / 16; k += blockDim.x) d4[k] = s4[k];
+    } else {
+        for (int j = threadIdx.x; j < ny; j += blockDim.x) r[j] = s[j];
+    }
+}
+
+// the rows go in place: asked for, and the device addresses pageable host memory through
+// the host's page tables
+static bool di_in_place()
+{
+    if (g_di.rows_mode != WG_ROWS_AUTO) return false;
+    if (g_di.pageable < 0) {
+        int dev = 0, a = 0, b = 0;
+        if (cudaGetDevice(&dev) != cudaSuccess ||
+            cudaDeviceGetAttribute(&a, cudaDevAttrPageableMemoryAccess, dev) != cudaSuccess ||
+            cudaDeviceGetAttribute(&b, cudaDevAttrPageableMemoryAccessUsesHostPageTables, dev) != cudaSuccess) {
+            cudaGetLastError();
+            a = b = 0;
+        }
+        g_di.pageable = (a == 1 && b == 1) ? 1 : 0;
+    }
+    return g_di.pageable == 1;
+}
+
+// rows (NX pointers to NY values) -> pitched device array, in place or through pinned staging
 // Row copies between the caller's row arrays and the pinned stage, split over up to 8
 // host threads (one thread copies at well under the host link's rate: 43 against 12.5 ms
 // per strict evolve_wave on config 2; 16 threads and a second stage measured the same);
@@ -238,6 +294,14 @@ static wg_status di_upload_rows(E **rows, E *dev)
     if (s) return s;
     for (int i = 0; i < nx; i++)
         if (!rows[i]) { set_error("row %d is NULL", i); return WG_ERR_INVALID; }
+    if (di_in_place()) {
+        // the kernel reads the caller's row table and rows; the call waits for it, so the
+        // rows may change (or go) as soon as it returns
+        k_rows_in<E><<<nx, 256, 0, g_di.st>>>(rows, nx, ny, P, dev);
+        WG_CUDA(cudaGetLastError());
+        WG_CUDA(cudaStreamSynchronize(g_di.st));
+        return WG_OK;
+    }
     WG_CUDA(cudaStreamSynchronize(g_di.st));  // staging may still feed an earlier copy
     E *h = (E *)g_di.hstage;
     par_rows(nx, [&](int a, int b) {
@@ -254,6 +318,14 @@ static wg_status di_download_rows(double *dev, double **rows)
 {
     const int nx = g_di.prm.nx, ny = g_di.prm.ny, P = g_di.pitch;
     const size_t bytes = (size_t)nx * P * sizeof(double);
+    if (di_in_place()) {
+        for (int i = 0; i < nx; i++)
+            if (!rows[i]) { set_error("row %d is NULL", i); return WG_ERR_INVALID; }
+        k_rows_out<<<nx, 256, 0, g_di.st>>>(rows, nx, ny, P, dev);
+        WG_CUDA(cudaGetLastError());
+        WG_CUDA(cudaStreamSynchronize(g_di.st));
+        return WG_OK;
+    }
     wg_status s = di_stage(bytes);
     if (s) return s;
     WG_CUDA(cudaMemcpyAsync(g_di.hstage, dev, bytes, cudaMemcpyDeviceToHost, g_di.st));
@@ -443,6 +515,17 @@ wg_status wg_dropin_set_mode(int32_t mode)
     g_di.statics_valid = false;
     g_di.energy_statics_valid = false;
     g_di.rec_key = nullptr;
+    return WG_OK;
+}
+
+wg_status wg_dropin_set_rows(int32_t rows_mode)
+{
+    std::lock_guard<std::mutex> lk(g_di_mu);
+    if (rows_mode != WG_ROWS_AUTO && rows_mode != WG_ROWS_PACKED) {
+        set_error("unknown rows mode %d", rows_mode);
+        return WG_ERR_INVALID;
+    }
+    g_di.rows_mode = rows_mode;
     return WG_OK;
 }
 

@@ -48,6 +48,7 @@ SIGNATURES = {
     "wg_params_default": (None, [_V, _I32, _I32]),
     "wg_dropin_configure": (_I32, [_V]),
     "wg_dropin_set_mode": (_I32, [_I32]),
+    "wg_dropin_set_rows": (_I32, [_I32]),
     "wg_dropin_sync": (_I32, []),
     "wg_dropin_invalidate": (_I32, []),
     "wg_dropin_get_time": (_I32, [ctypes.POINTER(_I64)]),
