@@ -371,7 +371,9 @@ def run_ours(args):
                              bytes_per_update=bytes_per_cell_update(prec, "table"), energies=energies)
     accuracy = run_accuracy(args, P, W, sc, stream) if (rank == 0 and not args.no_accuracy) else None
 
-    # end to end through the C ABI with pinned host buffers (FP32)
+    # end to end through the C ABI with page-locked host buffers (FP32): every step moves
+    # the state in and out over the host link (the library's forming kernels read and
+    # write these buffers in place)
     s = make_scene("fp32")
     h_phi = torch.empty(CELLS, dtype=torch.float32).pin_memory()
     h_psi = torch.empty(CELLS, dtype=torch.float32).pin_memory()
